@@ -1,0 +1,232 @@
+"""GB300-native meshless Voronoi/Laguerre cell engine.
+
+A drop-in for geogram's meshless cell path.  The Python surface mirrors the
+reference's C++ one:
+
+  NearestNeighborSearch   points/nn_search.h:69-262 (set_points,
+                          get_nearest_neighbors by point or by index)
+  compute_cells           the results of VBW::ConvexCell for every seed
+                          (volume, compute_mg, v_global_index, facet_area;
+                          voronoi/convex_cell.h:768-830), clipped until the
+                          security radius certifies them (generic_RVD.h:
+                          2278-2352)
+  lloyd_step / lloyd_iterations
+                          CentroidalVoronoiTesselation::Lloyd_iterations
+                          (voronoi/CVT.cpp:133-167) on meshless cells
+
+Everything runs on the GPU through libgbv.so (C ABI in include/gbv.h).
+Host arrays are numpy; device arrays are torch CUDA tensors.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from ._lib import (CELL_ALL_NEIGHBOURS, CELL_CERTIFIED, CELL_DUPLICATE, PRECISION_FP32_RECHECK,
+                   PRECISION_FP64, CellOptions, CellReport, GbvError)
+
+__all__ = [
+    "Context", "NearestNeighborSearch", "Cells", "compute_cells", "lloyd_step",
+    "lloyd_iterations", "GbvError", "CELL_CERTIFIED", "CELL_ALL_NEIGHBOURS", "CELL_DUPLICATE",
+    "PRECISION_FP64", "PRECISION_FP32_RECHECK", "cell_options",
+]
+
+
+class Context:
+    """One GPU context (a CUDA stream plus the device buffers)."""
+
+    def __init__(self, device: int = 0):
+        self._lib = _lib.load()
+        h = ctypes.c_void_p()
+        _lib.check(self._lib.gbv_create(int(device), ctypes.byref(h)))
+        self.handle = h
+        self.device = device
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            self._lib.gbv_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+_default_ctx: Context | None = None
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+def cell_options(box=((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)), k0: int = 20, check_sr: bool = True,
+                 precision: str | int = "fp64") -> CellOptions:
+    o = CellOptions()
+    _lib.load().gbv_cell_options_default(ctypes.byref(o))
+    for c in range(3):
+        o.box_min[c] = float(box[0][c])
+        o.box_max[c] = float(box[1][c])
+    o.k0 = int(k0)
+    o.check_sr = 1 if check_sr else 0
+    if isinstance(precision, str):
+        precision = {"fp64": PRECISION_FP64, "fp32": PRECISION_FP32_RECHECK,
+                     "fp32_recheck": PRECISION_FP32_RECHECK}[precision]
+    o.precision = int(precision)
+    return o
+
+
+class NearestNeighborSearch:
+    """GEO::NearestNeighborSearch on the GPU (points/nn_search.h:69-262).
+
+    The reference's kd-tree stores a pointer to the caller's points
+    (kd_tree.cpp:121-126); here the points are copied to the GPU by
+    set_points, so the caller's array may be released afterwards.
+    """
+
+    def __init__(self, dimension: int = 3, ctx: Context | None = None):
+        if dimension not in (3, 4):
+            raise ValueError("dimension must be 3 or 4")
+        self.dimension = dimension
+        self.ctx = ctx or default_context()
+        self.nb_points = 0
+
+    def stride_supported(self) -> bool:
+        return True
+
+    def set_points(self, points: np.ndarray, stride: int | None = None) -> None:
+        pts = np.ascontiguousarray(points, dtype=np.float64)
+        if stride is None:
+            pts = pts.reshape(-1, self.dimension)
+            stride = self.dimension
+        n = pts.size // stride
+        _lib.check(self.ctx._lib.gbv_nn_set_points(self.ctx.handle, n, _lib.ptr(pts),
+                                                   self.dimension, stride))
+        self.nb_points = n
+
+    def get_nearest_neighbors(self, k: int, query: np.ndarray):
+        """k nearest stored points of each query row: (idx, d2), ascending."""
+        q = np.ascontiguousarray(query, dtype=np.float64).reshape(-1, self.dimension)
+        idx = np.empty((len(q), k), np.uint32)
+        d2 = np.empty((len(q), k), np.float64)
+        _lib.check(self.ctx._lib.gbv_nn_get_nearest_neighbors(
+            self.ctx.handle, len(q), _lib.ptr(q), k, _lib.ptr(idx), _lib.ptr(d2)))
+        return idx, d2
+
+    def get_nearest_neighbors_by_index(self, k: int):
+        """k nearest of every stored point, the point itself first (d2=0)."""
+        idx = np.empty((self.nb_points, k), np.uint32)
+        d2 = np.empty((self.nb_points, k), np.float64)
+        _lib.check(self.ctx._lib.gbv_nn_get_nearest_neighbors_all(
+            self.ctx.handle, k, _lib.ptr(idx), _lib.ptr(d2)))
+        return idx, d2
+
+
+@dataclass
+class Cells:
+    """Per-seed results, in the caller's seed order.
+
+    volume[i]   ConvexCell::volume()
+    mg[i]       ConvexCell::compute_mg() (volume-weighted centroid)
+    rowptr, neighbors, facet_area: CSR of the facets shared with other
+                seeds, v_global_index(v) and facet_area(v) in the
+                reference's order (clipping order)
+    status[i]   CELL_CERTIFIED / CELL_ALL_NEIGHBOURS / CELL_DUPLICATE
+    """
+    volume: np.ndarray
+    mg: np.ndarray
+    rowptr: np.ndarray
+    neighbors: np.ndarray
+    facet_area: np.ndarray
+    status: np.ndarray
+    report: dict = field(default_factory=dict)
+
+    def barycenter(self) -> np.ndarray:
+        """ConvexCell::barycenter (convex_cell.cpp:1255-1265): mg/m, 0-safe."""
+        m = self.volume[:, None]
+        return np.where(m != 0.0, self.mg / np.where(m != 0.0, m, 1.0), self.mg)
+
+    def neighbors_of(self, i: int):
+        a, b = self.rowptr[i], self.rowptr[i + 1]
+        return self.neighbors[a:b], self.facet_area[a:b]
+
+
+def compute_cells(xyz: np.ndarray, weights: np.ndarray | None = None, *,
+                  box=((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)), k0: int = 20, check_sr: bool = True,
+                  precision: str | int = "fp64", ctx: Context | None = None) -> Cells:
+    """Certified Laguerre cells of the seeds xyz (n x 3) with weights (n)."""
+    ctx = ctx or default_context()
+    x = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+    n = len(x)
+    w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float64).reshape(n)
+    o = cell_options(box, k0, check_sr, precision)
+    rep = CellReport()
+    L = ctx._lib
+    _lib.check(L.gbv_cells_compute(ctx.handle, _lib.ptr(x), _lib.ptr(w), n, ctypes.byref(o),
+                                   ctypes.byref(rep)))
+    vol = np.empty(n)
+    mg = np.empty((n, 3))
+    rowptr = np.empty(n + 1, np.uint32)
+    nbr = np.empty(max(rep.nnz, 1), np.uint32)
+    area = np.empty(max(rep.nnz, 1))
+    status = np.empty(n, np.int32)
+    _lib.check(L.gbv_cells_fetch(ctx.handle, _lib.ptr(vol), _lib.ptr(mg), _lib.ptr(rowptr),
+                                 _lib.ptr(nbr), _lib.ptr(area), _lib.ptr(status)))
+    return Cells(vol, mg, rowptr, nbr[:rep.nnz], area[:rep.nnz], status, rep.as_dict())
+
+
+def compute_cells_device(xyz, weights=None, *, box=((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)),
+                         k0: int = 20, check_sr: bool = True, precision="fp64",
+                         stream=None, ctx: Context | None = None) -> dict:
+    """Same on torch CUDA tensors (float64, n x 3 and n); results stay on
+    the device (read them with device_results)."""
+    ctx = ctx or default_context()
+    n = xyz.shape[0]
+    o = cell_options(box, k0, check_sr, precision)
+    rep = CellReport()
+    st = ctypes.c_void_p(stream.cuda_stream) if stream is not None else None
+    _lib.check(ctx._lib.gbv_cells_compute_device(ctx.handle, _lib.ptr(xyz), _lib.ptr(weights), n,
+                                                 ctypes.byref(o), st, ctypes.byref(rep)))
+    return rep.as_dict()
+
+
+def lloyd_step(xyz: np.ndarray, weights: np.ndarray | None = None, *,
+               box=((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)), precision="fp64",
+               ctx: Context | None = None) -> tuple[np.ndarray, dict]:
+    """One Lloyd iteration (CVT.cpp:133-167): returns the moved seeds."""
+    ctx = ctx or default_context()
+    x = np.array(xyz, dtype=np.float64, copy=True).reshape(-1, 3)
+    n = len(x)
+    w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float64).reshape(n)
+    o = cell_options(box, 20, True, precision)
+    rep = CellReport()
+    _lib.check(ctx._lib.gbv_lloyd_step(ctx.handle, _lib.ptr(x), _lib.ptr(w), n, ctypes.byref(o),
+                                       ctypes.byref(rep)))
+    return x, rep.as_dict()
+
+
+def lloyd_iterations(xyz_dev, iters: int, weights_dev=None, *,
+                     box=((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)), precision="fp64", stream=None,
+                     ctx: Context | None = None) -> dict:
+    """`iters` Lloyd iterations in place on a torch CUDA tensor (n x 3)."""
+    ctx = ctx or default_context()
+    o = cell_options(box, 20, True, precision)
+    rep = CellReport()
+    st = ctypes.c_void_p(stream.cuda_stream) if stream is not None else None
+    _lib.check(ctx._lib.gbv_lloyd_device(ctx.handle, _lib.ptr(xyz_dev), _lib.ptr(weights_dev),
+                                         xyz_dev.shape[0], iters, ctypes.byref(o), st,
+                                         ctypes.byref(rep)))
+    return rep.as_dict()

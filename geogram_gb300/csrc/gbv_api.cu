@@ -1,0 +1,795 @@
+// C ABI of the cell engine: context, device buffers and the passes that
+// take every seed to a certified cell.
+//
+// A compute call runs, on the context's stream:
+//   1. build_grid: bounding box, counting sort of the seeds by Morton cell;
+//   2. kNN with a list of 64 (or k0 without the security radius);
+//   3. the clipping kernel over all cells (FP64, or FP32 + FP64 geometry);
+//   4. the cells FP32 could not certify: FP64 clipping with the same lists;
+//   5. cells that overflowed the small capacity: the large FP64 kernel;
+//   6. cells whose list ran out before certification: a longer list (x4,
+//      up to n - 1) for those cells only, then 4-5 again on them;
+//   7. unsort into the caller's order and compact the facets into CSR.
+// Steps 4-6 are the security-radius growth of generic_RVD.h:2278-2352:
+// since a certified cell does not depend on how long the list was, growing
+// the list of the few uncertified cells gives the reference's result.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "gbv_clip.cuh"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+gbv_status fail(gbv_status st, const std::string& msg) {
+  g_last_error = msg;
+  return st;
+}
+
+struct CudaError {
+  cudaError_t e;
+  std::string where;
+};
+
+#define GBV_CUDA(call)                                                     \
+  do {                                                                     \
+    cudaError_t e_ = (call);                                               \
+    if (e_ != cudaSuccess) throw CudaError{e_, #call};                     \
+  } while (0)
+
+struct StatusError {
+  gbv_status st;
+  std::string msg;
+};
+
+}  // namespace
+
+struct gbv_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[8] = {};
+  std::map<std::string, std::pair<void*, size_t>> bufs;
+
+  gbv::SortedSeeds S;
+  gbv::GridScratch scr;
+  unsigned long long* counters = nullptr;  // [0] exact calls [1] max clips
+  uint32_t* list_counts = nullptr;         // [4] classification counters
+  uint32_t* h_counts = nullptr;            // pinned mirror
+
+  // last cell results, caller order
+  uint32_t n = 0;
+  uint64_t nnz = 0;
+  bool has_cells = false;
+  double* vol = nullptr;
+  double* mg = nullptr;
+  uint32_t* rowptr = nullptr;
+  uint32_t* nbr = nullptr;
+  double* area = nullptr;
+  int32_t* status = nullptr;
+
+  // nearest-neighbour search state
+  bool nn_ready = false;
+  uint32_t nn_n = 0, nn_dim = 3;
+
+  template <class T>
+  T* buf(const std::string& name, size_t count) {
+    size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
+    auto it = bufs.find(name);
+    if (it != bufs.end() && it->second.second >= bytes) return (T*)it->second.first;
+    if (it != bufs.end()) {
+      GBV_CUDA(cudaFree(it->second.first));
+      bufs.erase(it);
+    }
+    void* p = nullptr;
+    GBV_CUDA(cudaMalloc(&p, bytes));
+    bufs[name] = {p, bytes};
+    return (T*)p;
+  }
+};
+
+namespace gbv {
+
+// ---------------------------------------------------------------------
+// Small kernels of the orchestration
+// ---------------------------------------------------------------------
+
+// Collects the queries of a pass whose cell ended with one of the three
+// retry statuses, with the list row each used.
+__global__ void classify_kernel(const uint32_t* __restrict__ qlist,
+                                const uint32_t* __restrict__ qrow, uint32_t nq,
+                                const int32_t* __restrict__ status, uint32_t* __restrict__ counts,
+                                uint32_t* __restrict__ recheck_s, uint32_t* __restrict__ recheck_r,
+                                uint32_t* __restrict__ over_s, uint32_t* __restrict__ over_r,
+                                uint32_t* __restrict__ morek_s, uint32_t* __restrict__ err_s) {
+  const uint32_t qi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (qi >= nq) return;
+  const uint32_t s = qlist ? qlist[qi] : qi;
+  const uint32_t r = qrow ? qrow[qi] : qi;
+  const int32_t st = status[s];
+  if (st == CELL_RECHECK) {
+    uint32_t k = atomicAdd(&counts[0], 1u);
+    recheck_s[k] = s;
+    recheck_r[k] = r;
+  } else if (st == CELL_OVERFLOW) {
+    uint32_t k = atomicAdd(&counts[1], 1u);
+    over_s[k] = s;
+    over_r[k] = r;
+  } else if (st == CELL_NEED_MORE_K) {
+    uint32_t k = atomicAdd(&counts[2], 1u);
+    morek_s[k] = s;
+  } else if (st == CELL_ERROR) {
+    uint32_t k = atomicAdd(&counts[3], 1u);
+    if (k == 0) err_s[0] = s;
+  }
+}
+
+__global__ void facet_count_kernel(const uint32_t* __restrict__ slot_of,
+                                   const uint32_t* __restrict__ nf, uint32_t n,
+                                   uint32_t* __restrict__ rowptr) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) rowptr[i] = nf[slot_of[i]];
+  if (i == n) rowptr[n] = 0;
+}
+
+// Unsorts the per-cell results into the caller's order and writes the CSR.
+__global__ void unsort_kernel(const uint32_t* __restrict__ slot_of, uint32_t n,
+                              const double* __restrict__ vol_s, const double* __restrict__ mg_s,
+                              const int32_t* __restrict__ st_s, const uint32_t* __restrict__ nf,
+                              const uint32_t* __restrict__ f_nbr,
+                              const double* __restrict__ f_area,
+                              const uint32_t* __restrict__ rowptr, double* __restrict__ vol,
+                              double* __restrict__ mg, int32_t* __restrict__ status,
+                              uint32_t* __restrict__ nbr, double* __restrict__ area) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t s = slot_of[i];
+  vol[i] = vol_s[s];
+  mg[3 * (size_t)i] = mg_s[s];
+  mg[3 * (size_t)i + 1] = mg_s[(size_t)n + s];
+  mg[3 * (size_t)i + 2] = mg_s[2 * (size_t)n + s];
+  status[i] = st_s[s];
+  const uint32_t b = rowptr[i], c = nf[s];
+  for (uint32_t f = 0; f < c; ++f) {
+    nbr[b + f] = f_nbr[(size_t)f * n + s];
+    area[b + f] = f_area[(size_t)f * n + s];
+  }
+}
+
+// Compensated (Neumaier) FP64 sum, deterministic: fixed partition into
+// blocks, fixed order inside each block, then one block over the partials.
+constexpr int kSumThreads = 256;
+
+__device__ __forceinline__ void neumaier_add(double& s, double& c, double x) {
+  const double t = s + x;
+  if (fabs(s) >= fabs(x)) c += (s - t) + x;
+  else c += (x - t) + s;
+  s = t;
+}
+
+__global__ void sum_partial_kernel(const double* __restrict__ x, size_t n,
+                                   double* __restrict__ part) {
+  __shared__ double ss[kSumThreads], sc[kSumThreads];
+  double s = 0.0, c = 0.0;
+  const size_t chunk = (n + gridDim.x - 1) / gridDim.x;
+  const size_t b = blockIdx.x * chunk, e = min(n, b + chunk);
+  for (size_t i = b + threadIdx.x; i < e; i += kSumThreads) neumaier_add(s, c, x[i]);
+  ss[threadIdx.x] = s;
+  sc[threadIdx.x] = c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double S = 0.0, C = 0.0;
+    for (int t = 0; t < kSumThreads; ++t) {
+      neumaier_add(S, C, ss[t]);
+      C += sc[t];
+    }
+    part[2 * blockIdx.x] = S;
+    part[2 * blockIdx.x + 1] = C;
+  }
+}
+
+__global__ void sum_final_kernel(const double* __restrict__ part, int np, double* __restrict__ out) {
+  if (threadIdx.x != 0) return;
+  double S = 0.0, C = 0.0;
+  for (int b = 0; b < np; ++b) {
+    neumaier_add(S, C, part[2 * b]);
+    C += part[2 * b + 1];
+  }
+  out[0] = S + C;
+}
+
+__global__ void sum_u32_kernel(const uint32_t* __restrict__ x, size_t n,
+                               unsigned long long* __restrict__ out) {
+  unsigned long long s = 0;
+  for (size_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    s += x[i];
+  s = __reduce_add_sync(0xFFFFFFFFu, (unsigned)min(s, 0xFFFFFFFFull)) ;
+  if ((threadIdx.x & 31) == 0) atomicAdd(out, s);
+}
+
+// Lloyd update (CVT.cpp:150-160): x_i <- mg_i / m_i when m_i > 1e-30.
+__global__ void lloyd_update_kernel(double* __restrict__ xyz, const double* __restrict__ vol,
+                                    const double* __restrict__ mg, uint32_t n) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double m = vol[i];
+  if (m > 1e-30) {
+    xyz[3 * (size_t)i] = mg[3 * (size_t)i] / m;
+    xyz[3 * (size_t)i + 1] = mg[3 * (size_t)i + 1] / m;
+    xyz[3 * (size_t)i + 2] = mg[3 * (size_t)i + 2] / m;
+  }
+}
+
+__global__ void to_query4_kernel(const double* __restrict__ q, uint32_t nq, uint32_t dim,
+                                 double4* __restrict__ out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nq) return;
+  out[i] = make_double4(q[(size_t)i * dim], q[(size_t)i * dim + 1], q[(size_t)i * dim + 2],
+                        dim == 4 ? q[(size_t)i * dim + 3] : 0.0);
+}
+
+// ---------------------------------------------------------------------
+// Host helpers
+// ---------------------------------------------------------------------
+
+static void setup_seeds(gbv_context* c, uint32_t n, bool weighted) {
+  const int L = choose_levels(n);
+  SortedSeeds& S = c->S;
+  S.xd = c->buf<double4>("xd", n);
+  S.q = c->buf<double>("q", n);
+  S.xf = c->buf<float4>("xf", n);
+  S.ws = weighted ? c->buf<double>("ws", n) : nullptr;
+  S.perm = c->buf<uint32_t>("perm", n);
+  S.slot_of = c->buf<uint32_t>("slot_of", n);
+  S.cell_start = c->buf<uint32_t>("cell_start", ((size_t)1 << (3 * L)) + 1);
+  S.gd = c->buf<GridDesc>("gd", 1);
+  S.aux = c->buf<double>("aux", 4);
+  S.L = L;
+  c->scr.cid = c->buf<uint32_t>("cid", n);
+  c->scr.rank = c->buf<uint32_t>("rank", n);
+  c->scr.scan_tmp_elems = scan_tmp_elems(((size_t)1 << (3 * L)) + 1);
+  c->scr.scan_tmp = c->buf<uint32_t>("scan_tmp", c->scr.scan_tmp_elems);
+  c->scr.red = c->buf<double>("red", 8 * 128);
+}
+
+static inline unsigned nblocks(size_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+struct CellsTiming {
+  float grid = 0, knn = 0, clip = 0, total = 0;
+};
+
+// The whole cell computation on device inputs.
+static void cells_device(gbv_context* c, const double* d_xyz, const double* d_w, uint32_t n,
+                         const gbv_cell_options& o, cudaStream_t st, gbv_cell_report* rep) {
+  if (n == 0) throw StatusError{GBV_ERR_INVALID_ARGUMENT, "n must be > 0"};
+  const bool fp32 = o.precision == GBV_PRECISION_FP32_RECHECK;
+  setup_seeds(c, n, d_w != nullptr);
+  c->nn_ready = false;
+  SortedSeeds& S = c->S;
+  GBV_CUDA(cudaEventRecord(c->ev[0], st));
+  build_grid(d_xyz, 3, 3, d_w, n, S.L, S, c->scr, st);
+  GBV_CUDA(cudaEventRecord(c->ev[1], st));
+
+  // outputs by slot
+  int32_t* status_s = c->buf<int32_t>("status_s", n);
+  double* vol_s = c->buf<double>("vol_s", n);
+  double* mg_s = c->buf<double>("mg_s", 3 * (size_t)n);
+  uint32_t* nf = c->buf<uint32_t>("nf", n);
+  uint32_t* nclip = c->buf<uint32_t>("nclip", n);
+  uint32_t* f_nbr = c->buf<uint32_t>("f_nbr", (size_t)kMaxFacets * n);
+  double* f_area = c->buf<double>("f_area", (size_t)kMaxFacets * n);
+  GBV_CUDA(cudaMemsetAsync(c->counters, 0, 2 * sizeof(unsigned long long), st));
+
+  // first pass
+  const uint32_t nm1 = n > 1 ? n - 1 : 0;
+  uint32_t K = o.check_sr ? std::min<uint32_t>(kKnnSmemK, nm1)
+                          : std::min<uint32_t>(o.k0, nm1);
+  if (K > kKnnSmemK) K = kKnnSmemK;  // longer first lists: see the retry pass
+  uint32_t* knn = c->buf<uint32_t>("knn", (size_t)std::max<uint32_t>(K, 1) * n);
+  uint32_t* kcnt = c->buf<uint32_t>("kcnt", n);
+  {
+    KnnArgs ka{};
+    ka.S = &S;
+    ka.nq = n;
+    ka.k = K;
+    ka.mode = KNN_CELLS;
+    ka.nbr = knn;
+    ka.out_stride = n;
+    ka.cnt = kcnt;
+    if (K > 0) launch_knn(ka, st);
+    else GBV_CUDA(cudaMemsetAsync(kcnt, 0, sizeof(uint32_t) * n, st));
+  }
+  GBV_CUDA(cudaEventRecord(c->ev[2], st));
+
+  ClipArgs base{};
+  base.S = S;
+  base.n_total = n;
+  for (int k = 0; k < 3; ++k) {
+    base.box[k] = o.box_min[k];
+    base.box[3 + k] = o.box_max[k];
+  }
+  base.check_sr = o.check_sr ? 1 : 0;
+  base.status = status_s;
+  base.vol = vol_s;
+  base.mg = mg_s;
+  base.nf = nf;
+  base.nclip = nclip;
+  base.f_nbr = f_nbr;
+  base.f_area = f_area;
+  base.out_stride = n;
+  base.counters = c->counters;
+
+  ClipArgs a = base;
+  a.nbr = knn;
+  a.nbr_stride = n;
+  a.nbr_cnt = kcnt;
+  a.list_k = K;
+  a.nq = n;
+  if (fp32) launch_clip_fp32(a, st);
+  else launch_clip_fp64(a, CLIP_SMALL, st);
+  GBV_CUDA(last_launch_error);
+  GBV_CUDA(cudaEventRecord(c->ev[5], st));
+
+  uint32_t* rs = c->buf<uint32_t>("recheck_s", n);
+  uint32_t* rr = c->buf<uint32_t>("recheck_r", n);
+  uint32_t* os = c->buf<uint32_t>("over_s", n);
+  uint32_t* orw = c->buf<uint32_t>("over_r", n);
+  uint32_t* ms = c->buf<uint32_t>("morek_s", n);
+  uint32_t* es = c->buf<uint32_t>("err_s", 1);
+  uint32_t n_recheck = 0, n_over = 0, n_morek = 0;
+
+  // classify the queries of a finished pass; returns the three counts
+  auto classify = [&](const uint32_t* ql, const uint32_t* qr, uint32_t nq, uint32_t out[4]) {
+    GBV_CUDA(cudaMemsetAsync(c->list_counts, 0, 4 * sizeof(uint32_t), st));
+    classify_kernel<<<nblocks(nq, 256), 256, 0, st>>>(ql, qr, nq, status_s, c->list_counts, rs,
+                                                      rr, os, orw, ms, es);
+    GBV_CUDA(cudaMemcpyAsync(c->h_counts, c->list_counts, 4 * sizeof(uint32_t),
+                             cudaMemcpyDeviceToHost, st));
+    GBV_CUDA(cudaStreamSynchronize(st));
+    for (int k = 0; k < 4; ++k) out[k] = c->h_counts[k];
+    if (out[3]) {
+      throw StatusError{GBV_ERR_STATE, "inconsistent polytope in " + std::to_string(out[3]) +
+                                           " cell(s) (conflict zone not a disk)"};
+    }
+  };
+
+  // Runs the FP64 fixes of a finished pass whose lists are given: cells
+  // FP32 could not certify are re-clipped in FP64, cells that overflowed
+  // the small capacity run the large kernel.  Returns the number of cells
+  // that still need a longer list; their slots are in "morek_acc".
+  auto fix_pass = [&](const uint32_t* lists, uint32_t stride, const uint32_t* cnts,
+                      uint32_t listk, const uint32_t* ql, const uint32_t* qr,
+                      uint32_t nq) -> uint32_t {
+    uint32_t* mk_acc = c->buf<uint32_t>("morek_acc", n);
+    uint32_t* rc_s = c->buf<uint32_t>("rc_s", n);
+    uint32_t* rc_r = c->buf<uint32_t>("rc_r", n);
+    uint32_t* ov_s = c->buf<uint32_t>("ov_s", n);
+    uint32_t* ov_r = c->buf<uint32_t>("ov_r", n);
+    uint32_t nmk = 0, nrc = 0, nov = 0;
+    auto append = [&](uint32_t* dst, uint32_t at, const uint32_t* src, uint32_t cnt) {
+      if (cnt) GBV_CUDA(cudaMemcpyAsync(dst + at, src, cnt * sizeof(uint32_t),
+                                        cudaMemcpyDeviceToDevice, st));
+    };
+    auto clip_list = [&](const uint32_t* ls, const uint32_t* lr, uint32_t cnt, int shape) {
+      ClipArgs b = base;
+      b.nbr = lists;
+      b.nbr_stride = stride;
+      b.nbr_cnt = cnts;
+      b.list_k = listk;
+      b.qlist = ls;
+      b.qrow = lr;
+      b.nq = cnt;
+      launch_clip_fp64(b, shape, st);
+      GBV_CUDA(last_launch_error);
+    };
+    uint32_t c1[4];
+    classify(ql, qr, nq, c1);
+    append(rc_s, 0, rs, c1[0]);
+    append(rc_r, 0, rr, c1[0]);
+    nrc = c1[0];
+    append(ov_s, 0, os, c1[1]);
+    append(ov_r, 0, orw, c1[1]);
+    nov = c1[1];
+    append(mk_acc, 0, ms, c1[2]);
+    nmk = c1[2];
+    if (nrc) {
+      n_recheck += nrc;
+      clip_list(rc_s, rc_r, nrc, CLIP_SMALL);
+      uint32_t c2[4];
+      classify(rc_s, rc_r, nrc, c2);
+      append(ov_s, nov, os, c2[1]);
+      append(ov_r, nov, orw, c2[1]);
+      nov += c2[1];
+      append(mk_acc, nmk, ms, c2[2]);
+      nmk += c2[2];
+    }
+    if (nov) {
+      n_over += nov;
+      clip_list(ov_s, ov_r, nov, CLIP_LARGE);
+      uint32_t c3[4];
+      classify(ov_s, ov_r, nov, c3);
+      if (c3[1] || c3[0]) {
+        throw StatusError{GBV_ERR_CAPACITY,
+                          std::to_string(c3[1]) + " cell(s) exceed the large capacity (" +
+                              std::to_string(kLargeT) + " corners, " +
+                              std::to_string(kLargeP) + " planes)"};
+      }
+      append(mk_acc, nmk, ms, c3[2]);
+      nmk += c3[2];
+    }
+    return nmk;
+  };
+
+  uint32_t morek = fix_pass(knn, n, kcnt, K, nullptr, nullptr, n);
+  uint32_t listk = K;
+  while (morek > 0) {
+    n_morek += morek;
+    if (listk >= nm1) throw StatusError{GBV_ERR_STATE, "list growth did not terminate"};
+    listk = std::min<uint64_t>(nm1, (uint64_t)listk * 4);
+    uint32_t* ql = c->buf<uint32_t>("mk_q", morek);
+    GBV_CUDA(cudaMemcpyAsync(ql, c->buf<uint32_t>("morek_acc", n), morek * 4,
+                             cudaMemcpyDeviceToDevice, st));
+    uint32_t* l2 = c->buf<uint32_t>("mk_lists", (size_t)listk * morek);
+    uint32_t* c2 = c->buf<uint32_t>("mk_cnt", morek);
+    KnnArgs ka{};
+    ka.S = &S;
+    ka.nq = morek;
+    ka.qlist = ql;
+    ka.k = listk;
+    ka.mode = KNN_CELLS;
+    ka.nbr = l2;
+    ka.out_stride = morek;
+    ka.cnt = c2;
+    if (listk > kKnnSmemK) {
+      ka.gl_d2 = c->buf<double>("mk_gd2", (size_t)listk * morek);
+      ka.gl_slot = c->buf<uint32_t>("mk_gslot", (size_t)listk * morek);
+    }
+    launch_knn(ka, st);
+    ClipArgs b = base;
+    b.nbr = l2;
+    b.nbr_stride = morek;
+    b.nbr_cnt = c2;
+    b.list_k = listk;
+    b.qlist = ql;
+    b.qrow = nullptr;
+    b.nq = morek;
+    launch_clip_fp64(b, CLIP_SMALL, st);
+    GBV_CUDA(last_launch_error);
+    morek = fix_pass(l2, morek, c2, listk, ql, nullptr, morek);
+  }
+  GBV_CUDA(cudaEventRecord(c->ev[3], st));
+
+  // unsort + CSR
+  c->vol = c->buf<double>("vol", n);
+  c->mg = c->buf<double>("mg", 3 * (size_t)n);
+  c->status = c->buf<int32_t>("status", n);
+  c->rowptr = c->buf<uint32_t>("rowptr", (size_t)n + 1);
+  facet_count_kernel<<<nblocks((size_t)n + 1, 256), 256, 0, st>>>(S.slot_of, nf, n, c->rowptr);
+  uint32_t* stmp = c->buf<uint32_t>("csr_scan_tmp", scan_tmp_elems((size_t)n + 1));
+  exclusive_scan_u32(c->rowptr, (size_t)n + 1, stmp, st);
+  uint32_t nnz32 = 0;
+  GBV_CUDA(cudaMemcpyAsync(&c->h_counts[0], c->rowptr + n, 4, cudaMemcpyDeviceToHost, st));
+  GBV_CUDA(cudaStreamSynchronize(st));
+  nnz32 = c->h_counts[0];
+  c->nnz = nnz32;
+  c->nbr = c->buf<uint32_t>("nbr", std::max<uint32_t>(nnz32, 1));
+  c->area = c->buf<double>("area", std::max<uint32_t>(nnz32, 1));
+  unsort_kernel<<<nblocks(n, 256), 256, 0, st>>>(S.slot_of, n, vol_s, mg_s, status_s, nf, f_nbr,
+                                                 f_area, c->rowptr, c->vol, c->mg, c->status,
+                                                 c->nbr, c->area);
+  GBV_CUDA(cudaEventRecord(c->ev[4], st));
+  c->n = n;
+  c->has_cells = true;
+
+  if (rep) {
+    double* part = c->buf<double>("sum_part", 2 * 256);
+    double* out = c->buf<double>("sum_out", 1);
+    sum_partial_kernel<<<256, kSumThreads, 0, st>>>(c->vol, n, part);
+    sum_final_kernel<<<1, 32, 0, st>>>(part, 256, out);
+    unsigned long long* clips = c->buf<unsigned long long>("clip_sum", 1);
+    GBV_CUDA(cudaMemsetAsync(clips, 0, 8, st));
+    sum_u32_kernel<<<256, 256, 0, st>>>(nclip, n, clips);
+    double vs = 0;
+    unsigned long long cs = 0, hc[2] = {0, 0};
+    GBV_CUDA(cudaMemcpyAsync(&vs, out, 8, cudaMemcpyDeviceToHost, st));
+    GBV_CUDA(cudaMemcpyAsync(&cs, clips, 8, cudaMemcpyDeviceToHost, st));
+    GBV_CUDA(cudaMemcpyAsync(hc, c->counters, 16, cudaMemcpyDeviceToHost, st));
+    GBV_CUDA(cudaStreamSynchronize(st));
+    float t01 = 0, t12 = 0, t25 = 0, t53 = 0, t04 = 0;
+    GBV_CUDA(cudaEventElapsedTime(&t01, c->ev[0], c->ev[1]));
+    GBV_CUDA(cudaEventElapsedTime(&t12, c->ev[1], c->ev[2]));
+    GBV_CUDA(cudaEventElapsedTime(&t25, c->ev[2], c->ev[5]));
+    GBV_CUDA(cudaEventElapsedTime(&t53, c->ev[5], c->ev[3]));
+    GBV_CUDA(cudaEventElapsedTime(&t04, c->ev[0], c->ev[4]));
+    rep->nnz = c->nnz;
+    rep->n_cells = n;
+    rep->n_recheck_fp64 = n_recheck;
+    rep->n_more_k = n_morek;
+    rep->n_overflow = n_over;
+    rep->max_clips = (uint32_t)hc[1];
+    rep->knn_k = K;
+    rep->mean_clips = (double)cs / n;
+    rep->volume_sum = vs;
+    rep->ms_grid = t01;
+    rep->ms_knn = t12;
+    rep->ms_clip = t25;
+    rep->ms_retry = t53;
+    rep->n_exact = hc[0];
+    rep->ms_total = t04;
+  } else {
+    GBV_CUDA(cudaStreamSynchronize(st));
+  }
+  GBV_CUDA(cudaGetLastError());
+}
+
+template <class F>
+static gbv_status guarded(F&& f) {
+  try {
+    f();
+    return GBV_OK;
+  } catch (const CudaError& e) {
+    return fail(GBV_ERR_CUDA, e.where + ": " + cudaGetErrorString(e.e));
+  } catch (const StatusError& e) {
+    return fail(e.st, e.msg);
+  } catch (const std::exception& e) {
+    return fail(GBV_ERR_STATE, e.what());
+  }
+}
+
+static gbv_status check_opts(const gbv_cell_options* o) {
+  if (!o) return fail(GBV_ERR_INVALID_ARGUMENT, "options is NULL");
+  if (o->precision != GBV_PRECISION_FP64 && o->precision != GBV_PRECISION_FP32_RECHECK)
+    return fail(GBV_ERR_INVALID_ARGUMENT, "unknown precision");
+  for (int k = 0; k < 3; ++k)
+    if (!(o->box_max[k] > o->box_min[k])) return fail(GBV_ERR_INVALID_ARGUMENT, "empty box");
+  if (o->k0 == 0) return fail(GBV_ERR_INVALID_ARGUMENT, "k0 must be > 0");
+  return GBV_OK;
+}
+
+}  // namespace gbv
+
+using namespace gbv;
+
+extern "C" {
+
+const char* gbv_last_error(void) { return g_last_error.c_str(); }
+
+void gbv_cell_options_default(gbv_cell_options* o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  for (int k = 0; k < 3; ++k) {
+    o->box_min[k] = 0.0;
+    o->box_max[k] = 1.0;
+  }
+  o->k0 = 20;
+  o->check_sr = 1;
+  o->precision = GBV_PRECISION_FP64;
+}
+
+gbv_status gbv_create(int device, gbv_context** out) {
+  if (!out) return fail(GBV_ERR_INVALID_ARGUMENT, "out is NULL");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return fail(GBV_ERR_NO_DEVICE, "no CUDA device");
+  }
+  if (device < 0 || device >= ndev) return fail(GBV_ERR_INVALID_ARGUMENT, "bad device index");
+  gbv_context* c = new gbv_context();
+  c->device = device;
+  gbv_status st = guarded([&] {
+    GBV_CUDA(cudaSetDevice(device));
+    GBV_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    for (auto& e : c->ev) GBV_CUDA(cudaEventCreate(&e));
+    c->counters = c->buf<unsigned long long>("counters", 2);
+    c->list_counts = c->buf<uint32_t>("list_counts", 4);
+    GBV_CUDA(cudaMallocHost(&c->h_counts, 4 * sizeof(uint32_t)));
+  });
+  if (st != GBV_OK) {
+    delete c;
+    return st;
+  }
+  *out = c;
+  return GBV_OK;
+}
+
+gbv_status gbv_destroy(gbv_context* c) {
+  if (!c) return GBV_OK;
+  cudaSetDevice(c->device);
+  for (auto& kv : c->bufs) cudaFree(kv.second.first);
+  if (c->h_counts) cudaFreeHost(c->h_counts);
+  for (auto& e : c->ev)
+    if (e) cudaEventDestroy(e);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return GBV_OK;
+}
+
+gbv_status gbv_cells_compute_device(gbv_context* c, const double* d_xyz, const double* d_w,
+                                    uint32_t n, const gbv_cell_options* opt, void* stream,
+                                    gbv_cell_report* report) {
+  if (!c || !d_xyz) return fail(GBV_ERR_INVALID_ARGUMENT, "NULL argument");
+  gbv_status s = check_opts(opt);
+  if (s != GBV_OK) return s;
+  return guarded([&] {
+    GBV_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    cells_device(c, d_xyz, d_w, n, *opt, st, report);
+  });
+}
+
+gbv_status gbv_cells_compute(gbv_context* c, const double* xyz, const double* w, uint32_t n,
+                             const gbv_cell_options* opt, gbv_cell_report* report) {
+  if (!c || !xyz) return fail(GBV_ERR_INVALID_ARGUMENT, "NULL argument");
+  gbv_status s = check_opts(opt);
+  if (s != GBV_OK) return s;
+  return guarded([&] {
+    GBV_CUDA(cudaSetDevice(c->device));
+    double* dx = c->buf<double>("in_xyz", 3 * (size_t)n);
+    double* dw = w ? c->buf<double>("in_w", n) : nullptr;
+    GBV_CUDA(cudaMemcpyAsync(dx, xyz, 3 * sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+    if (w) GBV_CUDA(cudaMemcpyAsync(dw, w, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+    cells_device(c, dx, dw, n, *opt, c->stream, report);
+  });
+}
+
+gbv_status gbv_cells_fetch(gbv_context* c, double* vol, double* mg, uint32_t* rowptr,
+                           uint32_t* nbr, double* area, int32_t* status) {
+  if (!c) return fail(GBV_ERR_INVALID_ARGUMENT, "NULL context");
+  if (!c->has_cells) return fail(GBV_ERR_STATE, "no cells computed");
+  return guarded([&] {
+    GBV_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = c->stream;
+    const size_t n = c->n;
+    if (vol) GBV_CUDA(cudaMemcpyAsync(vol, c->vol, 8 * n, cudaMemcpyDeviceToHost, st));
+    if (mg) GBV_CUDA(cudaMemcpyAsync(mg, c->mg, 24 * n, cudaMemcpyDeviceToHost, st));
+    if (rowptr) GBV_CUDA(cudaMemcpyAsync(rowptr, c->rowptr, 4 * (n + 1), cudaMemcpyDeviceToHost, st));
+    if (nbr && c->nnz) GBV_CUDA(cudaMemcpyAsync(nbr, c->nbr, 4 * c->nnz, cudaMemcpyDeviceToHost, st));
+    if (area && c->nnz) GBV_CUDA(cudaMemcpyAsync(area, c->area, 8 * c->nnz, cudaMemcpyDeviceToHost, st));
+    if (status) GBV_CUDA(cudaMemcpyAsync(status, c->status, 4 * n, cudaMemcpyDeviceToHost, st));
+    GBV_CUDA(cudaStreamSynchronize(st));
+  });
+}
+
+gbv_status gbv_cells_device_results(gbv_context* c, const double** vol, const double** mg,
+                                    const uint32_t** rowptr, const uint32_t** nbr,
+                                    const double** area, const int32_t** status) {
+  if (!c) return fail(GBV_ERR_INVALID_ARGUMENT, "NULL context");
+  if (!c->has_cells) return fail(GBV_ERR_STATE, "no cells computed");
+  if (vol) *vol = c->vol;
+  if (mg) *mg = c->mg;
+  if (rowptr) *rowptr = c->rowptr;
+  if (nbr) *nbr = c->nbr;
+  if (area) *area = c->area;
+  if (status) *status = c->status;
+  return GBV_OK;
+}
+
+gbv_status gbv_lloyd_device(gbv_context* c, double* d_xyz, const double* d_w, uint32_t n,
+                            uint32_t iters, const gbv_cell_options* opt, void* stream,
+                            gbv_cell_report* report) {
+  if (!c || !d_xyz) return fail(GBV_ERR_INVALID_ARGUMENT, "NULL argument");
+  gbv_status s = check_opts(opt);
+  if (s != GBV_OK) return s;
+  return guarded([&] {
+    GBV_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    for (uint32_t it = 0; it < iters; ++it) {
+      cells_device(c, d_xyz, d_w, n, *opt, st, report);
+      lloyd_update_kernel<<<nblocks(n, 256), 256, 0, st>>>(d_xyz, c->vol, c->mg, n);
+    }
+    GBV_CUDA(cudaStreamSynchronize(st));
+  });
+}
+
+gbv_status gbv_lloyd_step(gbv_context* c, double* xyz, const double* w, uint32_t n,
+                          const gbv_cell_options* opt, gbv_cell_report* report) {
+  if (!c || !xyz) return fail(GBV_ERR_INVALID_ARGUMENT, "NULL argument");
+  gbv_status s = check_opts(opt);
+  if (s != GBV_OK) return s;
+  return guarded([&] {
+    GBV_CUDA(cudaSetDevice(c->device));
+    double* dx = c->buf<double>("lloyd_xyz", 3 * (size_t)n);
+    double* dw = w ? c->buf<double>("in_w", n) : nullptr;
+    GBV_CUDA(cudaMemcpyAsync(dx, xyz, 24 * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+    if (w) GBV_CUDA(cudaMemcpyAsync(dw, w, 8 * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+    cells_device(c, dx, dw, n, *opt, c->stream, report);
+    lloyd_update_kernel<<<nblocks(n, 256), 256, 0, c->stream>>>(dx, c->vol, c->mg, n);
+    GBV_CUDA(cudaMemcpyAsync(xyz, dx, 24 * (size_t)n, cudaMemcpyDeviceToHost, c->stream));
+    GBV_CUDA(cudaStreamSynchronize(c->stream));
+  });
+}
+
+gbv_status gbv_nn_set_points(gbv_context* c, uint32_t n, const double* pts, uint32_t dim,
+                             uint32_t stride) {
+  if (!c || !pts) return fail(GBV_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (n == 0) return fail(GBV_ERR_INVALID_ARGUMENT, "n must be > 0");
+  if (dim != 3 && dim != 4) return fail(GBV_ERR_INVALID_ARGUMENT, "dim must be 3 or 4");
+  if (stride < dim) return fail(GBV_ERR_INVALID_ARGUMENT, "stride < dim");
+  return guarded([&] {
+    GBV_CUDA(cudaSetDevice(c->device));
+    double* dp = c->buf<double>("nn_pts", (size_t)n * stride);
+    GBV_CUDA(cudaMemcpyAsync(dp, pts, sizeof(double) * (size_t)n * stride,
+                             cudaMemcpyHostToDevice, c->stream));
+    setup_seeds(c, n, false);
+    build_grid(dp, stride, dim, nullptr, n, c->S.L, c->S, c->scr, c->stream);
+    GBV_CUDA(cudaStreamSynchronize(c->stream));
+    c->nn_ready = true;
+    c->nn_n = n;
+    c->nn_dim = dim;
+    c->has_cells = false;
+  });
+}
+
+gbv_status gbv_nn_get_nearest_neighbors(gbv_context* c, uint32_t nq, const double* q, uint32_t k,
+                                        uint32_t* idx, double* d2) {
+  if (!c || !q || !idx) return fail(GBV_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (!c->nn_ready) return fail(GBV_ERR_STATE, "set_points was not called");
+  if (k == 0 || k > c->nn_n) return fail(GBV_ERR_INVALID_ARGUMENT, "need 0 < k <= n");
+  return guarded([&] {
+    GBV_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = c->stream;
+    double* dq = c->buf<double>("nn_q", (size_t)nq * c->nn_dim);
+    double4* q4 = c->buf<double4>("nn_q4", nq);
+    uint32_t* oi = c->buf<uint32_t>("nn_oi", (size_t)nq * k);
+    double* od = c->buf<double>("nn_od", (size_t)nq * k);
+    GBV_CUDA(cudaMemcpyAsync(dq, q, sizeof(double) * (size_t)nq * c->nn_dim,
+                             cudaMemcpyHostToDevice, st));
+    to_query4_kernel<<<nblocks(nq, 256), 256, 0, st>>>(dq, nq, c->nn_dim, q4);
+    KnnArgs ka{};
+    ka.S = &c->S;
+    ka.nq = nq;
+    ka.qpts = q4;
+    ka.k = k;
+    ka.mode = KNN_QUERY;
+    ka.exp_idx = oi;
+    ka.exp_d2 = od;
+    if (k > kKnnSmemK) {
+      ka.gl_d2 = c->buf<double>("nn_gd2", (size_t)k * nq);
+      ka.gl_slot = c->buf<uint32_t>("nn_gslot", (size_t)k * nq);
+    }
+    launch_knn(ka, st);
+    GBV_CUDA(cudaMemcpyAsync(idx, oi, 4 * (size_t)nq * k, cudaMemcpyDeviceToHost, st));
+    if (d2) GBV_CUDA(cudaMemcpyAsync(d2, od, 8 * (size_t)nq * k, cudaMemcpyDeviceToHost, st));
+    GBV_CUDA(cudaStreamSynchronize(st));
+    GBV_CUDA(cudaGetLastError());
+  });
+}
+
+gbv_status gbv_nn_get_nearest_neighbors_all(gbv_context* c, uint32_t k, uint32_t* idx,
+                                            double* d2) {
+  if (!c || !idx) return fail(GBV_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (!c->nn_ready) return fail(GBV_ERR_STATE, "set_points was not called");
+  if (k == 0 || k > c->nn_n) return fail(GBV_ERR_INVALID_ARGUMENT, "need 0 < k <= n");
+  return guarded([&] {
+    GBV_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = c->stream;
+    const uint32_t n = c->nn_n;
+    uint32_t* oi = c->buf<uint32_t>("nn_oi", (size_t)n * k);
+    double* od = c->buf<double>("nn_od", (size_t)n * k);
+    KnnArgs ka{};
+    ka.S = &c->S;
+    ka.nq = n;
+    ka.k = k;
+    ka.mode = KNN_ALL;
+    ka.exp_idx = oi;
+    ka.exp_d2 = od;
+    if (k > kKnnSmemK) {
+      ka.gl_d2 = c->buf<double>("nn_gd2", (size_t)k * n);
+      ka.gl_slot = c->buf<uint32_t>("nn_gslot", (size_t)k * n);
+    }
+    launch_knn(ka, st);
+    GBV_CUDA(cudaMemcpyAsync(idx, oi, 4 * (size_t)n * k, cudaMemcpyDeviceToHost, st));
+    if (d2) GBV_CUDA(cudaMemcpyAsync(d2, od, 8 * (size_t)n * k, cudaMemcpyDeviceToHost, st));
+    GBV_CUDA(cudaStreamSynchronize(st));
+    GBV_CUDA(cudaGetLastError());
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,426 @@
+// Grid build (counting sort of Morton-ordered seeds) and kNN search.
+//
+// Replaces the reference's BalancedKdTree (points/kd_tree.cpp:121-542):
+// instead of a median-split tree, seeds are counting-sorted into a uniform
+// grid whose fine cells are numbered in Morton order.  Every node of the
+// implicit octree over that grid is then a contiguous range of fine cells,
+// hence of sorted seeds, found with two loads from cell_start; the kNN
+// query is a depth-first traversal of that octree with box-distance
+// pruning (the same pruning rule as kd_tree.cpp:300,330).  Distances are
+// screened in FP32 against a conservative bound and ranked in exact FP64
+// with the reference's arithmetic, ties broken by point index.
+#include <cfloat>
+#include <cmath>
+
+#include "gbv_grid.cuh"
+
+namespace gbv {
+
+// ---------------------------------------------------------------------
+// Exclusive scan (uint32, in place), 1024 elements per block.
+// ---------------------------------------------------------------------
+constexpr int kScanThreads = 256;
+constexpr int kScanPer = 4;
+constexpr int kScanBlock = kScanThreads * kScanPer;
+
+__global__ void scan_block_kernel(uint32_t* __restrict__ data, size_t n,
+                                  uint32_t* __restrict__ sums) {
+  __shared__ uint32_t warp_tot[kScanThreads / 32];
+  const size_t base = (size_t)blockIdx.x * kScanBlock + (size_t)threadIdx.x * kScanPer;
+  uint32_t v[kScanPer];
+  uint32_t run = 0;
+#pragma unroll
+  for (int i = 0; i < kScanPer; ++i) {
+    v[i] = (base + i < n) ? data[base + i] : 0u;
+    uint32_t t = v[i];
+    v[i] = run;
+    run += t;
+  }
+  // inclusive warp scan of per-thread totals
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t x = run;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_tot[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = (lane < kScanThreads / 32) ? warp_tot[lane] : 0u;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+      if (lane >= o) w += y;
+    }
+    if (lane < kScanThreads / 32) warp_tot[lane] = w;
+  }
+  __syncthreads();
+  uint32_t off = (x - run) + (warp > 0 ? warp_tot[warp - 1] : 0u);
+#pragma unroll
+  for (int i = 0; i < kScanPer; ++i)
+    if (base + i < n) data[base + i] = v[i] + off;
+  if (threadIdx.x == kScanThreads - 1 && sums) sums[blockIdx.x] = off + run;
+}
+
+__global__ void scan_add_kernel(uint32_t* __restrict__ data, size_t n,
+                                const uint32_t* __restrict__ sums) {
+  const uint32_t add = sums[blockIdx.x];
+  const size_t base = (size_t)blockIdx.x * kScanBlock;
+  for (int i = threadIdx.x; i < kScanBlock; i += blockDim.x) {
+    size_t j = base + i;
+    if (j < n) data[j] += add;
+  }
+}
+
+size_t scan_tmp_elems(size_t n) {
+  size_t tot = 0;
+  while (n > (size_t)kScanBlock) {
+    n = (n + kScanBlock - 1) / kScanBlock;
+    tot += n + 1;
+  }
+  return tot + 1;
+}
+
+void exclusive_scan_u32(uint32_t* data, size_t n, uint32_t* tmp, cudaStream_t st) {
+  if (n == 0) return;
+  size_t nb = (n + kScanBlock - 1) / kScanBlock;
+  if (nb == 1) {
+    scan_block_kernel<<<1, kScanThreads, 0, st>>>(data, n, nullptr);
+    return;
+  }
+  uint32_t* sums = tmp;
+  scan_block_kernel<<<(unsigned)nb, kScanThreads, 0, st>>>(data, n, sums);
+  exclusive_scan_u32(sums, nb, tmp + nb + 1, st);
+  scan_add_kernel<<<(unsigned)nb, kScanThreads, 0, st>>>(data, n, sums);
+}
+
+// ---------------------------------------------------------------------
+// Bounding box, max weight
+// ---------------------------------------------------------------------
+constexpr int kRedThreads = 256;
+
+// Per-block min x,y,z / max x,y,z / max w, written to part[8*block].
+// v[6] = max w (or max |h| when dim = 4), v[7] = -min w.
+__global__ void bbox_partial_kernel(const double* __restrict__ xyz, uint32_t stride,
+                                    uint32_t dim, const double* __restrict__ w, uint32_t n,
+                                    double* __restrict__ part) {
+  double v[8] = {DBL_MAX, DBL_MAX, DBL_MAX, -DBL_MAX, -DBL_MAX, -DBL_MAX, -DBL_MAX, -DBL_MAX};
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += gridDim.x * blockDim.x) {
+    for (int c = 0; c < 3; ++c) {
+      double x = xyz[(size_t)i * stride + c];
+      v[c] = fmin(v[c], x);
+      v[3 + c] = fmax(v[3 + c], x);
+    }
+    if (w) {
+      v[6] = fmax(v[6], w[i]);
+      v[7] = fmax(v[7], -w[i]);
+    } else if (dim == 4) {
+      v[6] = fmax(v[6], fabs(xyz[(size_t)i * stride + 3]));
+    }
+  }
+  __shared__ double sh[8][kRedThreads];
+  for (int c = 0; c < 8; ++c) sh[c][threadIdx.x] = v[c];
+  __syncthreads();
+  for (int s = kRedThreads / 2; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s) {
+      for (int c = 0; c < 3; ++c)
+        sh[c][threadIdx.x] = fmin(sh[c][threadIdx.x], sh[c][threadIdx.x + s]);
+      for (int c = 3; c < 8; ++c)
+        sh[c][threadIdx.x] = fmax(sh[c][threadIdx.x], sh[c][threadIdx.x + s]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int c = 0; c < 8; ++c) part[8 * blockIdx.x + c] = sh[c][0];
+}
+
+// Reduces the partials and fills the grid descriptor.
+__global__ void bbox_final_kernel(const double* __restrict__ part, int nparts, int L,
+                                  int has_w, int dim, GridDesc* __restrict__ gd,
+                                  double* __restrict__ wmax_out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double v[8] = {DBL_MAX, DBL_MAX, DBL_MAX, -DBL_MAX, -DBL_MAX, -DBL_MAX, -DBL_MAX, -DBL_MAX};
+  for (int b = 0; b < nparts; ++b) {
+    for (int c = 0; c < 3; ++c) v[c] = fmin(v[c], part[8 * b + c]);
+    for (int c = 3; c < 8; ++c) v[c] = fmax(v[c], part[8 * b + c]);
+  }
+  GridDesc g;
+  double ext = fmax(v[3] - v[0], fmax(v[4] - v[1], v[5] - v[2]));
+  if (!(ext > 0.0)) ext = 1.0;
+  g.L = L;
+  g.G = 1 << L;
+  g.h = ext / g.G * (1.0 + 1e-9);
+  g.inv_h = 1.0 / g.h;
+  for (int c = 0; c < 3; ++c) {
+    g.lo[c] = v[c];
+    g.lo_f[c] = (float)v[c];
+  }
+  g.h_f = (float)g.h;
+  *gd = g;
+  *wmax_out = has_w ? v[6] : 0.0;
+  // max |coordinate| (lift included) for the FP32 screening bound
+  double m = 0.0;
+  for (int c = 0; c < 3; ++c) m = fmax(m, fmax(fabs(v[c]), fabs(v[3 + c])));
+  if (has_w) m = fmax(m, sqrt(fmax(v[6] + v[7], 0.0)));
+  else if (dim == 4) m = fmax(m, v[6]);
+  wmax_out[1] = m;
+}
+
+__global__ void cell_id_kernel(const double* __restrict__ xyz, uint32_t stride, uint32_t n,
+                               const GridDesc* __restrict__ gd, uint32_t* __restrict__ cid,
+                               uint32_t* __restrict__ rank, uint32_t* __restrict__ count) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const GridDesc g = *gd;
+  uint32_t c3[3];
+  for (int c = 0; c < 3; ++c) {
+    double u = (xyz[(size_t)i * stride + c] - g.lo[c]) * g.inv_h;
+    int iu = (int)floor(u);
+    c3[c] = (uint32_t)clampi(iu, 0, g.G - 1);
+  }
+  uint32_t code = morton3(c3[0], c3[1], c3[2]);
+  cid[i] = code;
+  rank[i] = atomicAdd(&count[code], 1u);
+}
+
+__global__ void scatter_kernel(const double* __restrict__ xyz, uint32_t stride,
+                               uint32_t dim, const double* __restrict__ w, uint32_t n,
+                               const uint32_t* __restrict__ cid,
+                               const uint32_t* __restrict__ rank,
+                               const uint32_t* __restrict__ start,
+                               const double* __restrict__ wmax, SortedSeeds S) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint32_t s = start[cid[i]] + rank[i];
+  double x = xyz[(size_t)i * stride], y = xyz[(size_t)i * stride + 1],
+         z = xyz[(size_t)i * stride + 2];
+  double wi = w ? w[i] : 0.0;
+  // h_i = sqrt(W - w_i): the 4-d lift of compute_OTM/main.cpp:280-283
+  double h = w ? sqrt(__dsub_rn(*wmax, wi)) : (dim == 4 ? xyz[(size_t)i * stride + 3] : 0.0);
+  // q = w - |p|^2 evaluated as periodic_delaunay_3d.cpp:3712-3726 does:
+  // (x*x + y*y) + z*z, then w - len2, no fused multiply-add.
+  double len2 = __dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z));
+  S.xd[s] = make_double4(x, y, z, h);
+  S.q[s] = __dsub_rn(wi, len2);
+  S.xf[s] = make_float4((float)x, (float)y, (float)z, (float)h);
+  if (S.ws) S.ws[s] = wi;
+  S.perm[s] = i;
+  S.slot_of[i] = s;
+}
+
+int choose_levels(uint32_t n) {
+  int L = 1;
+  while (L < 9 && (double)(1u << (3 * L)) < (double)n) ++L;
+  return L;
+}
+
+void build_grid(const double* xyz, uint32_t stride, uint32_t dim, const double* w,
+                uint32_t n, int L, SortedSeeds& S, GridScratch& scr, cudaStream_t st) {
+  const int nparts = 120;
+  bbox_partial_kernel<<<nparts, kRedThreads, 0, st>>>(xyz, stride, dim, w, n, scr.red);
+  bbox_final_kernel<<<1, 32, 0, st>>>(scr.red, nparts, L, w != nullptr, (int)dim, S.gd,
+                                      S.aux);
+  const size_t ncells = (size_t)1 << (3 * L);
+  cudaMemsetAsync(S.cell_start, 0, sizeof(uint32_t) * (ncells + 1), st);
+  const unsigned nb = (n + 255) / 256;
+  cell_id_kernel<<<nb, 256, 0, st>>>(xyz, stride, n, S.gd, scr.cid, scr.rank,
+                                     S.cell_start);
+  exclusive_scan_u32(S.cell_start, ncells + 1, scr.scan_tmp, st);
+  scatter_kernel<<<nb, 256, 0, st>>>(xyz, stride, dim, w, n, scr.cid, scr.rank,
+                                     S.cell_start, S.aux, S);
+  S.n = n;
+  S.L = L;
+}
+
+// ---------------------------------------------------------------------
+// kNN: depth-first traversal of the implicit Morton octree
+// ---------------------------------------------------------------------
+constexpr int kKnnThreads = 64;
+constexpr uint32_t kLeaf = 24;
+
+struct KnnList {
+  double* d2;
+  uint32_t* slot;
+  uint32_t stride;
+  __device__ double& d(uint32_t r) { return d2[(size_t)r * stride]; }
+  __device__ uint32_t& s(uint32_t r) { return slot[(size_t)r * stride]; }
+};
+
+// Squared distance from point u (fine-cell units) to the box of an octree
+// node [i*side, (i+1)*side)^3, in fine-cell units, shrunk by a small slack
+// so that it never exceeds the true distance to any seed assigned to it.
+__device__ __forceinline__ float node_box_d2(float ux, float uy, float uz, uint32_t ix,
+                                             uint32_t iy, uint32_t iz, float side) {
+  float bx = ix * side, by = iy * side, bz = iz * side;
+  float dx = fmaxf(fmaxf(bx - ux, ux - (bx + side)), 0.f);
+  float dy = fmaxf(fmaxf(by - uy, uy - (by + side)), 0.f);
+  float dz = fmaxf(fmaxf(bz - uz, uz - (bz + side)), 0.f);
+  dx = fmaxf(dx - 1e-3f, 0.f);
+  dy = fmaxf(dy - 1e-3f, 0.f);
+  dz = fmaxf(dz - 1e-3f, 0.f);
+  return dx * dx + dy * dy + dz * dz;
+}
+
+template <bool SMEM>
+__global__ void __launch_bounds__(kKnnThreads)
+knn_kernel(KnnArgs a, SortedSeeds S, const GridDesc* __restrict__ gdp,
+           const double* __restrict__ aux) {
+  __shared__ double s_d2[SMEM ? kKnnSmemK : 1][kKnnThreads];
+  __shared__ uint32_t s_slot[SMEM ? kKnnSmemK : 1][kKnnThreads];
+  const uint32_t qi = blockIdx.x * kKnnThreads + threadIdx.x;
+  if (qi >= a.nq) return;
+  const GridDesc g = *gdp;
+  KnnList lst;
+  if (SMEM) {
+    lst.d2 = &s_d2[0][threadIdx.x];
+    lst.slot = &s_slot[0][threadIdx.x];
+    lst.stride = kKnnThreads;
+  } else {
+    lst.d2 = a.gl_d2 + qi;
+    lst.slot = a.gl_slot + qi;
+    lst.stride = a.nq;
+  }
+  uint32_t qslot = kNone;
+  double4 q;
+  if (a.mode == KNN_QUERY) {
+    q = a.qpts[qi];
+  } else {
+    qslot = a.qlist ? a.qlist[qi] : qi;
+    q = S.xd[qslot];
+  }
+  const float4 qf = make_float4((float)q.x, (float)q.y, (float)q.z, (float)q.w);
+  const uint32_t qperm = (qslot != kNone) ? S.perm[qslot] : 0u;
+  const float ux = (float)((q.x - g.lo[0]) * g.inv_h);
+  const float uy = (float)((q.y - g.lo[1]) * g.inv_h);
+  const float uz = (float)((q.z - g.lo[2]) * g.inv_h);
+  const float h2f = g.h_f * g.h_f;
+  // bound on |FP32 distance - FP64 distance| from coordinate rounding
+  const float delta = 8.0f * (float)aux[1] * 5.9604645e-8f + 1e-30f;
+  const uint32_t K = a.k;
+  uint32_t cnt = 0;
+  double worst = DBL_MAX;
+  float thr = FLT_MAX;
+  bool dup_lower = false;
+
+  uint32_t stack[8 * 10 + 8];
+  int sp = 0;
+  stack[sp++] = 0u;  // (code << 4) | level
+  while (sp > 0) {
+    const uint32_t e = stack[--sp];
+    const int lev = (int)(e & 15u);
+    const uint32_t code = e >> 4;
+    const int shift = g.L - lev;
+    const float side = (float)(1u << shift);
+    if (cnt == K) {
+      float bd = node_box_d2(ux, uy, uz, compact3(code), compact3(code >> 1),
+                             compact3(code >> 2), side) * h2f;
+      if (bd > thr) continue;
+    }
+    const uint32_t c_lo = code << (3 * shift);
+    const uint32_t c_hi = (code + 1u) << (3 * shift);
+    const uint32_t b = S.cell_start[c_lo], en = S.cell_start[c_hi];
+    if (b == en) continue;
+    if (en - b <= kLeaf || lev == g.L) {
+      for (uint32_t s2 = b; s2 < en; ++s2) {
+        const float4 p = S.xf[s2];
+        float dx = p.x - qf.x, dy = p.y - qf.y, dz = p.z - qf.z, dh = p.w - qf.w;
+        float d32 = dx * dx + dy * dy + dz * dz + dh * dh;
+        if (d32 > thr) continue;
+        if (a.mode == KNN_CELLS && s2 == qslot) continue;
+        const double d = dist2_exact(q, S.xd[s2]);
+        if (a.mode == KNN_CELLS && d == 0.0) {
+          if (S.perm[s2] < qperm) dup_lower = true;
+          continue;
+        }
+        uint32_t pj = 0;
+        bool pj_loaded = false;
+        if (cnt == K) {
+          if (d > worst) continue;
+          if (d == worst) {
+            pj = S.perm[s2];
+            pj_loaded = true;
+            if (pj > S.perm[lst.s(K - 1)]) continue;
+          }
+        }
+        uint32_t pos = (cnt < K) ? cnt : K - 1;
+        while (pos > 0) {
+          const double dp = lst.d(pos - 1);
+          if (dp < d) break;
+          if (dp == d) {
+            if (!pj_loaded) {
+              pj = S.perm[s2];
+              pj_loaded = true;
+            }
+            if (S.perm[lst.s(pos - 1)] < pj) break;
+          }
+          lst.d(pos) = dp;
+          lst.s(pos) = lst.s(pos - 1);
+          --pos;
+        }
+        lst.d(pos) = d;
+        lst.s(pos) = s2;
+        if (cnt < K) ++cnt;
+        if (cnt == K) {
+          worst = lst.d(K - 1);
+          float r = sqrtf(__double2float_ru(worst)) * 1.0000076f + delta;
+          thr = r * r * 1.0000076f;
+        }
+      }
+      continue;
+    }
+    // expand: children sorted by box distance, nearest pushed last
+    const float cside = side * 0.5f;
+    float cd[8];
+    uint32_t cc[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      const uint32_t ch = (code << 3) | (uint32_t)c;
+      cd[c] = node_box_d2(ux, uy, uz, compact3(ch), compact3(ch >> 1), compact3(ch >> 2),
+                          cside) * h2f;
+      cc[c] = ch;
+    }
+    // insertion sort descending by distance
+#pragma unroll
+    for (int i = 1; i < 8; ++i) {
+#pragma unroll
+      for (int j = i; j > 0; --j) {
+        if (cd[j] > cd[j - 1]) {
+          float td = cd[j];
+          cd[j] = cd[j - 1];
+          cd[j - 1] = td;
+          uint32_t tc = cc[j];
+          cc[j] = cc[j - 1];
+          cc[j - 1] = tc;
+        }
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      if (cnt < K || cd[c] <= thr) stack[sp++] = (cc[c] << 4) | (uint32_t)(lev + 1);
+    }
+  }
+  if (a.mode == KNN_CELLS && dup_lower) cnt = 0;
+  if (a.cnt) a.cnt[qi] = (a.mode == KNN_CELLS && dup_lower) ? 0x80000000u : cnt;
+  if (a.nbr)
+    for (uint32_t r = 0; r < cnt; ++r) a.nbr[(size_t)r * a.out_stride + qi] = lst.s(r);
+  if (a.exp_idx) {
+    const size_t row = (a.mode == KNN_QUERY) ? qi : qperm;
+    for (uint32_t r = 0; r < K; ++r) {
+      a.exp_idx[row * K + r] = (r < cnt) ? S.perm[lst.s(r)] : kNone;
+      if (a.exp_d2) a.exp_d2[row * K + r] = (r < cnt) ? lst.d(r) : INFINITY;
+    }
+  }
+}
+
+void launch_knn(const KnnArgs& a, cudaStream_t st) {
+  if (a.nq == 0) return;
+  const unsigned nb = (a.nq + kKnnThreads - 1) / kKnnThreads;
+  if (a.k <= kKnnSmemK)
+    knn_kernel<true><<<nb, kKnnThreads, 0, st>>>(a, *a.S, a.S->gd, a.S->aux);
+  else
+    knn_kernel<false><<<nb, kKnnThreads, 0, st>>>(a, *a.S, a.S->gd, a.S->aux);
+}
+
+}  // namespace gbv

@@ -1,0 +1,192 @@
+/*
+ * gbv.h -- C ABI of the GB300 meshless Voronoi/Laguerre cell engine.
+ *
+ * A drop-in for geogram's meshless cell path.  Every entry point below
+ * replaces one reference interface; the citation is given beside it
+ * (paths relative to geogram's src/lib/).  Plain pointers and sizes only:
+ * no C++ or torch types cross this boundary, no exception leaves it, and
+ * every call returns a gbv_status (the message of the last failure on the
+ * calling thread is in gbv_last_error()).
+ *
+ * Ownership follows the reference: input arrays stay caller-owned; the
+ * context copies them to the GPU and owns its device buffers until
+ * gbv_destroy().  Host output arrays are caller-allocated.  Calls on one
+ * context are synchronous and must not be made concurrently; separate
+ * contexts may be used from separate threads.
+ */
+#ifndef GBV_H
+#define GBV_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    GBV_OK = 0,
+    GBV_ERR_INVALID_ARGUMENT = 1,
+    GBV_ERR_CUDA = 2,
+    GBV_ERR_NO_DEVICE = 3,
+    GBV_ERR_CAPACITY = 4,
+    GBV_ERR_NOT_CONVERGED = 5,
+    GBV_ERR_STATE = 6
+} gbv_status;
+
+/* Per-cell outcome (cell_status).  0-2 are the outcomes of the reference's
+ * security-radius loop, generic_RVD.h (geogram/voronoi) :2278-2352, with
+ * the neighbour lists of delaunay_nn.cpp:104-145. */
+enum {
+    GBV_CELL_CERTIFIED = 0,       /* stopped by d2(pi,pj) > 4.1 R2          */
+    GBV_CELL_ALL_NEIGHBOURS = 1,  /* every other seed was clipped           */
+    GBV_CELL_DUPLICATE = 2,       /* a lower-index seed at distance 0: the
+                                     neighbour list is empty, the cell is
+                                     the unclipped box (as the reference)   */
+    GBV_CELL_NEED_MORE_K = 16,    /* internal: list exhausted, retried      */
+    GBV_CELL_OVERFLOW = 17,       /* internal: capacity exceeded, retried   */
+    GBV_CELL_RECHECK = 18,        /* internal: FP32 could not certify       */
+    GBV_CELL_ERROR = 19           /* the conflict zone was not a disk (never
+                                     seen with exact signs; reported as an
+                                     error by the compute call)             */
+};
+
+typedef enum {
+    GBV_PRECISION_FP64 = 0,          /* all clipping in FP64, exact signs   */
+    GBV_PRECISION_FP32_RECHECK = 1   /* FP32 clipping with certified signs,
+                                        FP64 geometry, FP64 re-clip of every
+                                        cell FP32 could not certify         */
+} gbv_precision;
+
+typedef struct gbv_context gbv_context;
+
+typedef struct {
+    double box_min[3];   /* clipping box (init_with_box, convex_cell.cpp:175) */
+    double box_max[3];
+    uint32_t k0;         /* first neighbour list length (20, delaunay_nn.cpp:50) */
+    uint32_t check_sr;   /* 1: grow the list until certified (set_check_SR) */
+    uint32_t precision;  /* gbv_precision */
+    uint32_t reserved;
+} gbv_cell_options;
+
+typedef struct {
+    uint64_t nnz;              /* facets between seeds (CSR entries)        */
+    uint32_t n_cells;
+    uint32_t n_recheck_fp64;   /* cells re-clipped in FP64 (precision mode) */
+    uint32_t n_more_k;         /* cells that needed a longer list           */
+    uint32_t n_overflow;       /* cells re-run with the large capacity      */
+    uint32_t max_clips;        /* most neighbours visited by one cell       */
+    uint32_t knn_k;            /* list length of the first pass             */
+    double mean_clips;         /* mean neighbours visited per cell          */
+    double volume_sum;         /* compensated FP64 sum of cell volumes      */
+    uint64_t n_exact;          /* exact (expansion) predicate evaluations   */
+    double ms_grid, ms_knn, ms_clip, ms_retry, ms_total;
+} gbv_cell_report;
+
+/* ---------------------------------------------------------------- */
+/* Context                                                          */
+/* ---------------------------------------------------------------- */
+
+/* Last error message of the calling thread ("" if none). */
+const char* gbv_last_error(void);
+
+/* Creates a context on CUDA device `device`.  Replaces nothing in the
+ * reference (its engines are plain C++ objects); the context owns one
+ * CUDA stream and the device buffers. */
+gbv_status gbv_create(int device, gbv_context** out);
+gbv_status gbv_destroy(gbv_context* ctx);
+
+/* Fills the defaults: unit box, k0 = 20, check_sr = 1, FP64. */
+void gbv_cell_options_default(gbv_cell_options* opt);
+
+/* ---------------------------------------------------------------- */
+/* NearestNeighborSearch (points/nn_search.h:69-262)                 */
+/* ---------------------------------------------------------------- */
+
+/* NearestNeighborSearch::set_points(n, pts, stride), nn_search.h:96-121.
+ * dim = 3 (the reference's kd-tree takes any dimension; this engine takes
+ * 3, or 4 for the lifted power-diagram points).  stride is in doubles,
+ * >= dim (stride_supported() is true).  The points are copied to the GPU
+ * and the search structure is built there. */
+gbv_status gbv_nn_set_points(gbv_context* ctx, uint32_t n, const double* pts,
+                             uint32_t dim, uint32_t stride);
+
+/* NearestNeighborSearch::get_nearest_neighbors(k, q, idx, d2) for nq query
+ * points (nn_search.h:131-160): the k nearest stored points of each query,
+ * ascending squared distance, ties by point index.  q is nq*dim doubles;
+ * idx and d2 are nq*k. */
+gbv_status gbv_nn_get_nearest_neighbors(gbv_context* ctx, uint32_t nq,
+                                        const double* q, uint32_t k,
+                                        uint32_t* idx, double* d2);
+
+/* get_nearest_neighbors(k, q_index, idx, d2) (nn_search.h:166-176) for
+ * every stored point at once: row i holds the k nearest of point i, the
+ * point itself included (d2 = 0), as the reference returns it.  This is
+ * the batch table from which per-query calls are served. */
+gbv_status gbv_nn_get_nearest_neighbors_all(gbv_context* ctx, uint32_t k,
+                                            uint32_t* idx, double* d2);
+
+/* ---------------------------------------------------------------- */
+/* Laguerre cells (VBW::ConvexCell results, voronoi/convex_cell.h)   */
+/* ---------------------------------------------------------------- */
+
+/* For every seed: clip the box by the power bisectors of its nearest
+ * neighbours (convex_cell.cpp:461-516, plane periodic_delaunay_3d.cpp:
+ * 3722-3726) until the security radius certifies the cell
+ * (generic_RVD.h:2278-2352).  xyz: 3n doubles; w: n weights or NULL
+ * (Voronoi).  Inputs are host pointers; results stay on the device until
+ * gbv_cells_fetch().  The report may be NULL. */
+gbv_status gbv_cells_compute(gbv_context* ctx, const double* xyz,
+                             const double* w, uint32_t n,
+                             const gbv_cell_options* opt,
+                             gbv_cell_report* report);
+
+/* Same with device pointers, ordered on `stream` (a cudaStream_t, NULL =
+ * the context's stream). */
+gbv_status gbv_cells_compute_device(gbv_context* ctx, const double* d_xyz,
+                                    const double* d_w, uint32_t n,
+                                    const gbv_cell_options* opt, void* stream,
+                                    gbv_cell_report* report);
+
+/* Copies the last results to host arrays (each may be NULL):
+ *   vol[n]           ConvexCell::volume()      (convex_cell.cpp:1215-1253)
+ *   mg[3n]           ConvexCell::compute_mg()  (convex_cell.cpp:1267-1307)
+ *   nbr_rowptr[n+1], nbr_idx[nnz], nbr_area[nnz]: the facets shared with
+ *                    other seeds, i.e. v_global_index(v) and facet_area(v)
+ *                    (convex_cell.h:768-830) for every contributing v,
+ *                    in the reference's order (clipping order);
+ *   cell_status[n]   GBV_CELL_*. */
+gbv_status gbv_cells_fetch(gbv_context* ctx, double* vol, double* mg,
+                           uint32_t* nbr_rowptr, uint32_t* nbr_idx,
+                           double* nbr_area, int32_t* cell_status);
+
+/* Device pointers of the last results (valid until the next compute). */
+gbv_status gbv_cells_device_results(gbv_context* ctx, const double** vol,
+                                    const double** mg,
+                                    const uint32_t** nbr_rowptr,
+                                    const uint32_t** nbr_idx,
+                                    const double** nbr_area,
+                                    const int32_t** cell_status);
+
+/* ---------------------------------------------------------------- */
+/* CVT Lloyd step (voronoi/CVT.cpp:133-167)                          */
+/* ---------------------------------------------------------------- */
+
+/* One Lloyd iteration on the meshless cells: computes the cells of xyz
+ * (weights w or NULL) and replaces every seed by its centroid mg/m when
+ * m > 1e-30 (CVT.cpp:150-160).  xyz is updated in place (host array). */
+gbv_status gbv_lloyd_step(gbv_context* ctx, double* xyz, const double* w,
+                          uint32_t n, const gbv_cell_options* opt,
+                          gbv_cell_report* report);
+
+/* Same on device arrays (d_xyz updated in place) for `iters` iterations. */
+gbv_status gbv_lloyd_device(gbv_context* ctx, double* d_xyz, const double* d_w,
+                            uint32_t n, uint32_t iters,
+                            const gbv_cell_options* opt, void* stream,
+                            gbv_cell_report* report);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBV_H */

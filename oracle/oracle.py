@@ -1,0 +1,134 @@
+"""Oracle bindings -- TEST INFRASTRUCTURE ONLY.
+
+ctypes access to
+  - oracle/libgbv_oracle.so: the CPU restatement of the reference's path
+    (oracle/gbv_oracle.c), which runs anywhere gcc does;
+  - oracle/_ref/libgbv_ref.so: geogram's own BalancedKdTree and
+    VBW::ConvexCell compiled from the reference sources (built only where
+    the reference checkout is present).
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use
+this module, as the checker.  The product never imports it.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_LIB = os.path.join(HERE, "libgbv_oracle.so")
+REF_LIB = os.path.join(HERE, "_ref", "libgbv_ref.so")
+REF_SRC = "/root/reference"
+
+_port = None
+_ref = None
+
+
+def build_port() -> str:
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return PORT_LIB
+
+
+def build_ref(jobs: int = 8) -> str | None:
+    """Compiles the reference's sources into oracle/_ref (needs the checkout)."""
+    if not os.path.isdir(os.path.join(REF_SRC, "src", "lib", "geogram")):
+        return None
+    subprocess.run(["make", "-s", "-C", os.path.join(HERE, "ref"), f"-j{jobs}",
+                    f"REF={REF_SRC}"], check=True)
+    return REF_LIB
+
+
+def port():
+    global _port
+    if _port is None:
+        if not os.path.exists(PORT_LIB):
+            build_port()
+        lib = ctypes.CDLL(PORT_LIB)
+        P = ctypes.c_void_p
+        U = ctypes.c_uint32
+        lib.orc_knn.argtypes = [P, U, U, U, P, P, ctypes.c_int]
+        lib.orc_cells.argtypes = [P, P, U, U, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P, P,
+                                  P, P, U, P, P, P, P]
+        lib.orc_det4_sign.argtypes = [P, P, P, P]
+        _port = lib
+    return _port
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_LIB)
+
+
+def ref():
+    global _ref
+    if _ref is None:
+        if not ref_available():
+            raise RuntimeError("oracle/_ref/libgbv_ref.so is not built")
+        lib = ctypes.CDLL(REF_LIB)
+        P = ctypes.c_void_p
+        U = ctypes.c_uint32
+        lib.ref_init.argtypes = []
+        lib.ref_knn.argtypes = [P, U, U, U, P, P, ctypes.c_int]
+        lib.ref_cells.argtypes = [P, P, U, U, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P, P, P,
+                                  P, U, P, P, P]
+        lib.ref_init()
+        _ref = lib
+    return _ref
+
+
+def _p(a):
+    return None if a is None else ctypes.c_void_p(a.ctypes.data)
+
+
+def knn(pts: np.ndarray, k: int, nthreads: int = 1, which: str = "port"):
+    """k nearest (self included) of every point, ascending (d2, index)."""
+    pts = np.ascontiguousarray(pts, dtype=np.float64)
+    n, dim = pts.shape
+    idx = np.empty((n, k), np.uint32)
+    d2 = np.empty((n, k))
+    lib = port() if which == "port" else ref()
+    fn = lib.orc_knn if which == "port" else lib.ref_knn
+    r = fn(_p(pts), dim, n, k, _p(idx), _p(d2), nthreads)
+    if r != 0:
+        raise RuntimeError("knn failed")
+    return idx, d2
+
+
+def cells(xyz: np.ndarray, w: np.ndarray | None = None, k0: int = 20, check_sr: bool = True,
+          exact: bool = True, nthreads: int = 1, which: str = "port", max_nbr: int = 96) -> dict:
+    """Certified cells in the unit box; dict of per-seed arrays plus CSR."""
+    x = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+    n = len(x)
+    wa = None if w is None else np.ascontiguousarray(w, dtype=np.float64)
+    out = dict(vol=np.zeros(n), mg=np.zeros((n, 3)), cnt=np.zeros(n, np.uint32),
+               nidx=np.zeros((n, max_nbr), np.uint32), narea=np.zeros((n, max_nbr)),
+               k_list=np.zeros(n, np.uint32), n_clip=np.zeros(n, np.uint32),
+               status=np.zeros(n, np.int32))
+    args = [_p(x), _p(wa), n, k0, int(check_sr), int(exact), nthreads, _p(out["vol"]),
+            _p(out["mg"]), _p(out["cnt"]), _p(out["nidx"]), _p(out["narea"]), max_nbr,
+            _p(out["k_list"]), _p(out["n_clip"]), _p(out["status"])]
+    if which == "port":
+        ne = ctypes.c_long(0)
+        r = port().orc_cells(*args, ctypes.byref(ne))
+        out["n_exact"] = ne.value
+    else:
+        r = ref().ref_cells(*args)
+    if r != 0:
+        raise RuntimeError("cells failed")
+    cnt = out["cnt"].astype(np.int64)
+    if (out["status"] == 4).any():
+        raise RuntimeError("max_nbr too small")
+    rowptr = np.zeros(n + 1, np.int64)
+    rowptr[1:] = np.cumsum(cnt)
+    mask = np.arange(max_nbr)[None, :] < cnt[:, None]
+    out["rowptr"] = rowptr
+    out["nbr"] = out["nidx"][mask]
+    out["area"] = out["narea"][mask]
+    del out["nidx"], out["narea"]
+    return out
+
+
+def det4_sign(p0, p1, p2, p3) -> int:
+    a = [np.ascontiguousarray(p, dtype=np.float64) for p in (p0, p1, p2, p3)]
+    return int(port().orc_det4_sign(*[_p(x) for x in a]))
