@@ -101,14 +101,14 @@ namespace gbv {
 // Small kernels of the orchestration
 // ---------------------------------------------------------------------
 
-// Collects the queries of a pass whose cell ended with one of the three
-// retry statuses, with the list row each used.
+// Collects the queries of a pass whose cell ended with one of the retry
+// statuses, with the list row each used.
 __global__ void classify_kernel(const uint32_t* __restrict__ qlist,
                                 const uint32_t* __restrict__ qrow, uint32_t nq,
                                 const int32_t* __restrict__ status, uint32_t* __restrict__ counts,
                                 uint32_t* __restrict__ recheck_s, uint32_t* __restrict__ recheck_r,
                                 uint32_t* __restrict__ over_s, uint32_t* __restrict__ over_r,
-                                uint32_t* __restrict__ morek_s, uint32_t* __restrict__ err_s) {
+                                uint32_t* __restrict__ morek_s, uint32_t* __restrict__ morek_r) {
   const uint32_t qi = blockIdx.x * blockDim.x + threadIdx.x;
   if (qi >= nq) return;
   const uint32_t s = qlist ? qlist[qi] : qi;
@@ -125,10 +125,31 @@ __global__ void classify_kernel(const uint32_t* __restrict__ qlist,
   } else if (st == CELL_NEED_MORE_K) {
     uint32_t k = atomicAdd(&counts[2], 1u);
     morek_s[k] = s;
+    morek_r[k] = r;
   } else if (st == CELL_ERROR) {
-    uint32_t k = atomicAdd(&counts[3], 1u);
-    if (k == 0) err_s[0] = s;
+    atomicAdd(&counts[3], 1u);
   }
+}
+
+// Starts the extended lists of cells that ran out of neighbours: copies the
+// first k entries of each cell's current list and its lower bound.
+__global__ void extend_lists_kernel(const uint32_t* __restrict__ rows, uint32_t m,
+                                    const uint32_t* __restrict__ old_lists, uint32_t old_stride,
+                                    uint32_t k, const double* __restrict__ old_last_d2,
+                                    const uint32_t* __restrict__ old_last_idx,
+                                    uint32_t* __restrict__ new_lists, double* __restrict__ lo_d2,
+                                    uint32_t* __restrict__ lo_idx) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const uint32_t r = rows[i];
+  for (uint32_t j = 0; j < k; ++j) new_lists[(size_t)j * m + i] = old_lists[(size_t)j * old_stride + r];
+  lo_d2[i] = old_last_d2[r];
+  lo_idx[i] = old_last_idx[r];
+}
+
+__global__ void add_count_kernel(uint32_t* __restrict__ cnt, uint32_t m, uint32_t k) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < m) cnt[i] = k + (cnt[i] & 0x7FFFFFFFu);
 }
 
 __global__ void facet_count_kernel(const uint32_t* __restrict__ slot_of,
@@ -245,6 +266,8 @@ static void setup_seeds(gbv_context* c, uint32_t n, bool weighted) {
   S.xd = c->buf<double4>("xd", n);
   S.q = c->buf<double>("q", n);
   S.xf = c->buf<float4>("xf", n);
+  S.xl = c->buf<float4>("xl", n);
+  S.wf = weighted ? c->buf<float2>("wf", n) : nullptr;
   S.ws = weighted ? c->buf<double>("ws", n) : nullptr;
   S.perm = c->buf<uint32_t>("perm", n);
   S.slot_of = c->buf<uint32_t>("slot_of", n);
@@ -265,6 +288,17 @@ struct CellsTiming {
   float grid = 0, knn = 0, clip = 0, total = 0;
 };
 
+// One list buffer: lists[r * stride + row], counts and the exact (d2, index)
+// of each row's last entry (the lower bound of the next batch).
+struct ListSet {
+  const uint32_t* lists = nullptr;
+  uint32_t stride = 0;
+  const uint32_t* cnt = nullptr;
+  uint32_t k = 0;
+  const double* last_d2 = nullptr;
+  const uint32_t* last_idx = nullptr;
+};
+
 // The whole cell computation on device inputs.
 static void cells_device(gbv_context* c, const double* d_xyz, const double* d_w, uint32_t n,
                          const gbv_cell_options& o, cudaStream_t st, gbv_cell_report* rep) {
@@ -277,7 +311,7 @@ static void cells_device(gbv_context* c, const double* d_xyz, const double* d_w,
   build_grid(d_xyz, 3, 3, d_w, n, S.L, S, c->scr, st);
   GBV_CUDA(cudaEventRecord(c->ev[1], st));
 
-  // outputs by slot
+  // per-cell results by slot, and the combinatorics records
   int32_t* status_s = c->buf<int32_t>("status_s", n);
   double* vol_s = c->buf<double>("vol_s", n);
   double* mg_s = c->buf<double>("mg_s", 3 * (size_t)n);
@@ -285,15 +319,27 @@ static void cells_device(gbv_context* c, const double* d_xyz, const double* d_w,
   uint32_t* nclip = c->buf<uint32_t>("nclip", n);
   uint32_t* f_nbr = c->buf<uint32_t>("f_nbr", (size_t)kMaxFacets * n);
   double* f_area = c->buf<double>("f_area", (size_t)kMaxFacets * n);
+  CombBuf cb;
+  cb.tv = c->buf<uint32_t>("cb_tv", (size_t)kTMax * n);
+  cb.ta = c->buf<uint32_t>("cb_ta", (size_t)kTMax * n);
+  cb.key = c->buf<int16_t>("cb_key", (size_t)kTMax * n);
+  cb.pown = c->buf<uint32_t>("cb_pown", (size_t)kPMax * n);
+  cb.prank = c->buf<uint16_t>("cb_prank", (size_t)kPMax * n);
+  cb.tmask = c->buf<ulonglong2>("cb_tmask", n);
+  cb.pmask = c->buf<uint64_t>("cb_pmask", n);
+  cb.flags = c->buf<uint32_t>("cb_flags", n);
   GBV_CUDA(cudaMemsetAsync(c->counters, 0, 2 * sizeof(unsigned long long), st));
+  uint32_t* flag_count = c->buf<uint32_t>("knn_flag_count", 1);
+  uint32_t* flag_list = c->buf<uint32_t>("knn_flag_list", n);
 
-  // first pass
+  // first lists
   const uint32_t nm1 = n > 1 ? n - 1 : 0;
-  uint32_t K = o.check_sr ? std::min<uint32_t>(kKnnSmemK, nm1)
-                          : std::min<uint32_t>(o.k0, nm1);
-  if (K > kKnnSmemK) K = kKnnSmemK;  // longer first lists: see the retry pass
+  uint32_t K = o.check_sr ? std::min<uint32_t>(kKnnSmemK, nm1) : std::min<uint32_t>(o.k0, nm1);
+  const bool long_first = K > kKnnSmemK;  // only without the security radius
   uint32_t* knn = c->buf<uint32_t>("knn", (size_t)std::max<uint32_t>(K, 1) * n);
   uint32_t* kcnt = c->buf<uint32_t>("kcnt", n);
+  double* klast_d = c->buf<double>("klast_d", n);
+  uint32_t* klast_i = c->buf<uint32_t>("klast_i", n);
   {
     KnnArgs ka{};
     ka.S = &S;
@@ -303,53 +349,54 @@ static void cells_device(gbv_context* c, const double* d_xyz, const double* d_w,
     ka.nbr = knn;
     ka.out_stride = n;
     ka.cnt = kcnt;
+    ka.last_d2 = klast_d;
+    ka.last_idx = klast_i;
+    ka.flag_count = flag_count;
+    ka.flag_list = flag_list;
+    if (long_first) {
+      ka.gl_d2 = c->buf<double>("knn_gd2", (size_t)K * n);
+      ka.gl_slot = c->buf<uint32_t>("knn_gslot", (size_t)K * n);
+    }
     if (K > 0) launch_knn(ka, st);
     else GBV_CUDA(cudaMemsetAsync(kcnt, 0, sizeof(uint32_t) * n, st));
+    GBV_CUDA(cudaGetLastError());
   }
   GBV_CUDA(cudaEventRecord(c->ev[2], st));
 
-  ClipArgs base{};
-  base.S = S;
-  base.n_total = n;
+  ClipArgs cbase{};
+  cbase.S = S;
+  cbase.n_total = n;
+  GeomArgs gbase{};
+  gbase.S = S;
   for (int k = 0; k < 3; ++k) {
-    base.box[k] = o.box_min[k];
-    base.box[3 + k] = o.box_max[k];
+    cbase.box[k] = gbase.box[k] = o.box_min[k];
+    cbase.box[3 + k] = gbase.box[3 + k] = o.box_max[k];
   }
-  base.check_sr = o.check_sr ? 1 : 0;
-  base.status = status_s;
-  base.vol = vol_s;
-  base.mg = mg_s;
-  base.nf = nf;
-  base.nclip = nclip;
-  base.f_nbr = f_nbr;
-  base.f_area = f_area;
-  base.out_stride = n;
-  base.counters = c->counters;
+  cbase.check_sr = o.check_sr ? 1 : 0;
+  cbase.status = gbase.status = status_s;
+  cbase.nclip = nclip;
+  gbase.nclip = nclip;
+  cbase.comb = gbase.comb = cb;
+  cbase.counters = c->counters;
+  gbase.vol = vol_s;
+  gbase.mg = mg_s;
+  gbase.nf = nf;
+  gbase.f_nbr = f_nbr;
+  gbase.f_area = f_area;
+  gbase.out_stride = n;
 
-  ClipArgs a = base;
-  a.nbr = knn;
-  a.nbr_stride = n;
-  a.nbr_cnt = kcnt;
-  a.list_k = K;
-  a.nq = n;
-  if (fp32) launch_clip_fp32(a, st);
-  else launch_clip_fp64(a, CLIP_SMALL, st);
-  GBV_CUDA(last_launch_error);
-  GBV_CUDA(cudaEventRecord(c->ev[5], st));
-
-  uint32_t* rs = c->buf<uint32_t>("recheck_s", n);
-  uint32_t* rr = c->buf<uint32_t>("recheck_r", n);
-  uint32_t* os = c->buf<uint32_t>("over_s", n);
-  uint32_t* orw = c->buf<uint32_t>("over_r", n);
-  uint32_t* ms = c->buf<uint32_t>("morek_s", n);
-  uint32_t* es = c->buf<uint32_t>("err_s", 1);
+  uint32_t* rs = c->buf<uint32_t>("cls_rs", n);
+  uint32_t* rr = c->buf<uint32_t>("cls_rr", n);
+  uint32_t* os = c->buf<uint32_t>("cls_os", n);
+  uint32_t* orw = c->buf<uint32_t>("cls_or", n);
+  uint32_t* ms = c->buf<uint32_t>("cls_ms", n);
+  uint32_t* mr = c->buf<uint32_t>("cls_mr", n);
   uint32_t n_recheck = 0, n_over = 0, n_morek = 0;
 
-  // classify the queries of a finished pass; returns the three counts
   auto classify = [&](const uint32_t* ql, const uint32_t* qr, uint32_t nq, uint32_t out[4]) {
     GBV_CUDA(cudaMemsetAsync(c->list_counts, 0, 4 * sizeof(uint32_t), st));
     classify_kernel<<<nblocks(nq, 256), 256, 0, st>>>(ql, qr, nq, status_s, c->list_counts, rs,
-                                                      rr, os, orw, ms, es);
+                                                      rr, os, orw, ms, mr);
     GBV_CUDA(cudaMemcpyAsync(c->h_counts, c->list_counts, 4 * sizeof(uint32_t),
                              cudaMemcpyDeviceToHost, st));
     GBV_CUDA(cudaStreamSynchronize(st));
@@ -359,110 +406,143 @@ static void cells_device(gbv_context* c, const double* d_xyz, const double* d_w,
                                            " cell(s) (conflict zone not a disk)"};
     }
   };
-
-  // Runs the FP64 fixes of a finished pass whose lists are given: cells
-  // FP32 could not certify are re-clipped in FP64, cells that overflowed
-  // the small capacity run the large kernel.  Returns the number of cells
-  // that still need a longer list; their slots are in "morek_acc".
-  auto fix_pass = [&](const uint32_t* lists, uint32_t stride, const uint32_t* cnts,
-                      uint32_t listk, const uint32_t* ql, const uint32_t* qr,
-                      uint32_t nq) -> uint32_t {
-    uint32_t* mk_acc = c->buf<uint32_t>("morek_acc", n);
+  // clip + geometry of a set of cells with the given lists
+  auto run = [&](const ListSet& L, const uint32_t* ql, const uint32_t* qr, uint32_t nq,
+                 int kind /* 0: mode, 1: FP64 small, 2: FP64 large */) {
+    ClipArgs a = cbase;
+    a.nbr = L.lists;
+    a.nbr_stride = L.stride;
+    a.nbr_cnt = L.cnt;
+    a.list_k = L.k;
+    a.qlist = ql;
+    a.qrow = qr;
+    a.nq = nq;
+    const bool f32 = kind == 0 && fp32;
+    if (f32) launch_clip_fp32(a, st);
+    else launch_clip_fp64(a, kind == 2 ? CLIP_LARGE : CLIP_SMALL, st);
+    GBV_CUDA(last_launch_error);
+    GeomArgs g = gbase;
+    g.nbr = L.lists;
+    g.nbr_stride = L.stride;
+    g.qlist = ql;
+    g.qrow = qr;
+    g.nq = nq;
+    g.verify_sr = (f32 && o.check_sr) ? 1 : 0;
+    launch_geometry(g, st);
+    GBV_CUDA(last_launch_error);
+  };
+  // runs a pass and its FP64 fixes; returns the cells that still need a
+  // longer list (slots in mk_s, rows of L in mk_r)
+  uint32_t* mk_s = c->buf<uint32_t>("mk_s", n);
+  uint32_t* mk_r = c->buf<uint32_t>("mk_r", n);
+  auto process = [&](const ListSet& L, const uint32_t* ql, const uint32_t* qr,
+                     uint32_t nq) -> uint32_t {
     uint32_t* rc_s = c->buf<uint32_t>("rc_s", n);
     uint32_t* rc_r = c->buf<uint32_t>("rc_r", n);
     uint32_t* ov_s = c->buf<uint32_t>("ov_s", n);
     uint32_t* ov_r = c->buf<uint32_t>("ov_r", n);
-    uint32_t nmk = 0, nrc = 0, nov = 0;
     auto append = [&](uint32_t* dst, uint32_t at, const uint32_t* src, uint32_t cnt) {
       if (cnt) GBV_CUDA(cudaMemcpyAsync(dst + at, src, cnt * sizeof(uint32_t),
                                         cudaMemcpyDeviceToDevice, st));
     };
-    auto clip_list = [&](const uint32_t* ls, const uint32_t* lr, uint32_t cnt, int shape) {
-      ClipArgs b = base;
-      b.nbr = lists;
-      b.nbr_stride = stride;
-      b.nbr_cnt = cnts;
-      b.list_k = listk;
-      b.qlist = ls;
-      b.qrow = lr;
-      b.nq = cnt;
-      launch_clip_fp64(b, shape, st);
-      GBV_CUDA(last_launch_error);
-    };
+    run(L, ql, qr, nq, 0);
     uint32_t c1[4];
     classify(ql, qr, nq, c1);
-    append(rc_s, 0, rs, c1[0]);
-    append(rc_r, 0, rr, c1[0]);
-    nrc = c1[0];
-    append(ov_s, 0, os, c1[1]);
-    append(ov_r, 0, orw, c1[1]);
-    nov = c1[1];
-    append(mk_acc, 0, ms, c1[2]);
-    nmk = c1[2];
+    uint32_t nrc = c1[0], nov = c1[1], nmk = c1[2];
+    append(rc_s, 0, rs, nrc);
+    append(rc_r, 0, rr, nrc);
+    append(ov_s, 0, os, nov);
+    append(ov_r, 0, orw, nov);
+    append(mk_s, 0, ms, nmk);
+    append(mk_r, 0, mr, nmk);
     if (nrc) {
       n_recheck += nrc;
-      clip_list(rc_s, rc_r, nrc, CLIP_SMALL);
+      run(L, rc_s, rc_r, nrc, 1);
       uint32_t c2[4];
       classify(rc_s, rc_r, nrc, c2);
       append(ov_s, nov, os, c2[1]);
       append(ov_r, nov, orw, c2[1]);
       nov += c2[1];
-      append(mk_acc, nmk, ms, c2[2]);
+      append(mk_s, nmk, ms, c2[2]);
+      append(mk_r, nmk, mr, c2[2]);
       nmk += c2[2];
     }
     if (nov) {
       n_over += nov;
-      clip_list(ov_s, ov_r, nov, CLIP_LARGE);
+      run(L, ov_s, ov_r, nov, 2);
       uint32_t c3[4];
       classify(ov_s, ov_r, nov, c3);
-      if (c3[1] || c3[0]) {
-        throw StatusError{GBV_ERR_CAPACITY,
-                          std::to_string(c3[1]) + " cell(s) exceed the large capacity (" +
-                              std::to_string(kLargeT) + " corners, " +
-                              std::to_string(kLargeP) + " planes)"};
+      if (c3[0] || c3[1]) {
+        throw StatusError{GBV_ERR_CAPACITY, std::to_string(c3[1]) +
+                                                " cell(s) exceed the large capacity (" +
+                                                std::to_string(kLargeT) + " corners, " +
+                                                std::to_string(kLargeP) + " planes)"};
       }
-      append(mk_acc, nmk, ms, c3[2]);
+      append(mk_s, nmk, ms, c3[2]);
+      append(mk_r, nmk, mr, c3[2]);
       nmk += c3[2];
     }
     return nmk;
   };
 
-  uint32_t morek = fix_pass(knn, n, kcnt, K, nullptr, nullptr, n);
-  uint32_t listk = K;
+  ListSet L0;
+  L0.lists = knn;
+  L0.stride = n;
+  L0.cnt = kcnt;
+  L0.k = K;
+  L0.last_d2 = klast_d;
+  L0.last_idx = klast_i;
+  uint32_t morek = process(L0, nullptr, nullptr, n);
+  GBV_CUDA(cudaEventRecord(c->ev[5], st));
+  ListSet cur = L0;
+  int round = 0;
   while (morek > 0) {
     n_morek += morek;
-    if (listk >= nm1) throw StatusError{GBV_ERR_STATE, "list growth did not terminate"};
-    listk = std::min<uint64_t>(nm1, (uint64_t)listk * 4);
-    uint32_t* ql = c->buf<uint32_t>("mk_q", morek);
-    GBV_CUDA(cudaMemcpyAsync(ql, c->buf<uint32_t>("morek_acc", n), morek * 4,
-                             cudaMemcpyDeviceToDevice, st));
-    uint32_t* l2 = c->buf<uint32_t>("mk_lists", (size_t)listk * morek);
-    uint32_t* c2 = c->buf<uint32_t>("mk_cnt", morek);
+    if (cur.k >= nm1) throw StatusError{GBV_ERR_STATE, "list growth did not terminate"};
+    const uint32_t batch = std::min<uint32_t>(kKnnSmemK, nm1 - cur.k);
+    const uint32_t newk = cur.k + batch;
+    const std::string tag = std::to_string(round & 1);
+    uint32_t* q_s = c->buf<uint32_t>("ext_s" + tag, morek);
+    uint32_t* q_r = c->buf<uint32_t>("ext_r" + tag, morek);
+    GBV_CUDA(cudaMemcpyAsync(q_s, mk_s, morek * 4, cudaMemcpyDeviceToDevice, st));
+    GBV_CUDA(cudaMemcpyAsync(q_r, mk_r, morek * 4, cudaMemcpyDeviceToDevice, st));
+    uint32_t* lists = c->buf<uint32_t>("ext_lists" + tag, (size_t)newk * morek);
+    uint32_t* cnt = c->buf<uint32_t>("ext_cnt" + tag, morek);
+    double* lo_d = c->buf<double>("ext_lo_d" + tag, morek);
+    uint32_t* lo_i = c->buf<uint32_t>("ext_lo_i" + tag, morek);
+    double* last_d = c->buf<double>("ext_last_d" + tag, morek);
+    uint32_t* last_i = c->buf<uint32_t>("ext_last_i" + tag, morek);
+    extend_lists_kernel<<<nblocks(morek, 128), 128, 0, st>>>(q_r, morek, cur.lists, cur.stride,
+                                                             cur.k, cur.last_d2, cur.last_idx,
+                                                             lists, lo_d, lo_i);
     KnnArgs ka{};
     ka.S = &S;
     ka.nq = morek;
-    ka.qlist = ql;
-    ka.k = listk;
+    ka.qlist = q_s;
+    ka.k = batch;
     ka.mode = KNN_CELLS;
-    ka.nbr = l2;
+    ka.lo_d2 = lo_d;
+    ka.lo_idx = lo_i;
+    ka.nbr = lists + (size_t)cur.k * morek;
     ka.out_stride = morek;
-    ka.cnt = c2;
-    if (listk > kKnnSmemK) {
-      ka.gl_d2 = c->buf<double>("mk_gd2", (size_t)listk * morek);
-      ka.gl_slot = c->buf<uint32_t>("mk_gslot", (size_t)listk * morek);
-    }
+    ka.cnt = cnt;
+    ka.last_d2 = last_d;
+    ka.last_idx = last_i;
+    ka.flag_count = flag_count;
+    ka.flag_list = flag_list;
     launch_knn(ka, st);
-    ClipArgs b = base;
-    b.nbr = l2;
-    b.nbr_stride = morek;
-    b.nbr_cnt = c2;
-    b.list_k = listk;
-    b.qlist = ql;
-    b.qrow = nullptr;
-    b.nq = morek;
-    launch_clip_fp64(b, CLIP_SMALL, st);
-    GBV_CUDA(last_launch_error);
-    morek = fix_pass(l2, morek, c2, listk, ql, nullptr, morek);
+    add_count_kernel<<<nblocks(morek, 128), 128, 0, st>>>(cnt, morek, cur.k);
+    GBV_CUDA(cudaGetLastError());
+    ListSet nx;
+    nx.lists = lists;
+    nx.stride = morek;
+    nx.cnt = cnt;
+    nx.k = newk;
+    nx.last_d2 = last_d;
+    nx.last_idx = last_i;
+    morek = process(nx, q_s, nullptr, morek);
+    cur = nx;
+    ++round;
   }
   GBV_CUDA(cudaEventRecord(c->ev[3], st));
 
@@ -474,10 +554,9 @@ static void cells_device(gbv_context* c, const double* d_xyz, const double* d_w,
   facet_count_kernel<<<nblocks((size_t)n + 1, 256), 256, 0, st>>>(S.slot_of, nf, n, c->rowptr);
   uint32_t* stmp = c->buf<uint32_t>("csr_scan_tmp", scan_tmp_elems((size_t)n + 1));
   exclusive_scan_u32(c->rowptr, (size_t)n + 1, stmp, st);
-  uint32_t nnz32 = 0;
   GBV_CUDA(cudaMemcpyAsync(&c->h_counts[0], c->rowptr + n, 4, cudaMemcpyDeviceToHost, st));
   GBV_CUDA(cudaStreamSynchronize(st));
-  nnz32 = c->h_counts[0];
+  const uint32_t nnz32 = c->h_counts[0];
   c->nnz = nnz32;
   c->nbr = c->buf<uint32_t>("nbr", std::max<uint32_t>(nnz32, 1));
   c->area = c->buf<double>("area", std::max<uint32_t>(nnz32, 1));
@@ -517,11 +596,11 @@ static void cells_device(gbv_context* c, const double* d_xyz, const double* d_w,
     rep->knn_k = K;
     rep->mean_clips = (double)cs / n;
     rep->volume_sum = vs;
+    rep->n_exact = hc[0];
     rep->ms_grid = t01;
     rep->ms_knn = t12;
     rep->ms_clip = t25;
     rep->ms_retry = t53;
-    rep->n_exact = hc[0];
     rep->ms_total = t04;
   } else {
     GBV_CUDA(cudaStreamSynchronize(st));
@@ -750,6 +829,8 @@ gbv_status gbv_nn_get_nearest_neighbors(gbv_context* c, uint32_t nq, const doubl
     ka.mode = KNN_QUERY;
     ka.exp_idx = oi;
     ka.exp_d2 = od;
+    ka.flag_count = c->buf<uint32_t>("knn_flag_count", 1);
+    ka.flag_list = c->buf<uint32_t>("nn_flag_list", nq);
     if (k > kKnnSmemK) {
       ka.gl_d2 = c->buf<double>("nn_gd2", (size_t)k * nq);
       ka.gl_slot = c->buf<uint32_t>("nn_gslot", (size_t)k * nq);
@@ -780,6 +861,8 @@ gbv_status gbv_nn_get_nearest_neighbors_all(gbv_context* c, uint32_t k, uint32_t
     ka.mode = KNN_ALL;
     ka.exp_idx = oi;
     ka.exp_d2 = od;
+    ka.flag_count = c->buf<uint32_t>("knn_flag_count", 1);
+    ka.flag_list = c->buf<uint32_t>("nn_flag_list", n);
     if (k > kKnnSmemK) {
       ka.gl_d2 = c->buf<double>("nn_gd2", (size_t)k * n);
       ka.gl_slot = c->buf<uint32_t>("nn_gslot", (size_t)k * n);

@@ -4,30 +4,43 @@
 //
 // The cell is kept in the dual form of the reference's VBW::ConvexCell
 // (voronoi/convex_cell.h:419-1436): every clipping plane is a vertex,
-// every corner of the polytope is a triangle of three planes, with the
-// three adjacent triangles.  Clipping by a plane (convex_cell.cpp:461-516,
-// 761-865) removes the triangles whose corner is on the negative side and
+// every corner of the polytope is a triangle of three planes with its three
+// adjacent triangles.  Clipping by a plane (convex_cell.cpp:461-516,
+// 761-865) removes the triangles whose corner lies on the negative side and
 // fans new triangles from the new plane around the border of the removed
-// zone.  What differs from the CPU code is the layout and the bookkeeping:
+// zone.  What differs from the CPU code is layout and bookkeeping:
 //   - triangles live in fixed slots tracked by bit masks instead of linked
-//     lists, planes in slots recycled once no triangle uses them;
+//     lists; planes in slots recycled once no triangle uses them;
+//   - the reference's valid-list order, which decides how its geometry
+//     fans are rooted, is carried as one key per triangle (see below);
 //   - each triangle caches its corner and a bound on the corner's rounding
-//     error, so a conflict test is three FMAs and a compare; when the
+//     error, so a conflict test is three FMAs and a compare.  When the
 //     bound cannot decide the sign, the FP64 kernel evaluates the exact
 //     determinant sign (the reference's PCK::det_4d decision) and the FP32
 //     kernel marks the cell for an FP64 re-clip;
-//   - the security-radius test (generic_RVD.h:2278-2352) reads the
-//     cached corner radii.
+//   - the security-radius test (generic_RVD.h:2278-2352) reads the cached
+//     corner radii.
+// The kernel writes the cell's combinatorics; gbv_geom.cu turns them into
+// volume, centroid and facet areas.
+//
+// List-order keys.  The reference rebuilds its valid-triangle list at every
+// clip: survivors are relinked in reverse order, then the new triangles are
+// pushed at the head in creation order; the border walk starts at the
+// border edge met last while scanning that list.  With an "effective key"
+// eff = parity * key per triangle and the list read in ascending eff, one
+// clip is: parity flips (survivors reversed, nothing rewritten), the c-th
+// new triangle gets eff = -(max eff of the survivors) - 1 - c, and the walk
+// starts at the border edge maximising (new eff of the kept triangle, edge).
 #include <cfloat>
 #include <cmath>
 #include <type_traits>
 
 #include "gbv_clip.cuh"
 #include "gbv_exact.cuh"
+#include "gbv_refgeom.cuh"
 
 namespace gbv {
 
-constexpr uint32_t kBoxBase = 0xFFFFFF00u;  // pslot of box plane b is kBoxBase + b
 cudaError_t last_launch_error = cudaSuccess;
 constexpr int kClipThreads = 32;
 
@@ -43,6 +56,7 @@ struct Bits {
   }
   __device__ __forceinline__ bool test(int i) const { return (w[i >> 6] >> (i & 63)) & 1ull; }
   __device__ __forceinline__ void set(int i) { w[i >> 6] |= 1ull << (i & 63); }
+  __device__ __forceinline__ void reset(int i) { w[i >> 6] &= ~(1ull << (i & 63)); }
   __device__ __forceinline__ int popc() const {
     int c = 0;
 #pragma unroll
@@ -61,7 +75,6 @@ struct Bits {
     for (int i = 0; i < NW; ++i) e = e && (w[i] == o.w[i]);
     return e;
   }
-  // lowest set bit, -1 if none
   __device__ __forceinline__ int first() const {
 #pragma unroll
     for (int i = 0; i < NW; ++i)
@@ -90,29 +103,32 @@ __device__ __forceinline__ Bits<NW> full_bits(int n) {
 }
 
 // ---------------------------------------------------------------------
-// Per-thread cell storage in shared memory
+// Per-thread cell storage in shared memory, [slot][thread]
 // ---------------------------------------------------------------------
 template <typename Real, int BS, int T, int P>
 struct CellSmem;
 
 template <int BS, int T, int P>
 struct CellSmem<double, BS, T, P> {
-  double4 corner[T][BS];  // x, y, z (global frame); w packs (r2, eps) floats
+  double2 cxy[T][BS];     // corner x, y (reference frame and arithmetic)
+  double2 czr[T][BS];     // corner z, squared distance to the seed
+  float eps[T][BS];       // corner error bound (cramer_bound)
   uint32_t tv[T][BS];     // planes i | j << 8 | k << 16
-  uint32_t ta[T][BS];     // adjacent triangles across the edges opposite i, j, k
-  uint32_t pslot[P][BS];  // neighbour's sorted slot, or kBoxBase + box face
-  uint16_t prank[P][BS];  // position in the neighbour list
-  uint16_t pnb[P][BS];    // border scratch: triangle | edge << 8
-  uint8_t pnext[P][BS];   // border scratch: next border plane / facet triangle
+  uint32_t ta[T][BS];     // triangles across the edges opposite i, j, k
+  int16_t key[T][BS];
+  uint32_t pown[P][BS];   // plane owner: seed slot or kBoxBase + face
+  uint16_t prank[P][BS];  // list position of the plane's seed
+  uint16_t pnb[P][BS];    // border scratch: kept triangle | edge << 8
+  uint8_t pnext[P][BS];   // border scratch: next border plane
 };
 
 template <int BS, int T, int P>
 struct CellSmem<float, BS, T, P> {
-  float4 corner[T][BS];   // x, y, z (frame centred on the seed), eps
-  float4 plane[P][BS];    // local-frame plane equations
+  float4 c4[T][BS];       // corner x, y, z (frame centred on the seed), eps
   uint32_t tv[T][BS];
   uint32_t ta[T][BS];
-  uint32_t pslot[P][BS];
+  int16_t key[T][BS];
+  float4 pl[P][BS];       // local-frame plane equations
   uint16_t prank[P][BS];
   uint16_t pnb[P][BS];
   uint8_t pnext[P][BS];
@@ -122,8 +138,8 @@ template <typename Real>
 struct Consts;
 template <>
 struct Consts<double> {
-  // error-bound factors (units of 2^-53), inflated about twice over the
-  // rounding counts of the evaluation: det3 (5 levels), dot (3 levels)
+  // error-bound factors in units of 2^-53, about twice the rounding counts
+  // of the evaluation: 3x3 determinant (5 levels), dot product (3 levels)
   static constexpr double kDet = 12.0 * 1.1102230246251565e-16;
   static constexpr double kDot = 8.0 * 1.1102230246251565e-16;
   static constexpr double kUlp = 1.1102230246251565e-16;
@@ -136,152 +152,120 @@ struct Consts<float> {
   static constexpr float kUlp = 5.9604645e-8f;
 };
 
-__device__ __forceinline__ double pack2f(float lo, float hi) {
-  return __hiloint2double(__float_as_int(hi), __float_as_int(lo));
-}
-__device__ __forceinline__ float unpack_lo(double d) { return __int_as_float(__double2loint(d)); }
-__device__ __forceinline__ float unpack_hi(double d) { return __int_as_float(__double2hiint(d)); }
-
-template <typename R4>
-__device__ __forceinline__ auto pabs1(const R4& p) -> decltype(p.x) {
-  return fabs(p.x) + fabs(p.y) + fabs(p.z);
-}
-
-// Intersection of the three planes a, b, c (rows), by Cramer's rule as in
-// ConvexCell::compute_triangle_point (convex_cell.cpp:1055-1081), with the
-// permanents of the 3x3 minors that bound the rounding error.  Returns the
-// corner (x, y, z) and eps, a bound on |corner - exact corner| per
-// coordinate plus the rounding of a later dot product with it; eps is +inf
-// when the sign of the denominator cannot be certified.
-template <typename Real, typename R4>
-__device__ __forceinline__ void cramer(const R4& a, const R4& b, const R4& c, Real& x,
-                                       Real& y, Real& z, Real& eps) {
+// Error bound of a corner obtained by Cramer's rule from its homogeneous
+// coordinates with denominator W, the permanents (pX, pY, pZ, pW) of the
+// four 3x3 minors and cm = max |corner coordinate|: a bound on
+// |corner - exact corner| per coordinate plus the rounding of a later
+// 4-term dot product with the corner.  +inf when the sign of W is not sure.
+template <typename Real>
+__device__ __forceinline__ Real cramer_bound(Real W, Real pX, Real pY, Real pZ, Real pW, Real cm) {
   using K = Consts<Real>;
-  const Real mxy = b.x * c.y - b.y * c.x, pxy = fabs(b.x * c.y) + fabs(b.y * c.x);
-  const Real mxz = b.x * c.z - b.z * c.x, pxz = fabs(b.x * c.z) + fabs(b.z * c.x);
-  const Real mxw = b.x * c.w - b.w * c.x, pxw = fabs(b.x * c.w) + fabs(b.w * c.x);
-  const Real myz = b.y * c.z - b.z * c.y, pyz = fabs(b.y * c.z) + fabs(b.z * c.y);
-  const Real myw = b.y * c.w - b.w * c.y, pyw = fabs(b.y * c.w) + fabs(b.w * c.y);
-  const Real mzw = b.z * c.w - b.w * c.z, pzw = fabs(b.z * c.w) + fabs(b.w * c.z);
-  const Real W = a.x * myz - a.y * mxz + a.z * mxy;
-  const Real X = -(a.w * myz + a.y * mzw - a.z * myw);
-  const Real Y = a.x * mzw + a.w * mxz - a.z * mxw;
-  const Real Z = -(a.x * myw - a.y * mxw + a.w * mxy);
-  const Real pW = fabs(a.x) * pyz + fabs(a.y) * pxz + fabs(a.z) * pxy;
-  const Real pX = fabs(a.w) * pyz + fabs(a.y) * pzw + fabs(a.z) * pyw;
-  const Real pY = fabs(a.x) * pzw + fabs(a.w) * pxz + fabs(a.z) * pxw;
-  const Real pZ = fabs(a.x) * pyw + fabs(a.y) * pxw + fabs(a.w) * pxy;
-  const Real inv = Real(1) / W;
+  const Real den = fabs(W) - K::kDet * pW;
+  if (!(den > Real(0))) return Real(INFINITY);
+  const Real pm = fmax(pX, fmax(pY, pZ));
+  return (K::kDet * (pm + cm * pW) / den + Real(2) * K::kUlp * cm + K::kDot * cm) * Real(1.0001);
+}
+
+// Permanents of the 3x3 minors of rows a, b, c used by Cramer's rule.
+template <typename Real, typename R4>
+__device__ __forceinline__ void cramer_perms(const R4& a, const R4& b, const R4& c, Real& pX,
+                                             Real& pY, Real& pZ, Real& pW) {
+  const Real pxy = fabs(b.x * c.y) + fabs(b.y * c.x), pxz = fabs(b.x * c.z) + fabs(b.z * c.x);
+  const Real pxw = fabs(b.x * c.w) + fabs(b.w * c.x), pyz = fabs(b.y * c.z) + fabs(b.z * c.y);
+  const Real pyw = fabs(b.y * c.w) + fabs(b.w * c.y), pzw = fabs(b.z * c.w) + fabs(b.w * c.z);
+  pW = fabs(a.x) * pyz + fabs(a.y) * pxz + fabs(a.z) * pxy;
+  pX = fabs(a.w) * pyz + fabs(a.y) * pzw + fabs(a.z) * pyw;
+  pY = fabs(a.x) * pzw + fabs(a.w) * pxz + fabs(a.z) * pxw;
+  pZ = fabs(a.x) * pyw + fabs(a.y) * pxw + fabs(a.w) * pxy;
+}
+
+// FP32 corner: Cramer's rule through the 2x2 minors of rows b, c.
+__device__ __forceinline__ void corner_fp32(const float4& a, const float4& b, const float4& c,
+                                            float& x, float& y, float& z, float& eps) {
+  const float mxy = b.x * c.y - b.y * c.x, mxz = b.x * c.z - b.z * c.x;
+  const float mxw = b.x * c.w - b.w * c.x, myz = b.y * c.z - b.z * c.y;
+  const float myw = b.y * c.w - b.w * c.y, mzw = b.z * c.w - b.w * c.z;
+  const float W = a.x * myz - a.y * mxz + a.z * mxy;
+  const float X = -(a.w * myz + a.y * mzw - a.z * myw);
+  const float Y = a.x * mzw + a.w * mxz - a.z * mxw;
+  const float Z = -(a.x * myw - a.y * mxw + a.w * mxy);
+  const float inv = 1.0f / W;
   x = X * inv;
   y = Y * inv;
   z = Z * inv;
-  const Real cm = fmax(fabs(x), fmax(fabs(y), fabs(z)));
-  const Real den = fabs(W) - K::kDet * pW;
-  if (!(den > Real(0))) {
-    eps = Real(INFINITY);
-  } else {
-    const Real pm = fmax(pX, fmax(pY, pZ));
-    eps = (K::kDet * (pm + cm * pW) / den + Real(2) * K::kUlp * cm + K::kDot * cm) *
-          Real(1.0001);
-  }
+  float pX, pY, pZ, pW;
+  cramer_perms<float>(a, b, c, pX, pY, pZ, pW);
+  eps = cramer_bound<float>(W, pX, pY, pZ, pW, fmaxf(fabsf(x), fmaxf(fabsf(y), fabsf(z))));
+}
+
+// FP64 corner exactly as the reference computes it, with its error bound.
+__device__ __forceinline__ void corner_fp64(const double4& a, const double4& b,
+                                            const double4& c, double& x, double& y, double& z,
+                                            float& eps) {
+  const double4 p = r_triangle_point(a, b, c);
+  x = __ddiv_rn(p.x, p.w);
+  y = __ddiv_rn(p.y, p.w);
+  z = __ddiv_rn(p.z, p.w);
+  double pX, pY, pZ, pW;
+  cramer_perms<double>(a, b, c, pX, pY, pZ, pW);
+  const double e =
+      cramer_bound<double>(p.w, pX, pY, pZ, pW, fmax(fabs(x), fmax(fabs(y), fabs(z))));
+  eps = __double2float_ru(e);
 }
 
 // ---------------------------------------------------------------------
 // Plane equations
 // ---------------------------------------------------------------------
 struct SeedCtx {
-  double4 pi;   // x, y, z, h
-  double qi;    // w - |p|^2
-  double wi;
+  double4 pi;     // x, y, z, h
+  double qi;      // w - |p|^2
+  float4 fh, fl;  // FP32 value and remainder of (x, y, z, h)
+  float2 fw;      // FP32 value and remainder of w
   double box[6];
 };
 
 // Power bisector of seed i and the plane's owner in the reference's global
 // frame, periodic_delaunay_3d.cpp:3722-3726, or a box face
 // (convex_cell.cpp:189-194).  Bit-identical to the reference's plane.
-__device__ __forceinline__ double4 plane_fp64(uint32_t ps, const SeedCtx& sc,
-                                              const SortedSeeds& S) {
-  if (ps >= kBoxBase) {
-    switch (ps - kBoxBase) {
-      case 0: return make_double4(1.0, 0.0, 0.0, -sc.box[0]);
-      case 1: return make_double4(-1.0, 0.0, 0.0, sc.box[3]);
-      case 2: return make_double4(0.0, 1.0, 0.0, -sc.box[1]);
-      case 3: return make_double4(0.0, -1.0, 0.0, sc.box[4]);
-      case 4: return make_double4(0.0, 0.0, 1.0, -sc.box[2]);
-      default: return make_double4(0.0, 0.0, -1.0, sc.box[5]);
+__device__ __forceinline__ double4 plane_fp64(uint32_t own, const double4& pi, double qi,
+                                              const double* box, const SortedSeeds& S) {
+  if (own >= kBoxBase) {
+    switch (own - kBoxBase) {
+      case 0: return make_double4(1.0, 0.0, 0.0, -box[0]);
+      case 1: return make_double4(-1.0, 0.0, 0.0, box[3]);
+      case 2: return make_double4(0.0, 1.0, 0.0, -box[1]);
+      case 3: return make_double4(0.0, -1.0, 0.0, box[4]);
+      case 4: return make_double4(0.0, 0.0, 1.0, -box[2]);
+      default: return make_double4(0.0, 0.0, -1.0, box[5]);
     }
   }
-  const double4 pj = S.xd[ps];
-  const double qj = S.q[ps];
-  return make_double4(2.0 * __dsub_rn(sc.pi.x, pj.x), 2.0 * __dsub_rn(sc.pi.y, pj.y),
-                      2.0 * __dsub_rn(sc.pi.z, pj.z), __dsub_rn(sc.qi, qj));
+  const double4 pj = S.xd[own];
+  const double qj = S.q[own];
+  return make_double4(2.0 * __dsub_rn(pi.x, pj.x), 2.0 * __dsub_rn(pi.y, pj.y),
+                      2.0 * __dsub_rn(pi.z, pj.z), __dsub_rn(qi, qj));
 }
 
-// The same plane translated to the frame centred on seed i, in FP32:
-// (-2 d, |d|^2 + w_i - w_j) with d = p_j - p_i rounded from FP64.
-__device__ __forceinline__ float4 plane_fp32(uint32_t ps, const SeedCtx& sc,
-                                             const SortedSeeds& S, const double* wsorted) {
-  if (ps >= kBoxBase) {
-    switch (ps - kBoxBase) {
-      case 0: return make_float4(1.f, 0.f, 0.f, (float)(sc.pi.x - sc.box[0]));
-      case 1: return make_float4(-1.f, 0.f, 0.f, (float)(sc.box[3] - sc.pi.x));
-      case 2: return make_float4(0.f, 1.f, 0.f, (float)(sc.pi.y - sc.box[1]));
-      case 3: return make_float4(0.f, -1.f, 0.f, (float)(sc.box[4] - sc.pi.y));
-      case 4: return make_float4(0.f, 0.f, 1.f, (float)(sc.pi.z - sc.box[2]));
-      default: return make_float4(0.f, 0.f, -1.f, (float)(sc.box[5] - sc.pi.z));
-    }
+// A box face in the frame centred on the seed, in FP32.
+__device__ __forceinline__ float4 box_plane_fp32(int b, const SeedCtx& sc) {
+  switch (b) {
+    case 0: return make_float4(1.f, 0.f, 0.f, (sc.fh.x - (float)sc.box[0]) + sc.fl.x);
+    case 1: return make_float4(-1.f, 0.f, 0.f, ((float)sc.box[3] - sc.fh.x) - sc.fl.x);
+    case 2: return make_float4(0.f, 1.f, 0.f, (sc.fh.y - (float)sc.box[1]) + sc.fl.y);
+    case 3: return make_float4(0.f, -1.f, 0.f, ((float)sc.box[4] - sc.fh.y) - sc.fl.y);
+    case 4: return make_float4(0.f, 0.f, 1.f, (sc.fh.z - (float)sc.box[2]) + sc.fl.z);
+    default: return make_float4(0.f, 0.f, -1.f, ((float)sc.box[5] - sc.fh.z) - sc.fl.z);
   }
-  const double4 pj = S.xd[ps];
-  const float dx = (float)(pj.x - sc.pi.x), dy = (float)(pj.y - sc.pi.y),
-              dz = (float)(pj.z - sc.pi.z);
-  const float dw = wsorted ? (float)(wsorted[ps] - sc.wi) : 0.f;
-  return make_float4(-2.f * dx, -2.f * dy, -2.f * dz, (dx * dx + dy * dy + dz * dz) - dw);
-}
-
-// ---------------------------------------------------------------------
-// Geometry of the final cell (FP64): volume, mg and facet areas with the
-// fans of ConvexCell::compute_mg / facet_area (convex_cell.cpp:1160-1307).
-// ---------------------------------------------------------------------
-template <int T, int P, class CornerFn, class TvFn, class TaFn>
-struct Geometry {
-  CornerFn corner;
-  TvFn tv;
-  TaFn ta;
-  __device__ __forceinline__ int find_vertex(uint32_t t, uint32_t v) const {
-    const uint32_t x = tv(t);
-    return ((x >> 8 & 0xFF) == v) + 2 * ((x >> 16 & 0xFF) == v);
-  }
-  __device__ __forceinline__ uint32_t adj(uint32_t t, int e) const {
-    return (ta(t) >> (8 * e)) & 0xFF;
-  }
-};
-
-__device__ __forceinline__ double tet_vol6(double3 p, double3 q, double3 r, double3 s) {
-  const double ux = q.x - p.x, uy = q.y - p.y, uz = q.z - p.z;
-  const double vx = r.x - p.x, vy = r.y - p.y, vz = r.z - p.z;
-  const double wx = s.x - p.x, wy = s.y - p.y, wz = s.z - p.z;
-  const double cx = uy * vz - uz * vy, cy = uz * vx - ux * vz, cz = ux * vy - uy * vx;
-  return fabs(cx * wx + cy * wy + cz * wz);
-}
-
-__device__ __forceinline__ double tri_area2(double3 p, double3 q, double3 r) {
-  const double ux = q.x - p.x, uy = q.y - p.y, uz = q.z - p.z;
-  const double vx = r.x - p.x, vy = r.y - p.y, vz = r.z - p.z;
-  const double wx = uy * vz - uz * vy, wy = uz * vx - ux * vz, wz = ux * vy - uy * vx;
-  return sqrt(wx * wx + wy * wy + wz * wz);
 }
 
 // ---------------------------------------------------------------------
 // The kernel
 // ---------------------------------------------------------------------
 template <typename Real, int T, int P>
-__global__ void __launch_bounds__(kClipThreads)
-clip_kernel(ClipArgs a) {
+__global__ void __launch_bounds__(kClipThreads) clip_kernel(ClipArgs a) {
   constexpr int BS = kClipThreads;
   constexpr int NWT = (T + 63) / 64;
-  using Smem = CellSmem<Real, BS, T, P>;
-  using R4 = typename std::conditional<std::is_same<Real, double>::value, double4, float4>::type;
   constexpr bool kFP64 = std::is_same<Real, double>::value;
+  using Smem = CellSmem<Real, BS, T, P>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
   const int tid = threadIdx.x;
@@ -289,41 +273,42 @@ clip_kernel(ClipArgs a) {
   if (qi >= a.nq) return;
   const SortedSeeds& S = a.S;
   const uint32_t s = a.qlist ? a.qlist[qi] : qi;
+  const uint32_t row = a.qrow ? a.qrow[qi] : qi;
 
   SeedCtx sc;
   sc.pi = S.xd[s];
-  sc.qi = S.q[s];
-  sc.wi = S.ws ? S.ws[s] : 0.0;
 #pragma unroll
   for (int c = 0; c < 6; ++c) sc.box[c] = a.box[c];
-  const double hi2 = sc.pi.w * sc.pi.w;
+  if constexpr (kFP64) {
+    sc.qi = S.q[s];
+  } else {
+    sc.fh = S.xf[s];
+    sc.fl = S.xl[s];
+    sc.fw = S.wf ? S.wf[s] : make_float2(0.f, 0.f);
+  }
+  const double hi2 = __dmul_rn(sc.pi.w, sc.pi.w);
+  const float hi2f = sc.fh.w * sc.fh.w;
 
-  auto plane_of = [&](uint32_t p) -> R4 {
-    if constexpr (kFP64) {
-      return plane_fp64(sm.pslot[p][tid], sc, S);
-    } else {
-      return sm.plane[p][tid];
-    }
+  // Plane p's equation (FP64: recomputed from its owner, FP32: stored).
+  auto plane_of = [&](uint32_t p) {
+    if constexpr (kFP64) return plane_fp64(sm.pown[p][tid], sc.pi, sc.qi, sc.box, S);
+    else return sm.pl[p][tid];
   };
-  auto r2_of = [&](uint32_t t) -> float {
+  // Creates the corner of triangle t from its planes; returns its r2.
+  auto make_corner = [&](uint32_t t, const auto& pa, const auto& pb, const auto& pc) -> Real {
     if constexpr (kFP64) {
-      return unpack_lo(sm.corner[t][tid].w);
-    } else {
-      const float4 c = sm.corner[t][tid];
-      return c.x * c.x + c.y * c.y + c.z * c.z;
-    }
-  };
-  // stores the corner of triangle t from its three planes; returns its r2
-  auto make_corner = [&](uint32_t t, const R4& pa, const R4& pb, const R4& pc) -> float {
-    Real x, y, z, eps;
-    cramer<Real>(pa, pb, pc, x, y, z, eps);
-    if constexpr (kFP64) {
-      const double dx = x - sc.pi.x, dy = y - sc.pi.y, dz = z - sc.pi.z;
-      const float r2 = __double2float_ru(dx * dx + dy * dy + dz * dz) * 1.0000002f;
-      sm.corner[t][tid] = make_double4(x, y, z, pack2f(r2, __double2float_ru(eps)));
+      double x, y, z;
+      float e;
+      corner_fp64(pa, pb, pc, x, y, z, e);
+      const double r2 = r_sqdist(sc.pi.x, sc.pi.y, sc.pi.z, make_double3(x, y, z));
+      sm.cxy[t][tid] = make_double2(x, y);
+      sm.czr[t][tid] = make_double2(z, r2);
+      sm.eps[t][tid] = e;
       return r2;
     } else {
-      sm.corner[t][tid] = make_float4(x, y, z, eps);
+      float x, y, z, e;
+      corner_fp32(pa, pb, pc, x, y, z, e);
+      sm.c4[t][tid] = make_float4(x, y, z, e);
       return x * x + y * y + z * z;
     }
   };
@@ -331,12 +316,12 @@ clip_kernel(ClipArgs a) {
   // ---- init_with_box (convex_cell.cpp:175-215): 6 planes, 8 corners
 #pragma unroll
   for (int b = 0; b < 6; ++b) {
-    sm.pslot[b][tid] = kBoxBase + b;
     sm.prank[b][tid] = 0xFFFF;
-    if constexpr (!kFP64) sm.plane[b][tid] = plane_fp32(kBoxBase + b, sc, S, S.ws);
+    if constexpr (kFP64) sm.pown[b][tid] = kBoxBase + b;
+    else sm.pl[b][tid] = box_plane_fp32(b, sc);
   }
   {
-    // triangles and adjacency of the box, in the reference's order
+    // triangles and adjacency of the box corners, in the reference's order
     const uint32_t bt[8] = {2 | 5 << 8 | 0 << 16, 5 | 3 << 8 | 0 << 16, 1 | 5 << 8 | 2 << 16,
                             5 | 1 << 8 | 3 << 16, 4 | 2 << 8 | 0 << 16, 4 | 0 << 8 | 3 << 16,
                             2 | 4 << 8 | 1 << 16, 4 | 3 << 8 | 1 << 16};
@@ -347,112 +332,154 @@ clip_kernel(ClipArgs a) {
     for (int t = 0; t < 8; ++t) {
       sm.tv[t][tid] = bt[t];
       sm.ta[t][tid] = ba[t];
+      sm.key[t][tid] = (int16_t)(-t);  // each pushed at the head of the list
     }
   }
   Bits<NWT> valid;
   valid.clear();
-  float R2 = 0.f;
+  Real R2 = 0;
   for (int t = 0; t < 8; ++t) {
     valid.set(t);
     const uint32_t v = sm.tv[t][tid];
-    float r2 = make_corner(t, plane_of(v & 0xFF), plane_of(v >> 8 & 0xFF), plane_of(v >> 16 & 0xFF));
-    R2 = fmaxf(R2, r2);
+    const Real r2 = make_corner(t, plane_of(v & 0xFF), plane_of(v >> 8 & 0xFF),
+                                plane_of(v >> 16 & 0xFF));
+    R2 = fmax(R2, r2);
   }
   uint64_t pused = 0x3Full;
-  bool recycled = false;
+  int parity = 1;
 
-  const uint32_t row = a.qrow ? a.qrow[qi] : qi;
   const uint32_t cnt_raw = a.nbr_cnt[row];
   const bool dup = (cnt_raw >> 31) != 0;
   const uint32_t cnt = dup ? 0u : cnt_raw;
-  int32_t st;
+  int32_t st = -1;
   uint32_t jj = 0;
-  uint32_t stop_slot = kNone;
   unsigned long long n_exact = 0;
 
   if (dup) {
     st = CELL_DUPLICATE;
   } else {
-    st = -1;
     for (; jj < cnt; ++jj) {
       const uint32_t j = a.nbr[(size_t)jj * a.nbr_stride + row];
-      const double4 pj = S.xd[j];
-      // ---- security radius (generic_RVD.h:2300-2324)
-      if (a.check_sr) {
-        if constexpr (kFP64) {
+      // ---- security radius (generic_RVD.h:2300-2324) and the plane
+      float4 Pf = make_float4(0.f, 0.f, 0.f, 0.f);
+      double4 Pd = make_double4(0.0, 0.0, 0.0, 0.0);
+      if constexpr (kFP64) {
+        const double4 pj = S.xd[j];
+        if (a.check_sr) {
           const double dij = dist2_exact(sc.pi, pj);
-          if (dij > 4.1 * ((double)R2 + hi2)) {
+          if (dij > __dmul_rn(4.1, __dadd_rn(R2, hi2))) {
             st = CELL_CERTIFIED;
-            stop_slot = j;
-            break;
-          }
-        } else {
-          const float dx = (float)(pj.x - sc.pi.x), dy = (float)(pj.y - sc.pi.y),
-                      dz = (float)(pj.z - sc.pi.z), dh = (float)(pj.w - sc.pi.w);
-          const float dij = dx * dx + dy * dy + dz * dz + dh * dh;
-          if (dij > 4.1f * (R2 + (float)hi2)) {
-            st = CELL_CERTIFIED;
-            stop_slot = j;
             break;
           }
         }
-      }
-      if (!valid.any()) continue;  // empty cell: nothing left to clip
-      // ---- the plane
-      R4 Pn;
-      Real bw;
-      if constexpr (kFP64) {
-        Pn = plane_fp64(j, sc, S);
-        bw = Consts<double>::kDot * fabs(Pn.w);
+        Pd = make_double4(2.0 * __dsub_rn(sc.pi.x, pj.x), 2.0 * __dsub_rn(sc.pi.y, pj.y),
+                          2.0 * __dsub_rn(sc.pi.z, pj.z), __dsub_rn(sc.qi, S.q[j]));
       } else {
-        Pn = plane_fp32(j, sc, S, S.ws);
-        const double qj = S.q[j];
-        // rounding of the reference's FP64 planes, seen from FP32
-        const float ref_term = (float)(3.5527136788005009e-15 *
-                                       (fabs(sc.qi) + fabs(qj) +
-                                        (double)pabs1(Pn) * (fmax(fabs(sc.pi.x), fmax(fabs(sc.pi.y), fabs(sc.pi.z))) + 1.0)));
-        bw = Consts<float>::kDot * fabsf(Pn.w) + ref_term;
+        // d = p_j - p_i from the value/remainder pairs keeps FP32 relative
+        // accuracy however close the two seeds are
+        const float4 jh = S.xf[j], jl = S.xl[j];
+        const float dx = (jh.x - sc.fh.x) + (jl.x - sc.fl.x);
+        const float dy = (jh.y - sc.fh.y) + (jl.y - sc.fl.y);
+        const float dz = (jh.z - sc.fh.z) + (jl.z - sc.fl.z);
+        const float dh = (jh.w - sc.fh.w) + (jl.w - sc.fl.w);
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        if (a.check_sr && d2 + dh * dh > 4.1f * (R2 + hi2f)) {
+          st = CELL_CERTIFIED;
+          break;
+        }
+        float dw = 0.f;
+        if (S.wf) {
+          const float2 wj = S.wf[j];
+          dw = (wj.x - sc.fw.x) + (wj.y - sc.fw.y);
+        }
+        // (-2 d, |d|^2 + w_i - w_j): the bisector in the seed's frame
+        Pf = make_float4(-2.f * dx, -2.f * dy, -2.f * dz, d2 - dw);
       }
-      const Real pa1 = pabs1(Pn) * Real(1.0001);
-      bw *= Real(1.0001);
+      // every clip relinks the reference's valid list in reverse order
+      const int par_old = parity;
+      parity = -parity;
+      if (!valid.any()) continue;  // empty cell: nothing left to clip
+      Real pa1, bw;
+      if constexpr (kFP64) {
+        pa1 = (fabs(Pd.x) + fabs(Pd.y) + fabs(Pd.z)) * 1.0001;
+        bw = Consts<double>::kDot * fabs(Pd.w) * 1.0001;
+      } else {
+        pa1 = (fabsf(Pf.x) + fabsf(Pf.y) + fabsf(Pf.z)) * 1.0001f;
+        // the reference's own FP64 planes carry a rounding of about
+        // 2^-52 (|w_i| + |w_j| + |p_i|^2 + |p_j|^2) in their offset
+        const float wj = S.wf ? S.wf[j].x : 0.f;
+        const float pn = sc.fh.x * sc.fh.x + sc.fh.y * sc.fh.y + sc.fh.z * sc.fh.z;
+        const float qmag = fabsf(sc.fw.x) + fabsf(wj) + 2.f * pn + 1.f;
+        bw = (Consts<float>::kDot * fabsf(Pf.w) + 3.5527137e-15f * qmag) * 1.0001f;
+      }
       // ---- conflict scan (triangle_is_in_conflict, convex_cell.cpp:870-912)
       Bits<NWT> conflict;
       conflict.clear();
-      float newR2 = 0.f;
+      Real keepR2 = 0;
+      int keep_max_eff = -0x7FFF;
       bool uncertain = false;
+      auto test = [&](int t) {
+        Real cx, cy, cz, r2, eps;
+        if constexpr (kFP64) {
+          const double2 xy = sm.cxy[t][tid], zr = sm.czr[t][tid];
+          cx = xy.x;
+          cy = xy.y;
+          cz = zr.x;
+          r2 = zr.y;
+          eps = (double)sm.eps[t][tid];
+        } else {
+          const float4 c = sm.c4[t][tid];
+          cx = c.x;
+          cy = c.y;
+          cz = c.z;
+          eps = c.w;
+          r2 = cx * cx + cy * cy + cz * cz;
+        }
+        Real sv;
+        if constexpr (kFP64) sv = fma(Pd.z, cz, fma(Pd.y, cy, fma(Pd.x, cx, Pd.w)));
+        else sv = fmaf(Pf.z, cz, fmaf(Pf.y, cy, fmaf(Pf.x, cx, Pf.w)));
+        const Real bound = fma(pa1, eps, bw);
+        bool in_conflict;
+        if (sv < -bound) {
+          in_conflict = true;
+        } else if (sv > bound) {
+          in_conflict = false;
+        } else {
+          if constexpr (kFP64) {
+            const uint32_t v = sm.tv[t][tid];
+            const double4 p0 = plane_of(v & 0xFF), p1 = plane_of(v >> 8 & 0xFF),
+                          p2 = plane_of(v >> 16 & 0xFF);
+            const double r0[4] = {p0.x, p0.y, p0.z, p0.w}, r1[4] = {p1.x, p1.y, p1.z, p1.w},
+                         rr2[4] = {p2.x, p2.y, p2.z, p2.w}, r3[4] = {Pd.x, Pd.y, Pd.z, Pd.w};
+            in_conflict = det4_sign_exact(r0, r1, rr2, r3) >= 0;
+            ++n_exact;
+          } else {
+            uncertain = true;
+            in_conflict = false;
+          }
+        }
+        if (in_conflict) {
+          conflict.set(t);
+        } else {
+          keepR2 = fmax(keepR2, r2);
+          keep_max_eff = max(keep_max_eff, par_old * (int)sm.key[t][tid]);
+        }
+      };
 #pragma unroll
       for (int wi = 0; wi < NWT; ++wi) {
         uint64_t m = valid.w[wi];
         while (m) {
-          const int t = wi * 64 + __ffsll((long long)m) - 1;
+          // four triangles per iteration, so that their loads overlap
+          const int t0 = wi * 64 + __ffsll((long long)m) - 1;
           m &= m - 1;
-          const R4 c = sm.corner[t][tid];
-          Real eps;
-          if constexpr (kFP64) eps = (double)unpack_hi(c.w);
-          else eps = c.w;
-          const Real sv = fma(Pn.z, c.z, fma(Pn.y, c.y, fma(Pn.x, c.x, Pn.w)));
-          const Real bound = fma(pa1, eps, bw);
-          bool in_conflict;
-          if (sv < -bound) {
-            in_conflict = true;
-          } else if (sv > bound) {
-            in_conflict = false;
-          } else {
-            if constexpr (kFP64) {
-              const uint32_t v = sm.tv[t][tid];
-              const double4 p0 = plane_of(v & 0xFF), p1 = plane_of(v >> 8 & 0xFF),
-                            p2 = plane_of(v >> 16 & 0xFF);
-              const double r0[4] = {p0.x, p0.y, p0.z, p0.w}, r1[4] = {p1.x, p1.y, p1.z, p1.w},
-                           rr2[4] = {p2.x, p2.y, p2.z, p2.w}, r3[4] = {Pn.x, Pn.y, Pn.z, Pn.w};
-              in_conflict = det4_sign_exact(r0, r1, rr2, r3) >= 0;
-              ++n_exact;
-            } else {
-              uncertain = true;
-              in_conflict = false;
-            }
-          }
-          if (in_conflict) conflict.set(t);
-          else newR2 = fmaxf(newR2, r2_of(t));
+          int t1 = -1, t2 = -1, t3 = -1;
+          if (m) { t1 = wi * 64 + __ffsll((long long)m) - 1; m &= m - 1; }
+          if (m) { t2 = wi * 64 + __ffsll((long long)m) - 1; m &= m - 1; }
+          if (m) { t3 = wi * 64 + __ffsll((long long)m) - 1; m &= m - 1; }
+          test(t0);
+          if (t1 >= 0) test(t1);
+          if (t2 >= 0) test(t2);
+          if (t3 >= 0) test(t3);
         }
       }
       if (!kFP64 && uncertain) {
@@ -462,14 +489,15 @@ clip_kernel(ClipArgs a) {
       if (!conflict.any()) continue;
       if (conflict.equals(valid)) {  // the whole cell is clipped away
         valid.clear();
-        R2 = 0.f;
+        R2 = 0;
         continue;
       }
       // ---- a slot for the new plane (recycle planes no triangle uses)
-      uint64_t freep = ~pused & (P >= 64 ? ~0ull : ((1ull << P) - 1ull));
+      const uint64_t pmask = (P >= 64) ? ~0ull : ((1ull << P) - 1ull);
+      uint64_t freep = ~pused & pmask;
       if (!freep) {
         uint64_t used = 0;
-        Bits<NWT> keep = andnot(valid, conflict);
+        const Bits<NWT> keep = andnot(valid, conflict);
 #pragma unroll
         for (int wi = 0; wi < NWT; ++wi) {
           uint64_t m = keep.w[wi];
@@ -481,8 +509,7 @@ clip_kernel(ClipArgs a) {
           }
         }
         pused = used;
-        recycled = true;
-        freep = ~pused & (P >= 64 ? ~0ull : ((1ull << P) - 1ull));
+        freep = ~pused & pmask;
         if (!freep) {
           st = CELL_OVERFLOW;
           break;
@@ -490,12 +517,13 @@ clip_kernel(ClipArgs a) {
       }
       const uint32_t lv = (uint32_t)(__ffsll((long long)freep) - 1);
       pused |= 1ull << lv;
-      sm.pslot[lv][tid] = j;
       sm.prank[lv][tid] = (uint16_t)jj;
-      if constexpr (!kFP64) sm.plane[lv][tid] = Pn;
+      if constexpr (kFP64) sm.pown[lv][tid] = j;
+      else sm.pl[lv][tid] = Pf;
       // ---- border of the conflict zone (triangulate_conflict_zone)
       int nborder = 0;
       uint32_t first_v = 0;
+      int best = -0x7FFFFFFF;
 #pragma unroll
       for (int wi = 0; wi < NWT; ++wi) {
         uint64_t m = conflict.w[wi];
@@ -508,15 +536,22 @@ clip_kernel(ClipArgs a) {
             const uint32_t nb = (ad >> (8 * e)) & 0xFF;
             if (conflict.test((int)nb)) continue;
             // edge opposite vertex e runs v[e+1] -> v[e+2] in t; the kept
-            // triangle nb holds it reversed, so walking the border along
-            // nb's orientation goes v[e+2] -> v[e+1]
+            // triangle nb holds it reversed, so the border walk, which
+            // follows nb's orientation, goes from y = v[e+2] to x = v[e+1]
             const uint32_t x = (v >> (8 * ((e + 1) % 3))) & 0xFF;
             const uint32_t y = (v >> (8 * ((e + 2) % 3))) & 0xFF;
             const uint32_t an = sm.ta[nb][tid];
-            const uint32_t eb = ((an >> 8 & 0xFF) == (uint32_t)t) + 2 * ((an >> 16 & 0xFF) == (uint32_t)t);
+            const uint32_t eb =
+                ((an >> 8 & 0xFF) == (uint32_t)t) + 2 * ((an >> 16 & 0xFF) == (uint32_t)t);
             sm.pnext[y][tid] = (uint8_t)x;
             sm.pnb[y][tid] = (uint16_t)(nb | (eb << 8));
-            first_v = y;
+            // the reference starts its walk at the border edge it meets last
+            // while scanning the relinked list (new eff = -old eff)
+            const int score = -par_old * (int)sm.key[nb][tid] * 4 + (int)eb;
+            if (score > best) {
+              best = score;
+              first_v = y;
+            }
             ++nborder;
           }
         }
@@ -529,55 +564,59 @@ clip_kernel(ClipArgs a) {
       // ---- fan new triangles (lv, next, v) around the border
       Bits<NWT> freet = andnot(full_bits<NWT>(T), andnot(valid, conflict));
       valid = andnot(valid, conflict);
-      R2 = newR2;
+      R2 = keepR2;
+      const int key_base = -keep_max_eff - 1;
       uint32_t v = first_v;
-      int prev_t = -1, first_t = -1;
-      R4 Pv = plane_of(v);
-      int steps = 0;
+      int prev_t = -1, first_t = -1, created = 0;
+      auto Pv = plane_of(v);
       do {
-        if (++steps > nborder) break;  // not a simple cycle: reported below
+        if (created >= nborder) break;  // not a simple cycle: reported below
         const uint32_t x = sm.pnext[v][tid];
         const uint32_t nbinfo = sm.pnb[v][tid];
         const uint32_t tn = nbinfo & 0xFF, eb = nbinfo >> 8;
         const int nt = freet.first();
-        freet.w[nt >> 6] &= ~(1ull << (nt & 63));
+        freet.reset(nt);
         valid.set(nt);
         sm.tv[nt][tid] = lv | (x << 8) | (v << 16);
         sm.ta[nt][tid] = tn | ((uint32_t)(prev_t < 0 ? 0 : prev_t) << 8);
+        sm.key[nt][tid] = (int16_t)(parity * (key_base - created));
         {
           uint32_t an = sm.ta[tn][tid];
           an = (an & ~(0xFFu << (8 * eb))) | ((uint32_t)nt << (8 * eb));
           sm.ta[tn][tid] = an;
         }
-        const R4 Px = plane_of(x);
-        const float r2 = make_corner(nt, Pn, Px, Pv);
-        R2 = fmaxf(R2, r2);
+        const auto Px = plane_of(x);
+        Real r2;
+        if constexpr (kFP64) r2 = make_corner(nt, Pd, Px, Pv);
+        else r2 = make_corner(nt, Pf, Px, Pv);
+        R2 = fmax(R2, r2);
         if (prev_t >= 0) {
-          uint32_t ap = sm.ta[prev_t][tid];
+          const uint32_t ap = sm.ta[prev_t][tid];
           sm.ta[prev_t][tid] = (ap & 0x0000FFFFu) | ((uint32_t)nt << 16);
         } else {
           first_t = nt;
         }
         prev_t = nt;
+        ++created;
         v = x;
         Pv = Px;
       } while (v != first_v);
-      if (v != first_v || steps != nborder) {
+      if (v != first_v || created != nborder) {
         st = CELL_ERROR;
         break;
       }
       {
-        uint32_t ap = sm.ta[prev_t][tid];
+        const uint32_t ap = sm.ta[prev_t][tid];
         sm.ta[prev_t][tid] = (ap & 0x0000FFFFu) | ((uint32_t)first_t << 16);
-        uint32_t af = sm.ta[first_t][tid];
+        const uint32_t af = sm.ta[first_t][tid];
         sm.ta[first_t][tid] = (af & 0xFFFF00FFu) | ((uint32_t)prev_t << 8);
       }
     }
     if (st < 0) {
       // list exhausted without certification
       const bool complete = (cnt < a.list_k) || (a.list_k >= a.n_total - 1);
-      st = (complete || !a.check_sr) ? (a.check_sr ? CELL_ALL_NEIGHBOURS : CELL_CERTIFIED)
-                                     : CELL_NEED_MORE_K;
+      if (!a.check_sr) st = CELL_CERTIFIED;
+      else st = complete ? CELL_ALL_NEIGHBOURS : CELL_NEED_MORE_K;
     }
   }
   if (a.counters) {
@@ -587,172 +626,49 @@ clip_kernel(ClipArgs a) {
     if ((unsigned)(tid & 31) == (unsigned)(__ffs(amask) - 1))
       atomicMax(&a.counters[1], (unsigned long long)mx);
   }
-
-  if (st == CELL_RECHECK || st == CELL_OVERFLOW || st == CELL_NEED_MORE_K ||
-      st == CELL_ERROR) {
-    a.status[s] = st;
-    a.nclip[s] = jj;
+  a.status[s] = st;
+  a.nclip[s] = jj;
+  if (st == CELL_RECHECK || st == CELL_OVERFLOW || st == CELL_NEED_MORE_K || st == CELL_ERROR)
     return;
-  }
 
-  // ---- FP64 corners of the final cell
-  // FP64 kernel: cached.  FP32 kernel: recomputed from the reference's
-  // FP64 planes into the space of the FP32 corners and planes.
-  auto corner64 = [&](uint32_t t) -> double3 {
-    if constexpr (kFP64) {
-      const double4 c = sm.corner[t][tid];
-      return make_double3(c.x, c.y, c.z);
-    } else {
-      const double2 xy = reinterpret_cast<const double2(*)[BS]>(&sm.corner[0][0])[t][tid];
-      const double zz = reinterpret_cast<const double(*)[BS]>(&sm.plane[0][0])[t][tid];
-      return make_double3(xy.x, xy.y, zz);
-    }
-  };
-  if constexpr (!kFP64) {
-    static_assert(sizeof(sm.plane) >= sizeof(double) * T * BS, "plane space too small");
-    double R2_64 = 0.0;
-#pragma unroll
-    for (int wi = 0; wi < NWT; ++wi) {
-      uint64_t m = valid.w[wi];
-      while (m) {
-        const int t = wi * 64 + __ffsll((long long)m) - 1;
-        m &= m - 1;
-        const uint32_t v = sm.tv[t][tid];
-        const double4 p0 = plane_fp64(sm.pslot[v & 0xFF][tid], sc, S);
-        const double4 p1 = plane_fp64(sm.pslot[v >> 8 & 0xFF][tid], sc, S);
-        const double4 p2 = plane_fp64(sm.pslot[v >> 16 & 0xFF][tid], sc, S);
-        double x, y, z, eps;
-        cramer<double>(p0, p1, p2, x, y, z, eps);
-        reinterpret_cast<double2(*)[BS]>(&sm.corner[0][0])[t][tid] = make_double2(x, y);
-        reinterpret_cast<double(*)[BS]>(&sm.plane[0][0])[t][tid] = z;
-        const double dx = x - sc.pi.x, dy = y - sc.pi.y, dz = z - sc.pi.z;
-        R2_64 = fmax(R2_64, dx * dx + dy * dy + dz * dz);
-      }
-    }
-    // the FP32 stop must also hold in FP64
-    if (st == CELL_CERTIFIED && stop_slot != kNone) {
-      const double dij = dist2_exact(sc.pi, S.xd[stop_slot]);
-      if (!(dij > 4.1 * (R2_64 + hi2))) {
-        a.status[s] = CELL_RECHECK;
-        a.nclip[s] = jj;
-        return;
-      }
-    }
-  }
-
-  // ---- v2t (pnext reused): one triangle per contributing plane
-#pragma unroll
-  for (int p = 0; p < P; ++p) sm.pnext[p][tid] = 0xFF;
+  // ---- the combinatorics, for the geometry kernel
+  const CombBuf& cb = a.comb;
+  const size_t tb = (size_t)s * kTMax, pb = (size_t)s * kPMax;
 #pragma unroll
   for (int wi = 0; wi < NWT; ++wi) {
     uint64_t m = valid.w[wi];
     while (m) {
       const int t = wi * 64 + __ffsll((long long)m) - 1;
       m &= m - 1;
-      const uint32_t v = sm.tv[t][tid];
-      sm.pnext[v & 0xFF][tid] = (uint8_t)t;
-      sm.pnext[v >> 8 & 0xFF][tid] = (uint8_t)t;
-      sm.pnext[v >> 16 & 0xFF][tid] = (uint8_t)t;
+      cb.tv[tb + t] = sm.tv[t][tid];
+      cb.ta[tb + t] = sm.ta[t][tid];
+      cb.key[tb + t] = sm.key[t][tid];
     }
   }
-  auto find_vertex = [&](uint32_t t, uint32_t v) -> int {
-    const uint32_t x = sm.tv[t][tid];
-    return ((x >> 8 & 0xFF) == v) + 2 * ((x >> 16 & 0xFF) == v);
-  };
-  auto adjacent = [&](uint32_t t, int e) -> uint32_t { return (sm.ta[t][tid] >> (8 * e)) & 0xFF; };
-
-  // ---- volume and mg (compute_mg): fans of tets from one corner
-  double m = 0.0, gx = 0.0, gy = 0.0, gz = 0.0;
-  {
-    int t_origin = -1;
-    double3 po = make_double3(0, 0, 0);
-    for (int p = 0; p < P; ++p) {
-      const uint32_t t0 = sm.pnext[p][tid];
-      if (t0 == 0xFF) continue;
-      if (t_origin < 0) {
-        t_origin = (int)t0;
-        po = corner64(t0);
-        continue;
-      }
-      uint32_t t = t0;
-      int cur = 0;
-      double3 q1 = make_double3(0, 0, 0), q2 = q1;
-      int guard = 0;
-      do {
-        const double3 pt = corner64(t);
-        if (cur == 0) q1 = pt;
-        else if (cur == 1) q2 = pt;
-        else {
-          const double cm = tet_vol6(po, q1, q2, pt) / 6.0;
-          m += cm;
-          gx += cm * (po.x + q1.x + q2.x + pt.x) / 4.0;
-          gy += cm * (po.y + q1.y + q2.y + pt.y) / 4.0;
-          gz += cm * (po.z + q1.z + q2.z + pt.z) / 4.0;
-          q2 = pt;
-        }
-        ++cur;
-        const int lvx = find_vertex(t, (uint32_t)p);
-        t = adjacent(t, (lvx + 1) % 3);
-      } while (t != t0 && ++guard < T);
+  for (uint64_t m = pused; m; m &= m - 1) {
+    const int p = __ffsll((long long)m) - 1;
+    const uint16_t rk = sm.prank[p][tid];
+    uint32_t own;
+    if constexpr (kFP64) {
+      own = sm.pown[p][tid];
+    } else {
+      // box faces only ever occupy their initial slots 0-5
+      own = (rk == 0xFFFF) ? kBoxBase + (uint32_t)p : a.nbr[(size_t)rk * a.nbr_stride + row];
     }
+    cb.pown[pb + p] = own;
+    cb.prank[pb + p] = rk;
   }
-  a.vol[s] = m;
-  a.mg[s] = gx;
-  a.mg[(size_t)a.out_stride + s] = gy;
-  a.mg[2 * (size_t)a.out_stride + s] = gz;
-
-  // ---- facets between seeds, in the reference's order (clipping order)
-  uint32_t nfac = 0;
-  for (int p = 0; p < P; ++p) {
-    const uint32_t t0 = sm.pnext[p][tid];
-    const uint32_t ps = sm.pslot[p][tid];
-    if (t0 == 0xFF || ps >= kBoxBase) continue;
-    double area = 0.0;
-    uint32_t t = t0;
-    int cur = 0;
-    double3 q0 = make_double3(0, 0, 0), q1 = q0;
-    int guard = 0;
-    do {
-      const double3 pt = corner64(t);
-      if (cur == 0) q0 = pt;
-      else if (cur == 1) q1 = pt;
-      else {
-        area += 0.5 * tri_area2(q0, q1, pt);
-        q1 = pt;
-      }
-      ++cur;
-      const int lvx = find_vertex(t, (uint32_t)p);
-      t = adjacent(t, (lvx + 1) % 3);
-    } while (t != t0 && ++guard < T);
-    uint32_t pos = nfac;
-    if (recycled) {
-      // order among contributing seed planes by list position
-      pos = 0;
-      const uint16_t rk = sm.prank[p][tid];
-      for (int p2 = 0; p2 < P; ++p2) {
-        if (sm.pnext[p2][tid] == 0xFF || sm.pslot[p2][tid] >= kBoxBase) continue;
-        pos += (sm.prank[p2][tid] < rk);
-      }
-    }
-    a.f_nbr[(size_t)pos * a.out_stride + s] = S.perm[ps];
-    a.f_area[(size_t)pos * a.out_stride + s] = area;
-    ++nfac;
-  }
-  a.nf[s] = nfac;
-  a.nclip[s] = jj;
-  a.status[s] = st;
+  cb.tmask[s] = make_ulonglong2(valid.w[0], NWT > 1 ? valid.w[NWT - 1] : 0ull);
+  cb.pmask[s] = pused;
+  cb.flags[s] = parity < 0 ? 1u : 0u;
 }
 
 template <typename Real, int T, int P>
 static void launch_clip(const ClipArgs& a, cudaStream_t st) {
   if (a.nq == 0) return;
   const size_t sh = sizeof(CellSmem<Real, kClipThreads, T, P>);
-  static bool configured = false;
-  if (!configured) {
-    cudaFuncSetAttribute(clip_kernel<Real, T, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)sh);
-    configured = true;
-  }
+  cudaFuncSetAttribute(clip_kernel<Real, T, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)sh);
   const unsigned nb = (a.nq + kClipThreads - 1) / kClipThreads;
   clip_kernel<Real, T, P><<<nb, kClipThreads, sh, st>>>(a);
   last_launch_error = cudaGetLastError();

@@ -1,22 +1,37 @@
-// Laguerre cell clipping kernels (declarations).
+// Laguerre cell clipping and geometry kernels (declarations).
 #pragma once
 
 #include "gbv_grid.cuh"
 
 namespace gbv {
 
-// Capacities of the two kernel shapes.  The small one runs every cell; the
-// large one runs the few cells whose polytope overflows the small one.
+// Capacities of the two clipping shapes.  The small one runs every cell;
+// the large one runs the few cells whose polytope overflows the small one.
 constexpr int kSmallT = 64, kSmallP = 32;
 constexpr int kLargeT = 128, kLargeP = 64;
-constexpr int kMaxFacets = kLargeP;  // facet slots per cell in the outputs
+constexpr int kTMax = kLargeT, kPMax = kLargeP;
+constexpr int kMaxFacets = kLargeP;   // facet slots per cell in the outputs
+constexpr uint32_t kBoxBase = 0xFFFFFF00u;  // plane owner of box face b: kBoxBase + b
+
+// Combinatorics of the clipped cells, one record per sorted slot, written
+// by the clipping kernels and read by the geometry kernel.
+struct CombBuf {
+  uint32_t* tv;     // [n][kTMax] plane slots of each triangle, i | j<<8 | k<<16
+  uint32_t* ta;     // [n][kTMax] adjacent triangles across edges opposite i, j, k
+  int16_t* key;     // [n][kTMax] stored list-order key (effective = parity * key)
+  uint32_t* pown;   // [n][kPMax] plane owner: seed slot or kBoxBase + face
+  uint16_t* prank;  // [n][kPMax] position of the plane's seed in the neighbour list
+  ulonglong2* tmask;  // [n] used triangle slots (bits 0-63, 64-127)
+  uint64_t* pmask;    // [n] used plane slots
+  uint32_t* flags;    // [n] bit 0: parity is -1
+};
 
 struct ClipArgs {
   SortedSeeds S;
-  // neighbour lists: list r of query qi at nbr[r * nbr_stride + qi]
+  // neighbour lists: list position r of list row `row` at nbr[r * nbr_stride + row]
   const uint32_t* nbr;
   uint32_t nbr_stride;
-  const uint32_t* nbr_cnt;    // [nq]; bit 31 = lower-index duplicate
+  const uint32_t* nbr_cnt;    // per row; bit 31 = lower-index duplicate
   uint32_t list_k;            // capacity of the lists
   uint32_t n_total;           // number of seeds
   const uint32_t* qlist;      // sorted slots to process (nullptr: all)
@@ -24,29 +39,47 @@ struct ClipArgs {
   uint32_t nq;
   double box[6];              // xmin ymin zmin xmax ymax zmax
   int check_sr;
-  // outputs indexed by sorted slot
-  int32_t* status;
-  double* vol;
-  double* mg;                 // [3][n] (component-major)
-  uint32_t* nf;               // facets between seeds
-  uint32_t* nclip;            // neighbours visited
-  uint32_t* f_nbr;            // [kMaxFacets][n] original index
-  double* f_area;             // [kMaxFacets][n]
-  uint32_t out_stride;        // n
-  // per-call counters: [0] exact predicate calls, [1] max clips
-  unsigned long long* counters;
+  int32_t* status;            // by sorted slot
+  uint32_t* nclip;            // by sorted slot: neighbours visited
+  CombBuf comb;
+  unsigned long long* counters;  // [0] exact predicate calls, [1] max clips
 };
 
 enum ClipShape : int { CLIP_SMALL = 0, CLIP_LARGE = 1 };
 
-// Error of the last clipping launch (launch configuration errors are not
-// sticky, so the orchestration checks this after every launch).
+// Error of the last launch of this module (launch configuration errors are
+// not sticky, so the orchestration checks this after every launch).
 extern cudaError_t last_launch_error;
 
 // FP64 clipping (exact conflict signs).
 void launch_clip_fp64(const ClipArgs& a, int shape, cudaStream_t st);
-// FP32 clipping with certified signs and FP64 geometry; cells that FP32
-// cannot certify get status GBV_CELL_RECHECK.
+// FP32 clipping with certified signs; cells that FP32 cannot certify get
+// status GBV_CELL_RECHECK.
 void launch_clip_fp32(const ClipArgs& a, cudaStream_t st);
+
+struct GeomArgs {
+  SortedSeeds S;
+  const uint32_t* nbr;        // the lists the cells were clipped with
+  uint32_t nbr_stride;
+  const uint32_t* qlist;      // sorted slots (nullptr: all)
+  const uint32_t* qrow;
+  uint32_t nq;
+  double box[6];
+  int verify_sr;              // FP32 clipping: check its stops in FP64
+  CombBuf comb;
+  int32_t* status;
+  const uint32_t* nclip;
+  // outputs by sorted slot
+  double* vol;
+  double* mg;                 // [3][n]
+  uint32_t* nf;
+  uint32_t* f_nbr;            // [kMaxFacets][n] original index
+  double* f_area;             // [kMaxFacets][n]
+  uint32_t out_stride;
+};
+
+// FP64 geometry of the final cells, one warp per cell, with the reference's
+// formulas and summation order.
+void launch_geometry(const GeomArgs& a, cudaStream_t st);
 
 }  // namespace gbv

@@ -204,7 +204,14 @@ __global__ void scatter_kernel(const double* __restrict__ xyz, uint32_t stride,
   double len2 = __dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z));
   S.xd[s] = make_double4(x, y, z, h);
   S.q[s] = __dsub_rn(wi, len2);
-  S.xf[s] = make_float4((float)x, (float)y, (float)z, (float)h);
+  const float4 hi = make_float4((float)x, (float)y, (float)z, (float)h);
+  S.xf[s] = hi;
+  S.xl[s] = make_float4((float)(x - (double)hi.x), (float)(y - (double)hi.y),
+                        (float)(z - (double)hi.z), (float)(h - (double)hi.w));
+  if (S.wf) {
+    const float whi = (float)wi;
+    S.wf[s] = make_float2(whi, (float)(wi - (double)whi));
+  }
   if (S.ws) S.ws[s] = wi;
   S.perm[s] = i;
   S.slot_of[i] = s;
@@ -239,14 +246,8 @@ void build_grid(const double* xyz, uint32_t stride, uint32_t dim, const double* 
 // ---------------------------------------------------------------------
 constexpr int kKnnThreads = 64;
 constexpr uint32_t kLeaf = 24;
-
-struct KnnList {
-  double* d2;
-  uint32_t* slot;
-  uint32_t stride;
-  __device__ double& d(uint32_t r) { return d2[(size_t)r * stride]; }
-  __device__ uint32_t& s(uint32_t r) { return slot[(size_t)r * stride]; }
-};
+constexpr int kKnnExtra = 8;                 // FP32 list slack beyond k
+constexpr int kKnnCap = kKnnSmemK + kKnnExtra;
 
 // Squared distance from point u (fine-cell units) to the box of an octree
 // node [i*side, (i+1)*side)^3, in fine-cell units, shrunk by a small slack
@@ -263,47 +264,12 @@ __device__ __forceinline__ float node_box_d2(float ux, float uy, float uz, uint3
   return dx * dx + dy * dy + dz * dz;
 }
 
-template <bool SMEM>
-__global__ void __launch_bounds__(kKnnThreads)
-knn_kernel(KnnArgs a, SortedSeeds S, const GridDesc* __restrict__ gdp,
-           const double* __restrict__ aux) {
-  __shared__ double s_d2[SMEM ? kKnnSmemK : 1][kKnnThreads];
-  __shared__ uint32_t s_slot[SMEM ? kKnnSmemK : 1][kKnnThreads];
-  const uint32_t qi = blockIdx.x * kKnnThreads + threadIdx.x;
-  if (qi >= a.nq) return;
-  const GridDesc g = *gdp;
-  KnnList lst;
-  if (SMEM) {
-    lst.d2 = &s_d2[0][threadIdx.x];
-    lst.slot = &s_slot[0][threadIdx.x];
-    lst.stride = kKnnThreads;
-  } else {
-    lst.d2 = a.gl_d2 + qi;
-    lst.slot = a.gl_slot + qi;
-    lst.stride = a.nq;
-  }
-  uint32_t qslot = kNone;
-  double4 q;
-  if (a.mode == KNN_QUERY) {
-    q = a.qpts[qi];
-  } else {
-    qslot = a.qlist ? a.qlist[qi] : qi;
-    q = S.xd[qslot];
-  }
-  const float4 qf = make_float4((float)q.x, (float)q.y, (float)q.z, (float)q.w);
-  const uint32_t qperm = (qslot != kNone) ? S.perm[qslot] : 0u;
-  const float ux = (float)((q.x - g.lo[0]) * g.inv_h);
-  const float uy = (float)((q.y - g.lo[1]) * g.inv_h);
-  const float uz = (float)((q.z - g.lo[2]) * g.inv_h);
+// Depth-first traversal, nearest child first.  thr() is the current
+// squared pruning distance (FP32); leaf(b, e) scans sorted slots [b, e).
+template <class Thr, class Leaf>
+__device__ __forceinline__ void traverse(const SortedSeeds& S, const GridDesc& g, float ux,
+                                         float uy, float uz, Thr thr, Leaf leaf) {
   const float h2f = g.h_f * g.h_f;
-  // bound on |FP32 distance - FP64 distance| from coordinate rounding
-  const float delta = 8.0f * (float)aux[1] * 5.9604645e-8f + 1e-30f;
-  const uint32_t K = a.k;
-  uint32_t cnt = 0;
-  double worst = DBL_MAX;
-  float thr = FLT_MAX;
-  bool dup_lower = false;
-
   uint32_t stack[8 * 10 + 8];
   int sp = 0;
   stack[sp++] = 0u;  // (code << 4) | level
@@ -313,64 +279,20 @@ knn_kernel(KnnArgs a, SortedSeeds S, const GridDesc* __restrict__ gdp,
     const uint32_t code = e >> 4;
     const int shift = g.L - lev;
     const float side = (float)(1u << shift);
-    if (cnt == K) {
-      float bd = node_box_d2(ux, uy, uz, compact3(code), compact3(code >> 1),
-                             compact3(code >> 2), side) * h2f;
-      if (bd > thr) continue;
+    const float t0 = thr();
+    if (t0 < FLT_MAX) {
+      const float bd = node_box_d2(ux, uy, uz, compact3(code), compact3(code >> 1),
+                                   compact3(code >> 2), side) * h2f;
+      if (bd > t0) continue;
     }
     const uint32_t c_lo = code << (3 * shift);
     const uint32_t c_hi = (code + 1u) << (3 * shift);
     const uint32_t b = S.cell_start[c_lo], en = S.cell_start[c_hi];
     if (b == en) continue;
     if (en - b <= kLeaf || lev == g.L) {
-      for (uint32_t s2 = b; s2 < en; ++s2) {
-        const float4 p = S.xf[s2];
-        float dx = p.x - qf.x, dy = p.y - qf.y, dz = p.z - qf.z, dh = p.w - qf.w;
-        float d32 = dx * dx + dy * dy + dz * dz + dh * dh;
-        if (d32 > thr) continue;
-        if (a.mode == KNN_CELLS && s2 == qslot) continue;
-        const double d = dist2_exact(q, S.xd[s2]);
-        if (a.mode == KNN_CELLS && d == 0.0) {
-          if (S.perm[s2] < qperm) dup_lower = true;
-          continue;
-        }
-        uint32_t pj = 0;
-        bool pj_loaded = false;
-        if (cnt == K) {
-          if (d > worst) continue;
-          if (d == worst) {
-            pj = S.perm[s2];
-            pj_loaded = true;
-            if (pj > S.perm[lst.s(K - 1)]) continue;
-          }
-        }
-        uint32_t pos = (cnt < K) ? cnt : K - 1;
-        while (pos > 0) {
-          const double dp = lst.d(pos - 1);
-          if (dp < d) break;
-          if (dp == d) {
-            if (!pj_loaded) {
-              pj = S.perm[s2];
-              pj_loaded = true;
-            }
-            if (S.perm[lst.s(pos - 1)] < pj) break;
-          }
-          lst.d(pos) = dp;
-          lst.s(pos) = lst.s(pos - 1);
-          --pos;
-        }
-        lst.d(pos) = d;
-        lst.s(pos) = s2;
-        if (cnt < K) ++cnt;
-        if (cnt == K) {
-          worst = lst.d(K - 1);
-          float r = sqrtf(__double2float_ru(worst)) * 1.0000076f + delta;
-          thr = r * r * 1.0000076f;
-        }
-      }
+      leaf(b, en);
       continue;
     }
-    // expand: children sorted by box distance, nearest pushed last
     const float cside = side * 0.5f;
     float cd[8];
     uint32_t cc[8];
@@ -381,46 +303,286 @@ knn_kernel(KnnArgs a, SortedSeeds S, const GridDesc* __restrict__ gdp,
                           cside) * h2f;
       cc[c] = ch;
     }
-    // insertion sort descending by distance
 #pragma unroll
     for (int i = 1; i < 8; ++i) {
 #pragma unroll
       for (int j = i; j > 0; --j) {
         if (cd[j] > cd[j - 1]) {
-          float td = cd[j];
+          const float td = cd[j];
           cd[j] = cd[j - 1];
           cd[j - 1] = td;
-          uint32_t tc = cc[j];
+          const uint32_t tc = cc[j];
           cc[j] = cc[j - 1];
           cc[j - 1] = tc;
         }
       }
     }
+    const float t1 = thr();
 #pragma unroll
-    for (int c = 0; c < 8; ++c) {
-      if (cnt < K || cd[c] <= thr) stack[sp++] = (cc[c] << 4) | (uint32_t)(lev + 1);
-    }
+    for (int c = 0; c < 8; ++c)
+      if (cd[c] <= t1) stack[sp++] = (cc[c] << 4) | (uint32_t)(lev + 1);
   }
-  if (a.mode == KNN_CELLS && dup_lower) cnt = 0;
+}
+
+struct QueryCtx {
+  uint32_t qslot;  // kNone for external queries
+  uint32_t qperm;
+  double4 q;
+  float4 qf;
+  float ux, uy, uz;
+  bool has_lo;
+  double lo_d;
+  uint32_t lo_i;
+};
+
+__device__ __forceinline__ QueryCtx make_query(const KnnArgs& a, const SortedSeeds& S,
+                                               const GridDesc& g, uint32_t qi) {
+  QueryCtx c;
+  c.qslot = kNone;
+  if (a.mode == KNN_QUERY) {
+    c.q = a.qpts[qi];
+  } else {
+    c.qslot = a.qlist ? a.qlist[qi] : qi;
+    c.q = S.xd[c.qslot];
+  }
+  c.qperm = (c.qslot != kNone) ? S.perm[c.qslot] : 0u;
+  c.qf = make_float4((float)c.q.x, (float)c.q.y, (float)c.q.z, (float)c.q.w);
+  c.ux = (float)((c.q.x - g.lo[0]) * g.inv_h);
+  c.uy = (float)((c.q.y - g.lo[1]) * g.inv_h);
+  c.uz = (float)((c.q.z - g.lo[2]) * g.inv_h);
+  c.has_lo = a.lo_d2 != nullptr;
+  c.lo_d = c.has_lo ? a.lo_d2[qi] : 0.0;
+  c.lo_i = c.has_lo ? a.lo_idx[qi] : 0u;
+  return c;
+}
+
+// (d, i) after the query's lower bound in (d2, original index) order?
+__device__ __forceinline__ bool after_lo(const QueryCtx& c, double d, uint32_t i) {
+  return !c.has_lo || d > c.lo_d || (d == c.lo_d && i > c.lo_i);
+}
+
+__device__ __forceinline__ void write_outputs(const KnnArgs& a, const SortedSeeds& S,
+                                              const QueryCtx& c, uint32_t qi, uint32_t cnt,
+                                              bool dup_lower, const double* ld, const uint32_t* ls,
+                                              uint32_t stride) {
   if (a.cnt) a.cnt[qi] = (a.mode == KNN_CELLS && dup_lower) ? 0x80000000u : cnt;
+  if (a.mode == KNN_CELLS && dup_lower) cnt = 0;
   if (a.nbr)
-    for (uint32_t r = 0; r < cnt; ++r) a.nbr[(size_t)r * a.out_stride + qi] = lst.s(r);
+    for (uint32_t r = 0; r < cnt; ++r) a.nbr[(size_t)r * a.out_stride + qi] = ls[(size_t)r * stride];
+  if (a.last_d2) {
+    a.last_d2[qi] = cnt ? ld[(size_t)(cnt - 1) * stride] : (c.has_lo ? c.lo_d : 0.0);
+    a.last_idx[qi] = cnt ? S.perm[ls[(size_t)(cnt - 1) * stride]] : (c.has_lo ? c.lo_i : 0u);
+  }
   if (a.exp_idx) {
-    const size_t row = (a.mode == KNN_QUERY) ? qi : qperm;
+    const size_t row = (a.mode == KNN_QUERY) ? qi : c.qperm;
+    const uint32_t K = a.k;
     for (uint32_t r = 0; r < K; ++r) {
-      a.exp_idx[row * K + r] = (r < cnt) ? S.perm[lst.s(r)] : kNone;
-      if (a.exp_d2) a.exp_d2[row * K + r] = (r < cnt) ? lst.d(r) : INFINITY;
+      a.exp_idx[row * K + r] = (r < cnt) ? S.perm[ls[(size_t)r * stride]] : kNone;
+      if (a.exp_d2) a.exp_d2[row * K + r] = (r < cnt) ? ld[(size_t)r * stride] : INFINITY;
     }
   }
+}
+
+// ---- exact search: FP64 distances of every candidate, FP64 list ---------
+// qsel: when non-null, the kernel runs only the queries qsel[0..*qcount).
+template <bool SMEM>
+__global__ void __launch_bounds__(kKnnThreads)
+knn_exact_kernel(KnnArgs a, SortedSeeds S, const GridDesc* __restrict__ gdp,
+                 const double* __restrict__ aux, const uint32_t* __restrict__ qsel,
+                 const uint32_t* __restrict__ qcount) {
+  __shared__ double s_d2[SMEM ? kKnnSmemK : 1][kKnnThreads];
+  __shared__ uint32_t s_slot[SMEM ? kKnnSmemK : 1][kKnnThreads];
+  uint32_t qi = blockIdx.x * kKnnThreads + threadIdx.x;
+  if (qsel) {
+    if (qi >= *qcount) return;
+    qi = qsel[qi];
+  } else if (qi >= a.nq) {
+    return;
+  }
+  const GridDesc g = *gdp;
+  double* ld;
+  uint32_t* ls;
+  uint32_t stride;
+  if (SMEM) {
+    ld = &s_d2[0][threadIdx.x];
+    ls = &s_slot[0][threadIdx.x];
+    stride = kKnnThreads;
+  } else {
+    ld = a.gl_d2 + qi;
+    ls = a.gl_slot + qi;
+    stride = a.nq;
+  }
+  const QueryCtx c = make_query(a, S, g, qi);
+  const float delta = 8.0f * (float)aux[1] * 5.9604645e-8f + 1e-30f;
+  const uint32_t K = a.k;
+  uint32_t cnt = 0;
+  double worst = DBL_MAX;
+  float thr = FLT_MAX;
+  bool dup_lower = false;
+  auto L = [&](uint32_t r) -> double& { return ld[(size_t)r * stride]; };
+  auto LS = [&](uint32_t r) -> uint32_t& { return ls[(size_t)r * stride]; };
+  traverse(S, g, c.ux, c.uy, c.uz, [&]() { return thr; }, [&](uint32_t b, uint32_t en) {
+    for (uint32_t s2 = b; s2 < en; ++s2) {
+      const float4 p = S.xf[s2];
+      const float dx = p.x - c.qf.x, dy = p.y - c.qf.y, dz = p.z - c.qf.z, dh = p.w - c.qf.w;
+      const float d32 = dx * dx + dy * dy + dz * dz + dh * dh;
+      if (d32 > thr) continue;
+      if (a.mode == KNN_CELLS && s2 == c.qslot) continue;
+      const double d = dist2_exact(c.q, S.xd[s2]);
+      const uint32_t pj = S.perm[s2];
+      if (a.mode == KNN_CELLS && d == 0.0) {
+        if (pj < c.qperm) dup_lower = true;
+        continue;
+      }
+      if (!after_lo(c, d, pj)) continue;
+      if (cnt == K) {
+        if (d > worst) continue;
+        if (d == worst && pj > S.perm[LS(K - 1)]) continue;
+      }
+      uint32_t pos = (cnt < K) ? cnt : K - 1;
+      while (pos > 0) {
+        const double dp = L(pos - 1);
+        if (dp < d) break;
+        if (dp == d && S.perm[LS(pos - 1)] < pj) break;
+        L(pos) = dp;
+        LS(pos) = LS(pos - 1);
+        --pos;
+      }
+      L(pos) = d;
+      LS(pos) = s2;
+      if (cnt < K) ++cnt;
+      if (cnt == K) {
+        worst = L(K - 1);
+        const float r = sqrtf(__double2float_ru(worst)) * 1.0000076f + delta;
+        thr = r * r * 1.0000076f;
+      }
+    }
+  });
+  write_outputs(a, S, c, qi, cnt, dup_lower, ld, ls, stride);
+}
+
+// ---- fast search: FP32 list of k + kKnnExtra, exact FP64 re-rank ---------
+// Every seed of the true k nearest (in exact (d2, index) order) lies within
+// FP32 distance sqrt(d32_k) + 2 delta of the query, where d32_k is the k-th
+// FP32 distance found and delta bounds |FP32 - FP64| distance.  The list
+// keeps every candidate under that threshold up to k + kKnnExtra entries;
+// if a candidate under the final threshold had to be dropped, the query is
+// flagged and redone by the exact search.
+__global__ void __launch_bounds__(kKnnThreads)
+knn_fast_kernel(KnnArgs a, SortedSeeds S, const GridDesc* __restrict__ gdp,
+                const double* __restrict__ aux) {
+  extern __shared__ __align__(16) unsigned char knn_smem[];
+  double(*s_d)[kKnnThreads] = reinterpret_cast<double(*)[kKnnThreads]>(knn_smem);
+  uint32_t(*s_s)[kKnnThreads] =
+      reinterpret_cast<uint32_t(*)[kKnnThreads]>(knn_smem + sizeof(double) * kKnnCap * kKnnThreads);
+  const uint32_t qi = blockIdx.x * kKnnThreads + threadIdx.x;
+  if (qi >= a.nq) return;
+  const int tid = threadIdx.x;
+  const GridDesc g = *gdp;
+  const QueryCtx c = make_query(a, S, g, qi);
+  const float delta = 8.0f * (float)aux[1] * 5.9604645e-8f + 1e-30f;
+  const uint32_t K = a.k;
+  const uint32_t cap = K + kKnnExtra;
+  // the FP32 distance lives in the low word of the list's double slot
+  auto D32 = [&](uint32_t r) -> float& { return *reinterpret_cast<float*>(&s_d[r][tid]); };
+  uint32_t cnt = 0;
+  float thr = FLT_MAX;
+  float dropped = FLT_MAX;
+  bool dup_lower = false;
+  // lower bound: candidates surely before it are skipped, those near it are
+  // compared exactly
+  float lo_skip = -1.f, lo_check = -1.f;
+  if (c.has_lo) {
+    const float r = sqrtf(__double2float_rd(c.lo_d));
+    const float r1 = fmaxf(r * 0.9999924f - delta, 0.f);
+    const float r2 = r * 1.0000076f + delta;
+    lo_skip = r1 * r1 * 0.9999924f;
+    lo_check = r2 * r2 * 1.0000076f;
+  }
+  traverse(S, g, c.ux, c.uy, c.uz, [&]() { return thr; }, [&](uint32_t b, uint32_t en) {
+    for (uint32_t s2 = b; s2 < en; ++s2) {
+      const float4 p = S.xf[s2];
+      const float dx = p.x - c.qf.x, dy = p.y - c.qf.y, dz = p.z - c.qf.z, dh = p.w - c.qf.w;
+      const float d32 = dx * dx + dy * dy + dz * dz + dh * dh;
+      if (d32 > thr) continue;
+      if (a.mode == KNN_CELLS && s2 == c.qslot) continue;
+      if (c.has_lo) {
+        if (d32 < lo_skip) continue;
+        if (d32 <= lo_check && !after_lo(c, dist2_exact(c.q, S.xd[s2]), S.perm[s2])) continue;
+      }
+      if (a.mode == KNN_CELLS && d32 <= 0.f) {
+        if (dist2_exact(c.q, S.xd[s2]) == 0.0) {
+          if (S.perm[s2] < c.qperm) dup_lower = true;
+          continue;
+        }
+      }
+      if (cnt == cap) {
+        if (d32 >= D32(cap - 1)) {
+          dropped = fminf(dropped, d32);
+          continue;
+        }
+        dropped = fminf(dropped, D32(cap - 1));
+      }
+      uint32_t pos = (cnt < cap) ? cnt : cap - 1;
+      while (pos > 0 && D32(pos - 1) > d32) {
+        D32(pos) = D32(pos - 1);
+        s_s[pos][tid] = s_s[pos - 1][tid];
+        --pos;
+      }
+      D32(pos) = d32;
+      s_s[pos][tid] = s2;
+      if (cnt < cap) ++cnt;
+      if (cnt >= K) {
+        const float r = sqrtf(D32(K - 1)) * 1.0000076f + 2.f * delta;
+        thr = r * r * 1.0000076f;
+      }
+    }
+  });
+  if (dropped <= thr) {
+    // a candidate that may belong to the k nearest was dropped
+    const uint32_t k = atomicAdd(a.flag_count, 1u);
+    a.flag_list[k] = qi;
+    if (a.cnt) a.cnt[qi] = 0;
+    return;
+  }
+  // exact distances, then insertion sort by (d2, original index)
+  for (uint32_t r = 0; r < cnt; ++r) s_d[r][tid] = dist2_exact(c.q, S.xd[s_s[r][tid]]);
+  for (uint32_t r = 1; r < cnt; ++r) {
+    const double d = s_d[r][tid];
+    const uint32_t sl = s_s[r][tid];
+    const uint32_t pj = S.perm[sl];
+    uint32_t pos = r;
+    while (pos > 0) {
+      const double dp = s_d[pos - 1][tid];
+      if (dp < d || (dp == d && S.perm[s_s[pos - 1][tid]] < pj)) break;
+      s_d[pos][tid] = dp;
+      s_s[pos][tid] = s_s[pos - 1][tid];
+      --pos;
+    }
+    s_d[pos][tid] = d;
+    s_s[pos][tid] = sl;
+  }
+  write_outputs(a, S, c, qi, cnt < K ? cnt : K, dup_lower, &s_d[0][tid], &s_s[0][tid],
+                kKnnThreads);
 }
 
 void launch_knn(const KnnArgs& a, cudaStream_t st) {
   if (a.nq == 0) return;
   const unsigned nb = (a.nq + kKnnThreads - 1) / kKnnThreads;
-  if (a.k <= kKnnSmemK)
-    knn_kernel<true><<<nb, kKnnThreads, 0, st>>>(a, *a.S, a.S->gd, a.S->aux);
-  else
-    knn_kernel<false><<<nb, kKnnThreads, 0, st>>>(a, *a.S, a.S->gd, a.S->aux);
+  if (a.k <= kKnnSmemK && a.flag_count) {
+    const size_t sh = (sizeof(double) + sizeof(uint32_t)) * kKnnCap * kKnnThreads;
+    cudaFuncSetAttribute(knn_fast_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh);
+    cudaMemsetAsync(a.flag_count, 0, sizeof(uint32_t), st);
+    knn_fast_kernel<<<nb, kKnnThreads, sh, st>>>(a, *a.S, a.S->gd, a.S->aux);
+    knn_exact_kernel<true><<<nb, kKnnThreads, 0, st>>>(a, *a.S, a.S->gd, a.S->aux, a.flag_list,
+                                                       a.flag_count);
+  } else if (a.k <= kKnnSmemK) {
+    knn_exact_kernel<true><<<nb, kKnnThreads, 0, st>>>(a, *a.S, a.S->gd, a.S->aux, nullptr,
+                                                       nullptr);
+  } else {
+    knn_exact_kernel<false><<<nb, kKnnThreads, 0, st>>>(a, *a.S, a.S->gd, a.S->aux, nullptr,
+                                                        nullptr);
+  }
 }
 
 }  // namespace gbv

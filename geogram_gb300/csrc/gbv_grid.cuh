@@ -10,6 +10,8 @@ struct SortedSeeds {
   double4* xd = nullptr;  // (x, y, z, h): h = sqrt(W - w), 0 for Voronoi
   double* q = nullptr;    // w - |p|^2 with the reference's arithmetic
   float4* xf = nullptr;   // (x, y, z, h) rounded to FP32
+  float4* xl = nullptr;   // FP32 remainders: x = xf + xl to about 2^-48 |x|
+  float2* wf = nullptr;   // weight as FP32 (value, remainder); nullptr: Voronoi
   double* ws = nullptr;   // weights by slot (nullptr for Voronoi)
   uint32_t* perm = nullptr;   // slot -> original index
   uint32_t* slot_of = nullptr;  // original index -> slot
@@ -57,21 +59,33 @@ struct KnnArgs {
   const double4* qpts;  // KNN_QUERY: query points (x,y,z,h)
   uint32_t k;
   int mode;
+  // optional lower bound per query: only neighbours after (lo_d2, lo_idx)
+  // in (d2, original index) order are returned (the next batch of a list)
+  const double* lo_d2;
+  const uint32_t* lo_idx;
   // outputs, [k][out_stride] slot-major (sorted slots of neighbours)
   uint32_t* nbr;        // may be null if only idx/d2 wanted
   uint32_t out_stride;
-  uint32_t* cnt;        // [nq] list lengths
+  uint32_t* cnt;        // [nq] list lengths (bit 31: lower-index duplicate)
+  // optional: (d2, original index) of each query's last returned neighbour
+  double* last_d2;
+  uint32_t* last_idx;
   // optional exported results in caller order: idx (original indices) and
   // d2, row-major [row][k]; row = perm[slot] (ALL) or query index (QUERY)
   uint32_t* exp_idx;
   double* exp_d2;
-  // global scratch for lists longer than the shared-memory capacity
+  // scratch: global lists for k > kKnnSmemK ([k][nq] each), and the queries
+  // the FP32 screening could not settle (count + list, nq entries)
   double* gl_d2;
   uint32_t* gl_slot;
+  uint32_t* flag_count;
+  uint32_t* flag_list;
 };
 
-// Launches the kNN search.  k <= kKnnSmemK uses shared-memory lists,
-// larger k uses gl_d2 / gl_slot ([k][nq]).
+// Launches the kNN search.  For k <= kKnnSmemK: FP32 screening with an
+// exact FP64 re-rank, then the exact search for the queries it could not
+// settle (needs flag_count / flag_list).  Larger k: the exact search with
+// global lists gl_d2 / gl_slot.
 constexpr uint32_t kKnnSmemK = 64;
 void launch_knn(const KnnArgs& a, cudaStream_t st);
 
