@@ -1,0 +1,308 @@
+#!/usr/bin/env python
+"""Headline benchmark: certified Laguerre cells per second on one GB300.
+
+Workload (one step = one pass of the cell engine plus the Lloyd update):
+power diagram of 1,000,000 seeds uniform in the unit cube, weights uniform
+in [0, 1e-4], clipped to the unit box with the security-radius loop, FP32
+clipping with FP64 re-clip of every cell FP32 cannot certify, FP64
+geometry; the seeds then move to their centroids (CVT Lloyd step,
+voronoi/CVT.cpp:133-167).  Steps are consecutive Lloyd iterations.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line.  `value` is cells/s with the seeds resident on the
+GPU (CUDA events on the library's stream, L2 flushed between steps);
+`e2e` is the same through the C ABI with host arrays (host->device and
+device->host copies inside the timed region); `cpu_baseline` times the
+CPU restatement of the reference (oracle/) on a bounded sample on this
+machine's cores.  --impl reference times that CPU implementation alone on
+the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_SEEDS = 1_000_000
+W_MAX = 1e-4
+METRIC = "Laguerre cells/s (power diagram, 1M seeds, FP32 clip + FP64 re-clip, one Lloyd step)"
+WORKLOAD = ("power diagram of 1M seeds uniform in [0,1]^3, weights U[0,1e-4], seed 0; "
+            "certified cells clipped to the unit box, FP32 clipping + FP64 re-clip, "
+            "one Lloyd iteration per step")
+
+
+def make_inputs(n: int, seed: int = 0):
+    rng = np.random.default_rng(seed)
+    x = rng.random((n, 3))
+    w = rng.random(n) * W_MAX
+    return x, w
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.samples = []
+        self._stop = threading.Event()
+        self._th = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(
+                    ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                     "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                if out.returncode == 0 and out.stdout.strip():
+                    self.samples.append([v.strip() for v in out.stdout.strip().split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._th = threading.Thread(target=self._run, daemon=True)
+        self._th.start()
+        return self
+
+    def __exit__(self, *exc):
+        self._stop.set()
+        if self._th:
+            self._th.join(timeout=10)
+
+    def summary(self) -> dict:
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no nvidia-smi samples"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4)
+                          if len(s) > 5 + k and s[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+def load_peaks() -> tuple[float, str]:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def cpu_baseline(x: np.ndarray, w: np.ndarray, sample: int) -> dict:
+    """The oracle (CPU restatement of the reference path) on cells [0, sample)
+    of the same seeds, with every host core."""
+    from oracle import oracle
+    cores = os.cpu_count() or 1
+    dt = oracle.cells_range_time(x, w, 0, sample, cores)
+    return {"value": sample / dt, "unit": "cells/s", "cores": cores, "kind": "port",
+            "sample": f"cells 0..{sample} of the {len(x)}-seed power diagram (all seeds as "
+                      f"neighbours), oracle/gbv_oracle.c with {cores} threads, {dt:.2f} s"}
+
+
+def max_over_ranks(x: float) -> float:
+    """Maximum of x over the ranks of the process group (x if no group)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    dev = (torch.device("cuda", torch.cuda.current_device()) if dist.get_backend() == "nccl"
+           else torch.device("cpu"))
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_reference(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    x, w = make_inputs(N_SEEDS)
+    from oracle import oracle
+    cores = os.cpu_count() or 1
+    m = args.ref_sample
+    for s in range(args.warmup):
+        oracle.cells_range_time(x, w, 0, m, cores)
+    times = []
+    for s in range(args.steps):
+        i0 = (s * m) % (N_SEEDS - m)
+        times.append(oracle.cells_range_time(x, w, i0, i0 + m, cores))
+    total = sum(times)
+    value = m * args.steps / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "cells/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded numpy)",
+        "config": {"workload": WORKLOAD, "n_seeds": N_SEEDS, "sample_cells_per_step": m},
+        "cpu_baseline": {"value": value, "unit": "cells/s", "cores": cores, "kind": "port",
+                         "sample": f"{m} cells per step of the {N_SEEDS}-seed power diagram, "
+                                   f"oracle/gbv_oracle.c with {cores} threads"},
+        "e2e": {"value": value, "unit": "cells/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args) -> None:
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    import geogram_gb300 as g
+    from geogram_gb300 import _lib
+    ctx = g.Context(local)
+    lib = _lib.load()
+    x_h, w_h = make_inputs(N_SEEDS, seed=rank)
+    x = torch.from_numpy(x_h).to(dev)
+    w = torch.from_numpy(w_h).to(dev)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def step():
+        return g.lloyd_iterations(x, 1, w, precision=args.precision, stream=stream, ctx=ctx)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    launches0 = lib.gbv_kernel_launches()
+    reports = []
+    ev_s = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ev_e = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    with ClockSampler(local) as clk:
+        for s in range(args.steps):
+            flush.fill_(float(s))  # L2 flush (256 MB > 126 MB L2), outside the events
+            ev_s[s].record(stream)
+            reports.append(step())
+            ev_e[s].record(stream)
+        torch.cuda.synchronize()
+    launches = lib.gbv_kernel_launches() - launches0
+    if world > 1:
+        dist.barrier()
+    step_ms = [a.elapsed_time(b) for a, b in zip(ev_s, ev_e)]
+    total_ms = max_over_ranks(sum(step_ms))
+    value = world * N_SEEDS * args.steps / (total_ms / 1e3)
+
+    # ---- e2e through the C ABI with host arrays (H2D + compute + D2H)
+    xe = x_h.copy()
+    e2e_t = []
+    for s in range(max(2, args.steps // 2)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        xe, _ = g.lloyd_step(xe, w_h, precision=args.precision, ctx=ctx)
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_value = world * N_SEEDS / statistics.mean(e2e_t[1:] if len(e2e_t) > 1 else e2e_t)
+
+    if rank == 0:
+        # ---- the dominant kernel's roofline (kNN, HBM): algorithmic bytes per
+        # seed = query float4 (16) + k list entries (4 k) + count, last
+        # (d2, index) (16), timed by the library's CUDA events on its stream
+        rep = reports[-1]
+        k = rep["knn_k"]
+        bytes_per_seed = 16 + 4 * k + 16
+        knn_ms = statistics.median(r["ms_knn"] for r in reports)
+        achieved = bytes_per_seed * N_SEEDS / (knn_ms / 1e3) / 1e9
+        peak, peak_kind = load_peaks()
+        # ---- plain FP64 path on the same seeds, and the error of this mode
+        # against it (both modes reproduce the reference's FP64 results)
+        xs = x.clone()
+        torch.cuda.synchronize()
+        rep32 = g.compute_cells_device(xs, w, precision=args.precision, stream=stream, ctx=ctx)
+        c32 = g.device_results(ctx)
+        rep64 = g.compute_cells_device(xs, w, precision="fp64", stream=stream, ctx=ctx)
+        c64 = g.device_results(ctx)
+        t64 = []
+        for _ in range(2):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            g.compute_cells_device(xs, w, precision="fp64", stream=stream, ctx=ctx)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            t64.append(e0.elapsed_time(e1))
+        fp64_cps = N_SEEDS / (min(t64) / 1e3)
+        rel_vol = float(np.max(np.abs(c32["volume"] - c64["volume"]) /
+                               np.maximum(np.abs(c64["volume"]), 1e-300)))
+        abs_mg = float(np.max(np.abs(c32["mg"] - c64["mg"])))
+        same_nbr = bool(np.array_equal(c32["rowptr"], c64["rowptr"]) and
+                        np.array_equal(c32["neighbors"], c64["neighbors"]))
+        cpu = cpu_baseline(x_h, w_h, args.cpu_sample)
+        line = {
+            "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64",
+            "data": "synthetic (seeded numpy, uniform seeds and weights)",
+            "config": {"workload": WORKLOAD, "n_seeds": N_SEEDS, "precision": args.precision,
+                       "l2": "flushed between steps (256 MB write)",
+                       "parallelism": "replicas only" if world > 1 else "1 GPU"},
+            "roofline": {"kernel": "knn_fast_kernel (first kNN pass)", "bound": "hbm",
+                         "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind,
+                         "bytes_per_seed": bytes_per_seed, "traffic": None},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "cells/s",
+                    "h2d_bytes_per_step": 32 * N_SEEDS, "d2h_bytes_per_step": 24 * N_SEEDS},
+            "gpu_launches": int(launches),
+            "clocks": clk.summary(),
+            "phases_ms": {kk: round(statistics.median(r[kk] for r in reports), 3)
+                          for kk in ("ms_grid", "ms_knn", "ms_clip", "ms_retry", "ms_total")},
+            "cells": {kk: reports[-1][kk] for kk in ("n_recheck_fp64", "n_more_k", "n_overflow",
+                                                     "mean_clips", "max_clips", "nnz")},
+            "fp64_plain": {"cells_per_s": fp64_cps, "speedup_of_this_mode": value / fp64_cps,
+                           "max_rel_vol_err_vs_fp64": rel_vol, "max_abs_mg_err_vs_fp64": abs_mg,
+                           "neighbour_lists_identical": same_nbr},
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--precision", default="fp32")
+    ap.add_argument("--cpu-sample", type=int, default=100_000)
+    ap.add_argument("--ref-sample", type=int, default=50_000)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -30,7 +30,7 @@ from ._lib import (CELL_ALL_NEIGHBOURS, CELL_CERTIFIED, CELL_DUPLICATE, PRECISIO
 
 __all__ = [
     "Context", "NearestNeighborSearch", "Cells", "compute_cells", "lloyd_step",
-    "lloyd_iterations", "GbvError", "CELL_CERTIFIED", "CELL_ALL_NEIGHBOURS", "CELL_DUPLICATE",
+    "lloyd_iterations", "compute_cells_device", "device_results", "GbvError", "CELL_CERTIFIED", "CELL_ALL_NEIGHBOURS", "CELL_DUPLICATE",
     "PRECISION_FP64", "PRECISION_FP32_RECHECK", "cell_options",
 ]
 
@@ -200,7 +200,23 @@ def compute_cells_device(xyz, weights=None, *, box=((0.0, 0.0, 0.0), (1.0, 1.0, 
     st = ctypes.c_void_p(stream.cuda_stream) if stream is not None else None
     _lib.check(ctx._lib.gbv_cells_compute_device(ctx.handle, _lib.ptr(xyz), _lib.ptr(weights), n,
                                                  ctypes.byref(o), st, ctypes.byref(rep)))
+    ctx.last_n, ctx.last_nnz = n, rep.nnz
     return rep.as_dict()
+
+
+def device_results(ctx: Context | None = None) -> dict:
+    """Copies the results of the last compute on `ctx` to host arrays."""
+    ctx = ctx or default_context()
+    n, nnz = ctx.last_n, ctx.last_nnz
+    out = dict(volume=np.empty(n), mg=np.empty((n, 3)), rowptr=np.empty(n + 1, np.uint32),
+               neighbors=np.empty(max(nnz, 1), np.uint32), facet_area=np.empty(max(nnz, 1)),
+               status=np.empty(n, np.int32))
+    _lib.check(ctx._lib.gbv_cells_fetch(ctx.handle, _lib.ptr(out["volume"]), _lib.ptr(out["mg"]),
+                                        _lib.ptr(out["rowptr"]), _lib.ptr(out["neighbors"]),
+                                        _lib.ptr(out["facet_area"]), _lib.ptr(out["status"])))
+    out["neighbors"] = out["neighbors"][:nnz]
+    out["facet_area"] = out["facet_area"][:nnz]
+    return out
 
 
 def lloyd_step(xyz: np.ndarray, weights: np.ndarray | None = None, *,

@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -96,6 +97,9 @@ struct gbv_context {
 };
 
 namespace gbv {
+
+static std::atomic<unsigned long long> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 // ---------------------------------------------------------------------
 // Small kernels of the orchestration
@@ -396,7 +400,7 @@ static void cells_device(gbv_context* c, const double* d_xyz, const double* d_w,
   auto classify = [&](const uint32_t* ql, const uint32_t* qr, uint32_t nq, uint32_t out[4]) {
     GBV_CUDA(cudaMemsetAsync(c->list_counts, 0, 4 * sizeof(uint32_t), st));
     classify_kernel<<<nblocks(nq, 256), 256, 0, st>>>(ql, qr, nq, status_s, c->list_counts, rs,
-                                                      rr, os, orw, ms, mr);
+                                                      rr, os, orw, ms, mr); count_launch();
     GBV_CUDA(cudaMemcpyAsync(c->h_counts, c->list_counts, 4 * sizeof(uint32_t),
                              cudaMemcpyDeviceToHost, st));
     GBV_CUDA(cudaStreamSynchronize(st));
@@ -514,7 +518,7 @@ static void cells_device(gbv_context* c, const double* d_xyz, const double* d_w,
     uint32_t* last_i = c->buf<uint32_t>("ext_last_i" + tag, morek);
     extend_lists_kernel<<<nblocks(morek, 128), 128, 0, st>>>(q_r, morek, cur.lists, cur.stride,
                                                              cur.k, cur.last_d2, cur.last_idx,
-                                                             lists, lo_d, lo_i);
+                                                             lists, lo_d, lo_i); count_launch();
     KnnArgs ka{};
     ka.S = &S;
     ka.nq = morek;
@@ -531,7 +535,7 @@ static void cells_device(gbv_context* c, const double* d_xyz, const double* d_w,
     ka.flag_count = flag_count;
     ka.flag_list = flag_list;
     launch_knn(ka, st);
-    add_count_kernel<<<nblocks(morek, 128), 128, 0, st>>>(cnt, morek, cur.k);
+    add_count_kernel<<<nblocks(morek, 128), 128, 0, st>>>(cnt, morek, cur.k); count_launch();
     GBV_CUDA(cudaGetLastError());
     ListSet nx;
     nx.lists = lists;
@@ -551,7 +555,7 @@ static void cells_device(gbv_context* c, const double* d_xyz, const double* d_w,
   c->mg = c->buf<double>("mg", 3 * (size_t)n);
   c->status = c->buf<int32_t>("status", n);
   c->rowptr = c->buf<uint32_t>("rowptr", (size_t)n + 1);
-  facet_count_kernel<<<nblocks((size_t)n + 1, 256), 256, 0, st>>>(S.slot_of, nf, n, c->rowptr);
+  facet_count_kernel<<<nblocks((size_t)n + 1, 256), 256, 0, st>>>(S.slot_of, nf, n, c->rowptr); count_launch();
   uint32_t* stmp = c->buf<uint32_t>("csr_scan_tmp", scan_tmp_elems((size_t)n + 1));
   exclusive_scan_u32(c->rowptr, (size_t)n + 1, stmp, st);
   GBV_CUDA(cudaMemcpyAsync(&c->h_counts[0], c->rowptr + n, 4, cudaMemcpyDeviceToHost, st));
@@ -562,7 +566,7 @@ static void cells_device(gbv_context* c, const double* d_xyz, const double* d_w,
   c->area = c->buf<double>("area", std::max<uint32_t>(nnz32, 1));
   unsort_kernel<<<nblocks(n, 256), 256, 0, st>>>(S.slot_of, n, vol_s, mg_s, status_s, nf, f_nbr,
                                                  f_area, c->rowptr, c->vol, c->mg, c->status,
-                                                 c->nbr, c->area);
+                                                 c->nbr, c->area); count_launch();
   GBV_CUDA(cudaEventRecord(c->ev[4], st));
   c->n = n;
   c->has_cells = true;
@@ -570,11 +574,11 @@ static void cells_device(gbv_context* c, const double* d_xyz, const double* d_w,
   if (rep) {
     double* part = c->buf<double>("sum_part", 2 * 256);
     double* out = c->buf<double>("sum_out", 1);
-    sum_partial_kernel<<<256, kSumThreads, 0, st>>>(c->vol, n, part);
-    sum_final_kernel<<<1, 32, 0, st>>>(part, 256, out);
+    sum_partial_kernel<<<256, kSumThreads, 0, st>>>(c->vol, n, part); count_launch();
+    sum_final_kernel<<<1, 32, 0, st>>>(part, 256, out); count_launch();
     unsigned long long* clips = c->buf<unsigned long long>("clip_sum", 1);
     GBV_CUDA(cudaMemsetAsync(clips, 0, 8, st));
-    sum_u32_kernel<<<256, 256, 0, st>>>(nclip, n, clips);
+    sum_u32_kernel<<<256, 256, 0, st>>>(nclip, n, clips); count_launch();
     double vs = 0;
     unsigned long long cs = 0, hc[2] = {0, 0};
     GBV_CUDA(cudaMemcpyAsync(&vs, out, 8, cudaMemcpyDeviceToHost, st));
@@ -639,6 +643,8 @@ using namespace gbv;
 extern "C" {
 
 const char* gbv_last_error(void) { return g_last_error.c_str(); }
+
+uint64_t gbv_kernel_launches(void) { return g_launches.load(); }
 
 void gbv_cell_options_default(gbv_cell_options* o) {
   if (!o) return;
@@ -761,7 +767,7 @@ gbv_status gbv_lloyd_device(gbv_context* c, double* d_xyz, const double* d_w, ui
     cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
     for (uint32_t it = 0; it < iters; ++it) {
       cells_device(c, d_xyz, d_w, n, *opt, st, report);
-      lloyd_update_kernel<<<nblocks(n, 256), 256, 0, st>>>(d_xyz, c->vol, c->mg, n);
+      lloyd_update_kernel<<<nblocks(n, 256), 256, 0, st>>>(d_xyz, c->vol, c->mg, n); count_launch();
     }
     GBV_CUDA(cudaStreamSynchronize(st));
   });
@@ -779,7 +785,7 @@ gbv_status gbv_lloyd_step(gbv_context* c, double* xyz, const double* w, uint32_t
     GBV_CUDA(cudaMemcpyAsync(dx, xyz, 24 * (size_t)n, cudaMemcpyHostToDevice, c->stream));
     if (w) GBV_CUDA(cudaMemcpyAsync(dw, w, 8 * (size_t)n, cudaMemcpyHostToDevice, c->stream));
     cells_device(c, dx, dw, n, *opt, c->stream, report);
-    lloyd_update_kernel<<<nblocks(n, 256), 256, 0, c->stream>>>(dx, c->vol, c->mg, n);
+    lloyd_update_kernel<<<nblocks(n, 256), 256, 0, c->stream>>>(dx, c->vol, c->mg, n); count_launch();
     GBV_CUDA(cudaMemcpyAsync(xyz, dx, 24 * (size_t)n, cudaMemcpyDeviceToHost, c->stream));
     GBV_CUDA(cudaStreamSynchronize(c->stream));
   });
@@ -820,7 +826,7 @@ gbv_status gbv_nn_get_nearest_neighbors(gbv_context* c, uint32_t nq, const doubl
     double* od = c->buf<double>("nn_od", (size_t)nq * k);
     GBV_CUDA(cudaMemcpyAsync(dq, q, sizeof(double) * (size_t)nq * c->nn_dim,
                              cudaMemcpyHostToDevice, st));
-    to_query4_kernel<<<nblocks(nq, 256), 256, 0, st>>>(dq, nq, c->nn_dim, q4);
+    to_query4_kernel<<<nblocks(nq, 256), 256, 0, st>>>(dq, nq, c->nn_dim, q4); count_launch();
     KnnArgs ka{};
     ka.S = &c->S;
     ka.nq = nq;

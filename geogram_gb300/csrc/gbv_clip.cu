@@ -670,7 +670,7 @@ static void launch_clip(const ClipArgs& a, cudaStream_t st) {
   cudaFuncSetAttribute(clip_kernel<Real, T, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)sh);
   const unsigned nb = (a.nq + kClipThreads - 1) / kClipThreads;
-  clip_kernel<Real, T, P><<<nb, kClipThreads, sh, st>>>(a);
+  clip_kernel<Real, T, P><<<nb, kClipThreads, sh, st>>>(a); count_launch();
   last_launch_error = cudaGetLastError();
 }
 

@@ -25,6 +25,9 @@ enum CellStatus : int32_t {
 
 constexpr uint32_t kNone = 0xFFFFFFFFu;
 
+// Host-side count of this library's kernel launches (gbv_kernel_launches).
+void count_launch();
+
 // Exact FP64 squared distance with the reference's evaluation order
 // (geometry_nd.h:65-73): ((((0 + dx^2) + dy^2) + dz^2) + dh^2), no fusion.
 __device__ __forceinline__ double dist2_exact(double4 a, double4 b) {

@@ -288,7 +288,7 @@ void launch_geometry(const GeomArgs& a, cudaStream_t st) {
   const size_t sh = sizeof(GeomWarpSmem) * kGeomWarps;
   cudaFuncSetAttribute(geom_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh);
   const unsigned nb = (a.nq + kGeomWarps - 1) / kGeomWarps;
-  geom_kernel<<<nb, kGeomWarps * 32, sh, st>>>(a);
+  geom_kernel<<<nb, kGeomWarps * 32, sh, st>>>(a); count_launch();
   last_launch_error = cudaGetLastError();
 }
 

@@ -86,13 +86,13 @@ void exclusive_scan_u32(uint32_t* data, size_t n, uint32_t* tmp, cudaStream_t st
   if (n == 0) return;
   size_t nb = (n + kScanBlock - 1) / kScanBlock;
   if (nb == 1) {
-    scan_block_kernel<<<1, kScanThreads, 0, st>>>(data, n, nullptr);
+    scan_block_kernel<<<1, kScanThreads, 0, st>>>(data, n, nullptr); count_launch();
     return;
   }
   uint32_t* sums = tmp;
-  scan_block_kernel<<<(unsigned)nb, kScanThreads, 0, st>>>(data, n, sums);
+  scan_block_kernel<<<(unsigned)nb, kScanThreads, 0, st>>>(data, n, sums); count_launch();
   exclusive_scan_u32(sums, nb, tmp + nb + 1, st);
-  scan_add_kernel<<<(unsigned)nb, kScanThreads, 0, st>>>(data, n, sums);
+  scan_add_kernel<<<(unsigned)nb, kScanThreads, 0, st>>>(data, n, sums); count_launch();
 }
 
 // ---------------------------------------------------------------------
@@ -226,17 +226,17 @@ int choose_levels(uint32_t n) {
 void build_grid(const double* xyz, uint32_t stride, uint32_t dim, const double* w,
                 uint32_t n, int L, SortedSeeds& S, GridScratch& scr, cudaStream_t st) {
   const int nparts = 120;
-  bbox_partial_kernel<<<nparts, kRedThreads, 0, st>>>(xyz, stride, dim, w, n, scr.red);
+  bbox_partial_kernel<<<nparts, kRedThreads, 0, st>>>(xyz, stride, dim, w, n, scr.red); count_launch();
   bbox_final_kernel<<<1, 32, 0, st>>>(scr.red, nparts, L, w != nullptr, (int)dim, S.gd,
-                                      S.aux);
+                                      S.aux); count_launch();
   const size_t ncells = (size_t)1 << (3 * L);
   cudaMemsetAsync(S.cell_start, 0, sizeof(uint32_t) * (ncells + 1), st);
   const unsigned nb = (n + 255) / 256;
   cell_id_kernel<<<nb, 256, 0, st>>>(xyz, stride, n, S.gd, scr.cid, scr.rank,
-                                     S.cell_start);
+                                     S.cell_start); count_launch();
   exclusive_scan_u32(S.cell_start, ncells + 1, scr.scan_tmp, st);
   scatter_kernel<<<nb, 256, 0, st>>>(xyz, stride, dim, w, n, scr.cid, scr.rank,
-                                     S.cell_start, S.aux, S);
+                                     S.cell_start, S.aux, S); count_launch();
   S.n = n;
   S.L = L;
 }
@@ -573,15 +573,15 @@ void launch_knn(const KnnArgs& a, cudaStream_t st) {
     const size_t sh = (sizeof(double) + sizeof(uint32_t)) * kKnnCap * kKnnThreads;
     cudaFuncSetAttribute(knn_fast_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh);
     cudaMemsetAsync(a.flag_count, 0, sizeof(uint32_t), st);
-    knn_fast_kernel<<<nb, kKnnThreads, sh, st>>>(a, *a.S, a.S->gd, a.S->aux);
+    knn_fast_kernel<<<nb, kKnnThreads, sh, st>>>(a, *a.S, a.S->gd, a.S->aux); count_launch();
     knn_exact_kernel<true><<<nb, kKnnThreads, 0, st>>>(a, *a.S, a.S->gd, a.S->aux, a.flag_list,
-                                                       a.flag_count);
+                                                       a.flag_count); count_launch();
   } else if (a.k <= kKnnSmemK) {
     knn_exact_kernel<true><<<nb, kKnnThreads, 0, st>>>(a, *a.S, a.S->gd, a.S->aux, nullptr,
-                                                       nullptr);
+                                                       nullptr); count_launch();
   } else {
     knn_exact_kernel<false><<<nb, kKnnThreads, 0, st>>>(a, *a.S, a.S->gd, a.S->aux, nullptr,
-                                                        nullptr);
+                                                        nullptr); count_launch();
   }
 }
 

@@ -90,6 +90,11 @@ typedef struct {
 /* Last error message of the calling thread ("" if none). */
 const char* gbv_last_error(void);
 
+/* Number of CUDA kernels this library has launched since it was loaded
+ * (all contexts).  Replaces nothing in the reference; used to account for
+ * the GPU work of a call. */
+uint64_t gbv_kernel_launches(void);
+
 /* Creates a context on CUDA device `device`.  Replaces nothing in the
  * reference (its engines are plain C++ objects); the context owns one
  * CUDA stream and the device buffers. */

@@ -662,6 +662,19 @@ static void* job_main(void* arg) {
     return NULL;
 }
 
+static void run_parallel_range(range_fn fn, void* ctx, unsigned b0, unsigned n, int nthreads) {
+    if (nthreads <= 1 || n - b0 < 256) {
+        fn(ctx, b0, n);
+        return;
+    }
+    unsigned next = b0;
+    job_t job = {fn, ctx, n, &next};
+    pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)nthreads);
+    for (int t = 0; t < nthreads; ++t) pthread_create(&th[t], NULL, job_main, &job);
+    for (int t = 0; t < nthreads; ++t) pthread_join(th[t], NULL);
+    free(th);
+}
+
 static void run_parallel(range_fn fn, void* ctx, unsigned n, int nthreads) {
     if (nthreads <= 1 || n < 256) {
         fn(ctx, 0, n);
@@ -714,6 +727,7 @@ typedef struct {
     double* nbr_area;
     int* status;
     long n_exact;
+    unsigned off;  /* outputs of seed i go to index i - off */
 } cells_ctx;
 
 /* Neighbour list of seed i (delaunay_nn.cpp:104-145). */
@@ -788,26 +802,27 @@ static void cells_range(void* vctx, unsigned b, unsigned e) {
         double m;
         v3 g;
         compute_mg(&C, &m, &g);
-        c->vol[i] = m;
-        c->mg[3 * (size_t)i] = g.x;
-        c->mg[3 * (size_t)i + 1] = g.y;
-        c->mg[3 * (size_t)i + 2] = g.z;
+        const size_t o = (size_t)(i - c->off);
+        c->vol[o] = m;
+        c->mg[3 * o] = g.x;
+        c->mg[3 * o + 1] = g.y;
+        c->mg[3 * o + 2] = g.z;
         unsigned cnt = 0;
         for (int v = 1; v < C.nb_v; ++v) {
             if (C.v2t[v] == END_OF_LIST) continue;
             uint32_t j = C.vglobal[v];
             if (j == 0xFFFFFFFFu) continue;
             if (cnt < c->max_nbr) {
-                c->nbr_idx[(size_t)i * c->max_nbr + cnt] = j;
-                c->nbr_area[(size_t)i * c->max_nbr + cnt] = facet_area(&C, v);
+                c->nbr_idx[o * c->max_nbr + cnt] = j;
+                c->nbr_area[o * c->max_nbr + cnt] = facet_area(&C, v);
             }
             ++cnt;
         }
         if (cnt > c->max_nbr) st = 4;
-        c->nbr_count[i] = cnt;
-        c->k_list[i] = list;
-        c->n_clip[i] = jj;
-        c->status[i] = st;
+        c->nbr_count[o] = cnt;
+        c->k_list[o] = list;
+        c->n_clip[o] = jj;
+        c->status[o] = st;
     }
     __atomic_fetch_add(&c->n_exact, C.n_exact, __ATOMIC_RELAXED);
     free(ix);
@@ -816,13 +831,15 @@ static void cells_range(void* vctx, unsigned b, unsigned e) {
     cell_free(&C);
 }
 
-/* Same contract as ref_cells in oracle/ref/ref_driver.cpp.  Returns the
- * number of exact (expansion) predicate evaluations in *n_exact. */
-int orc_cells(const double* xyz, const double* w, unsigned n, unsigned k0, int check_sr,
-              int exact, int nthreads, double* vol, double* mg, uint32_t* nbr_count,
-              uint32_t* nbr_idx, double* nbr_area, unsigned max_nbr, uint32_t* k_list,
-              uint32_t* n_clip, int* status, long* n_exact) {
-    if (n < 2) return 1;
+/* Cells of seeds [i0, i1) of the n seeds (all n take part as neighbours);
+ * outputs are indexed i - i0.  Same per-seed contract as ref_cells in
+ * oracle/ref/ref_driver.cpp.  *n_exact receives the number of exact
+ * (expansion) predicate evaluations. */
+int orc_cells_range(const double* xyz, const double* w, unsigned n, unsigned i0, unsigned i1,
+                    unsigned k0, int check_sr, int exact, int nthreads, double* vol, double* mg,
+                    uint32_t* nbr_count, uint32_t* nbr_idx, double* nbr_area, unsigned max_nbr,
+                    uint32_t* k_list, uint32_t* n_clip, int* status, long* n_exact) {
+    if (n < 2 || i0 > i1 || i1 > n) return 1;
     unsigned dim = w ? 4u : 3u;
     double* pts = (double*)malloc(sizeof(double) * (size_t)n * dim);
     double* hl = (double*)calloc(n, sizeof(double));
@@ -838,11 +855,20 @@ int orc_cells(const double* xyz, const double* w, unsigned n, unsigned k0, int c
     grid_t g;
     grid_build(&g, pts, dim, n);
     cells_ctx c = {xyz, w, pts, hl, dim, n, k0, max_nbr, check_sr, exact, &g,
-                   vol, mg, nbr_count, nbr_idx, k_list, n_clip, nbr_area, status, 0};
-    run_parallel(cells_range, &c, n, nthreads);
+                   vol, mg, nbr_count, nbr_idx, k_list, n_clip, nbr_area, status, 0, i0};
+    run_parallel_range(cells_range, &c, i0, i1, nthreads);
     if (n_exact) *n_exact = c.n_exact;
     grid_free(&g);
     free(pts);
     free(hl);
     return 0;
+}
+
+/* All n cells; same contract as ref_cells in oracle/ref/ref_driver.cpp. */
+int orc_cells(const double* xyz, const double* w, unsigned n, unsigned k0, int check_sr,
+              int exact, int nthreads, double* vol, double* mg, uint32_t* nbr_count,
+              uint32_t* nbr_idx, double* nbr_area, unsigned max_nbr, uint32_t* k_list,
+              uint32_t* n_clip, int* status, long* n_exact) {
+    return orc_cells_range(xyz, w, n, 0, n, k0, check_sr, exact, nthreads, vol, mg, nbr_count,
+                           nbr_idx, nbr_area, max_nbr, k_list, n_clip, status, n_exact);
 }

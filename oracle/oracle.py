@@ -52,6 +52,8 @@ def port():
         lib.orc_cells.argtypes = [P, P, U, U, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P, P,
                                   P, P, U, P, P, P, P]
         lib.orc_det4_sign.argtypes = [P, P, P, P]
+        lib.orc_cells_range.argtypes = [P, P, U, U, U, U, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_int, P, P, P, P, P, U, P, P, P, P]
         _port = lib
     return _port
 
@@ -127,6 +129,29 @@ def cells(xyz: np.ndarray, w: np.ndarray | None = None, k0: int = 20, check_sr: 
     out["area"] = out["narea"][mask]
     del out["nidx"], out["narea"]
     return out
+
+
+def cells_range_time(xyz: np.ndarray, w: np.ndarray | None, i0: int, i1: int,
+                     nthreads: int, max_nbr: int = 96) -> float:
+    """Seconds the CPU restatement takes for cells [i0, i1) of all the seeds
+    (the bounded CPU-baseline sample); raises if a cell failed."""
+    import time
+    x = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+    n = len(x)
+    wa = None if w is None else np.ascontiguousarray(w, dtype=np.float64)
+    m = i1 - i0
+    vol = np.zeros(m); mg = np.zeros(3 * m); cnt = np.zeros(m, np.uint32)
+    ni = np.zeros(m * max_nbr, np.uint32); na = np.zeros(m * max_nbr)
+    kl = np.zeros(m, np.uint32); nc = np.zeros(m, np.uint32); st = np.zeros(m, np.int32)
+    ne = ctypes.c_long(0)
+    t = time.perf_counter()
+    r = port().orc_cells_range(_p(x), _p(wa), n, i0, i1, 20, 1, 1, nthreads, _p(vol), _p(mg),
+                               _p(cnt), _p(ni), _p(na), max_nbr, _p(kl), _p(nc), _p(st),
+                               ctypes.byref(ne))
+    dt = time.perf_counter() - t
+    if r != 0 or (st == 4).any():
+        raise RuntimeError("oracle cells failed")
+    return dt
 
 
 def det4_sign(p0, p1, p2, p3) -> int:

@@ -1,0 +1,72 @@
+"""Generates the golden fixtures of tests/golden/ from the reference itself.
+
+Runs geogram's own BalancedKdTree and VBW::ConvexCell (compiled from the
+reference sources into oracle/_ref/libgbv_ref.so by oracle/ref/Makefile) on
+small seeded inputs and saves inputs and outputs as compressed .npz files.
+Needs the reference checkout; the fixtures are committed so that the tests
+run without it.
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import oracle  # noqa: E402
+
+
+def gmm(rng, n, k, sigma_lo, sigma_hi, lo=0.2, hi=0.8):
+    means = rng.uniform(lo, hi, (k, 3))
+    sig = rng.uniform(sigma_lo, sigma_hi, k)
+    out = []
+    while len(out) < n:
+        c = rng.integers(0, k, n)
+        p = means[c] + rng.normal(size=(n, 3)) * sig[c, None]
+        ok = np.all((p > 0) & (p < 1), axis=1)
+        out.extend(p[ok])
+    return np.array(out[:n])
+
+
+def cases():
+    rng = np.random.default_rng(0)
+    yield "uniform_1500", rng.random((1500, 3)), None
+    x = rng.random((1500, 3))
+    # weights on the scale of the squared spacing, as in a 1M-seed diagram
+    # with weights in [0, 1e-4] (w * (1e6 / n)^(2/3))
+    w = rng.random(1500) * 1e-4 * (1e6 / 1500) ** (2 / 3)
+    yield "power_1500", x, w
+    yield "clustered_1500", gmm(np.random.default_rng(1), 1500, 8, 0.05, 0.05), None
+    g = (np.arange(6) + 0.5) / 6
+    yield "lattice_216", np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3), None
+    x = np.random.default_rng(2).random((400, 3))
+    yield "duplicates_405", np.concatenate([x, x[[3, 17, 17, 99, 250]]]), None
+
+
+def main():
+    oracle.build_ref()
+    for name, x, w in cases():
+        x = np.ascontiguousarray(x)
+        r = oracle.cells(x, w, nthreads=8, which="ref")
+        np.savez_compressed(os.path.join(HERE, f"cells_{name}.npz"), x=x,
+                            w=np.zeros(0) if w is None else w, vol=r["vol"], mg=r["mg"],
+                            rowptr=r["rowptr"], nbr=r["nbr"], area=r["area"],
+                            status=r["status"], n_clip=r["n_clip"], k_list=r["k_list"])
+        print(name, len(x), "cells, nnz", len(r["nbr"]))
+    x = np.random.default_rng(3).random((2000, 3))
+    idx, d2 = oracle.knn(x, 21, nthreads=8, which="ref")
+    np.savez_compressed(os.path.join(HERE, "knn_2000.npz"), x=x, idx=idx, d2=d2)
+    x4 = np.concatenate([x, np.random.default_rng(4).random((2000, 1)) * 0.01], axis=1)
+    idx, d2 = oracle.knn(x4, 21, nthreads=8, which="ref")
+    np.savez_compressed(os.path.join(HERE, "knn4_2000.npz"), x=x4, idx=idx, d2=d2)
+    print("knn fixtures written")
+
+
+if __name__ == "__main__":
+    main()

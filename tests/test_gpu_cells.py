@@ -1,0 +1,155 @@
+"""GPU cells through the C ABI against the reference's results.
+
+The fixtures hold geogram's own outputs (BalancedKdTree + VBW::ConvexCell,
+tests/golden/make_golden.py).  Both precision modes must reproduce them bit
+for bit: neighbour lists, facet areas, volumes and centroids (the north
+star's bar is 1e-12 relative for volumes and centroids; the engine matches
+exactly).  Degenerate inputs (a lattice) are compared on the quantities
+that do not depend on how equidistant neighbours are ordered."""
+import numpy as np
+import pytest
+
+from conftest import canonical_ids, load_golden
+
+pytestmark = pytest.mark.gpu
+
+EXACT_CASES = ["uniform_1500", "power_1500", "clustered_1500"]
+PRECISIONS = ["fp64", "fp32"]
+
+
+@pytest.fixture(scope="module")
+def g():
+    import geogram_gb300 as g
+    return g
+
+
+def assert_cells_equal(c, ref, nbr=True):
+    assert np.array_equal(c.rowptr.astype(np.int64), np.asarray(ref["rowptr"], np.int64))
+    if nbr:
+        assert np.array_equal(c.neighbors, ref["nbr"])
+        assert np.array_equal(c.facet_area, ref["area"])
+    assert np.array_equal(c.volume, ref["vol"])
+    assert np.array_equal(c.mg, ref["mg"])
+    assert np.array_equal(c.status, ref["status"])
+
+
+@pytest.mark.parametrize("prec", PRECISIONS)
+@pytest.mark.parametrize("name", EXACT_CASES)
+def test_cells_bit_exact_vs_reference(g, name, prec):
+    ref = load_golden(f"cells_{name}.npz")
+    c = g.compute_cells(ref["x"], ref["w"], precision=prec)
+    assert_cells_equal(c, ref)
+
+
+@pytest.mark.parametrize("prec", PRECISIONS)
+def test_lattice_volumes(g, prec):
+    ref = load_golden("cells_lattice_216.npz")
+    c = g.compute_cells(ref["x"], precision=prec)
+    # equidistant neighbours are ordered differently (kd-tree traversal vs
+    # index): the same cells, summed over a different fan decomposition
+    assert np.max(np.abs(c.volume - ref["vol"]) / ref["vol"]) < 1e-12
+    assert np.array_equal(c.rowptr.astype(np.int64), ref["rowptr"])
+    assert c.report["n_exact"] > 0 or prec == "fp32"
+
+
+@pytest.mark.parametrize("prec", PRECISIONS)
+def test_lattice_vs_oracle_bit_exact(g, oracle_mod, prec):
+    """On a lattice the oracle orders ties by index like the GPU: identical."""
+    gg = (np.arange(7) + 0.5) / 7
+    x = np.stack(np.meshgrid(gg, gg, gg, indexing="ij"), -1).reshape(-1, 3)
+    r = oracle_mod.cells(x, nthreads=4)
+    c = g.compute_cells(x, precision=prec)
+    assert_cells_equal(c, r)
+
+
+@pytest.mark.parametrize("prec", PRECISIONS)
+@pytest.mark.parametrize("n", [2, 3, 9, 40, 65, 300])
+def test_small_n(g, oracle_mod, n, prec):
+    x = np.random.default_rng(n).random((n, 3))
+    r = oracle_mod.cells(x, nthreads=2)
+    c = g.compute_cells(x, precision=prec)
+    assert_cells_equal(c, r)
+
+
+@pytest.mark.parametrize("prec", PRECISIONS)
+def test_power_with_empty_cells(g, oracle_mod, prec):
+    """Large weights empty some cells; they must come out empty (volume 0)."""
+    rng = np.random.default_rng(21)
+    x = rng.random((2000, 3))
+    w = rng.random(2000) * 0.02
+    r = oracle_mod.cells(x, w, nthreads=8)
+    c = g.compute_cells(x, w, precision=prec)
+    assert (r["vol"] == 0).any()
+    assert_cells_equal(c, r)
+
+
+@pytest.mark.parametrize("prec", PRECISIONS)
+def test_without_security_radius(g, oracle_mod, prec):
+    """check_sr off: a single pass over the first k0 neighbours (generic_RVD.h:2328)."""
+    x = np.random.default_rng(7).random((1000, 3))
+    for k0 in (10, 20):
+        r = oracle_mod.cells(x, k0=k0, check_sr=False, nthreads=4)
+        c = g.compute_cells(x, k0=k0, check_sr=False, precision=prec)
+        assert_cells_equal(c, r)
+
+
+def test_non_unit_box(g):
+    """Seeds in [0,2]x[0,1]x[0,3]: the cells tile that box."""
+    rng = np.random.default_rng(8)
+    x = rng.random((3000, 3)) * np.array([2.0, 1.0, 3.0])
+    c = g.compute_cells(x, box=((0, 0, 0), (2, 1, 3)))
+    assert abs(c.volume.sum() - 6.0) < 1e-12
+    assert (c.status == g.CELL_CERTIFIED).mean() > 0.9
+
+
+def test_fp32_mode_equals_fp64_mode_at_scale(g):
+    rng = np.random.default_rng(9)
+    x = rng.random((200_000, 3))
+    w = rng.random(200_000) * 1e-4 * 5 ** (2 / 3)
+    a = g.compute_cells(x, w, precision="fp64")
+    b = g.compute_cells(x, w, precision="fp32")
+    assert np.array_equal(a.neighbors, b.neighbors)
+    assert np.array_equal(a.volume, b.volume)
+    assert np.array_equal(a.mg, b.mg)
+    assert b.report["n_recheck_fp64"] < 0.05 * len(x)
+
+
+def test_size_independent_properties_1m(g):
+    """At 1M seeds: total volume 1, symmetric adjacency, matching facet
+    areas on both sides, every cell certified or complete."""
+    rng = np.random.default_rng(10)
+    n = 1_000_000
+    x = rng.random((n, 3))
+    w = rng.random(n) * 1e-4
+    c = g.compute_cells(x, w, precision="fp32")
+    assert abs(c.report["volume_sum"] - 1.0) < 1e-12
+    assert abs(c.volume.sum() - 1.0) < 1e-11
+    assert set(np.unique(c.status)) <= {0, 1}
+    rows = np.repeat(np.arange(n, dtype=np.int64), np.diff(c.rowptr.astype(np.int64)))
+    key = rows * n + c.neighbors
+    rkey = c.neighbors.astype(np.int64) * n + rows
+    o1, o2 = np.argsort(key), np.argsort(rkey)
+    assert np.array_equal(key[o1], rkey[o2])
+    a1, a2 = c.facet_area[o1], c.facet_area[o2]
+    assert np.max(np.abs(a1 - a2) / np.maximum(a1, 1e-300)) < 1e-6
+
+
+@pytest.mark.parametrize("prec", PRECISIONS)
+def test_duplicates_vs_reference(g, oracle_mod, prec):
+    """Duplicated seeds: reference fixture up to which copy names a facet,
+    and the oracle (same tie order as the GPU) bit for bit."""
+    ref = load_golden("cells_duplicates_405.npz")
+    c = g.compute_cells(ref["x"], precision=prec)
+    canon = canonical_ids(ref["x"])
+    assert np.array_equal(c.volume, ref["vol"]) and np.array_equal(c.mg, ref["mg"])
+    assert np.array_equal(c.facet_area, ref["area"])
+    assert np.array_equal(canon[c.neighbors], canon[ref["nbr"]])
+    assert_cells_equal(c, oracle_mod.cells(ref["x"], nthreads=4))
+
+
+def test_duplicates_status(g):
+    ref = load_golden("cells_duplicates_405.npz")
+    c = g.compute_cells(ref["x"])
+    dup = np.nonzero(c.status == g.CELL_DUPLICATE)[0]
+    assert len(dup) == 4  # the higher-index copies
+    assert np.all(c.volume[dup] == 1.0)  # as the reference: unclipped box

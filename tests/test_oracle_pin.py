@@ -1,0 +1,89 @@
+"""The oracle's CPU restatement against the reference's own results.
+
+The golden fixtures were produced by geogram's BalancedKdTree and
+VBW::ConvexCell themselves (tests/golden/make_golden.py, oracle/_ref); the
+restatement must reproduce them bit for bit on non-degenerate inputs, and
+the cell volumes on degenerate ones (a lattice, where equidistant
+neighbours are ordered differently: the kd-tree by traversal, the oracle by
+index).  When the reference build is present the same is checked live."""
+import numpy as np
+import pytest
+
+from conftest import canonical_ids, load_golden
+
+EXACT_CASES = ["uniform_1500", "power_1500", "clustered_1500"]
+
+
+@pytest.mark.parametrize("name", EXACT_CASES)
+def test_port_matches_reference_fixture(oracle_mod, name):
+    g = load_golden(f"cells_{name}.npz")
+    r = oracle_mod.cells(g["x"], g["w"], nthreads=4)
+    for key in ("vol", "mg", "rowptr", "nbr", "area", "status", "n_clip", "k_list"):
+        assert np.array_equal(r[key], g[key]), key
+
+
+def test_port_matches_reference_with_duplicates(oracle_mod):
+    """Copies of a seed are equidistant ties: which copy names a facet
+    follows the tie order, so neighbours are compared up to duplicates."""
+    g = load_golden("cells_duplicates_405.npz")
+    r = oracle_mod.cells(g["x"], None, nthreads=4)
+    canon = canonical_ids(g["x"])
+    for key in ("vol", "mg", "rowptr", "area", "status", "n_clip", "k_list"):
+        assert np.array_equal(r[key], g[key]), key
+    assert np.array_equal(canon[r["nbr"]], canon[g["nbr"]])
+
+
+def test_port_matches_reference_on_lattice(oracle_mod):
+    g = load_golden("cells_lattice_216.npz")
+    r = oracle_mod.cells(g["x"], None, nthreads=4)
+    # tie order changes the fan decomposition: equal up to rounding
+    assert np.max(np.abs(r["vol"] - g["vol"]) / g["vol"]) < 1e-12
+    assert np.max(np.abs(r["mg"] - g["mg"])) < 1e-15
+    assert np.array_equal(r["rowptr"], g["rowptr"])
+    assert np.max(np.abs(np.sort(r["area"]) - np.sort(g["area"]))) < 1e-15
+    assert r["n_exact"] > 0  # the exact predicates were exercised
+    assert abs(r["vol"].sum() - 1.0) < 1e-14
+
+
+@pytest.mark.parametrize("name", ["knn_2000", "knn4_2000"])
+def test_port_knn_matches_reference_fixture(oracle_mod, name):
+    g = load_golden(f"{name}.npz")
+    idx, d2 = oracle_mod.knn(g["x"], 21, nthreads=4)
+    assert np.array_equal(idx, g["idx"])
+    assert np.array_equal(d2, g["d2"])
+
+
+def test_volume_invariant(oracle_mod):
+    """Sum of the cell volumes is the box volume (periodic_delaunay_3d.cpp:4345-4355)."""
+    x = np.random.default_rng(5).random((800, 3))
+    r = oracle_mod.cells(x, nthreads=4)
+    assert abs(r["vol"].sum() - 1.0) < 1e-13
+    # adjacency is symmetric
+    rows = np.repeat(np.arange(800), np.diff(r["rowptr"]))
+    pairs = set(zip(rows.tolist(), r["nbr"].tolist()))
+    assert all((j, i) in pairs for i, j in pairs)
+
+
+def test_det4_exact_sign(oracle_mod):
+    # singular (two equal rows) -> 0; identity -> +1; a tiny perturbation
+    # of a singular matrix beyond double filters -> its true sign
+    a = [1.0, 2.0, 3.0, 4.0]
+    b = [0.5, 0.25, 0.125, 1.0]
+    c = [3.0, 1.0, 4.0, 1.0]
+    assert oracle_mod.det4_sign(a, a, b, c) == 0
+    assert oracle_mod.det4_sign([1, 0, 0, 0], [0, 1, 0, 0], [0, 0, 1, 0], [0, 0, 0, 1]) == 1
+    d = [x + y for x, y in zip(a, b)]
+    eps = 2.0 ** -50  # representable next to 1.5, far below the filter bound
+    assert oracle_mod.det4_sign(a, b, c, [d[0] + eps, d[1], d[2], d[3]]) != 0
+    assert oracle_mod.det4_sign(a, b, c, d) == 0
+
+
+@pytest.mark.skipif("not __import__('oracle.oracle', fromlist=['x']).ref_available()")
+def test_port_matches_reference_live(oracle_mod):
+    x = np.random.default_rng(11).random((3000, 3))
+    w = np.random.default_rng(12).random(3000) * 2e-3
+    for ww in (None, w):
+        a = oracle_mod.cells(x, ww, nthreads=8, which="ref")
+        b = oracle_mod.cells(x, ww, nthreads=8, which="port")
+        for key in ("vol", "mg", "rowptr", "nbr", "area", "status", "n_clip", "k_list"):
+            assert np.array_equal(a[key], b[key]), key
