@@ -25,12 +25,14 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import _lib
-from ._lib import (CELL_ALL_NEIGHBOURS, CELL_CERTIFIED, CELL_DUPLICATE, PRECISION_FP32_RECHECK,
+from ._lib import (CELL_ALL_NEIGHBOURS, CELL_CERTIFIED, CELL_DUPLICATE, CELL_STALLED,
+                   PRECISION_FP32_RECHECK,
                    PRECISION_FP64, CellOptions, CellReport, GbvError)
 
 __all__ = [
     "Context", "NearestNeighborSearch", "Cells", "compute_cells", "lloyd_step",
     "lloyd_iterations", "compute_cells_device", "device_results", "GbvError", "CELL_CERTIFIED", "CELL_ALL_NEIGHBOURS", "CELL_DUPLICATE",
+    "CELL_STALLED",
     "PRECISION_FP64", "PRECISION_FP32_RECHECK", "cell_options",
 ]
 
@@ -101,7 +103,8 @@ class NearestNeighborSearch:
         if dimension not in (3, 4):
             raise ValueError("dimension must be 3 or 4")
         self.dimension = dimension
-        self.ctx = ctx or default_context()
+        # the point set lives in the context: one context per search object
+        self.ctx = ctx or Context(0)
         self.nb_points = 0
 
     def stride_supported(self) -> bool:

@@ -21,6 +21,7 @@ STATUS_NAMES = {
 CELL_CERTIFIED = 0
 CELL_ALL_NEIGHBOURS = 1
 CELL_DUPLICATE = 2
+CELL_STALLED = 3
 
 PRECISION_FP64 = 0
 PRECISION_FP32_RECHECK = 1

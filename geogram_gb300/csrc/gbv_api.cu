@@ -151,9 +151,13 @@ __global__ void extend_lists_kernel(const uint32_t* __restrict__ rows, uint32_t 
   lo_idx[i] = old_last_idx[r];
 }
 
-__global__ void add_count_kernel(uint32_t* __restrict__ cnt, uint32_t m, uint32_t k) {
+// Length of an extended list: the k entries copied plus the new batch; the
+// copies count of the first list is kept.
+__global__ void add_count_kernel(uint32_t* __restrict__ cnt, uint32_t m, uint32_t k,
+                                 const uint32_t* __restrict__ rows,
+                                 const uint32_t* __restrict__ old_cnt) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < m) cnt[i] = k + (cnt[i] & 0x7FFFFFFFu);
+  if (i < m) cnt[i] = pack_cnt(k + (cnt[i] & kCntMask), (old_cnt[rows[i]] >> 24) & 0x7Fu, false);
 }
 
 __global__ void facet_count_kernel(const uint32_t* __restrict__ slot_of,
@@ -370,6 +374,7 @@ static void cells_device(gbv_context* c, const double* d_xyz, const double* d_w,
   ClipArgs cbase{};
   cbase.S = S;
   cbase.n_total = n;
+  cbase.k0 = o.k0;
   GeomArgs gbase{};
   gbase.S = S;
   for (int k = 0; k < 3; ++k) {
@@ -535,7 +540,7 @@ static void cells_device(gbv_context* c, const double* d_xyz, const double* d_w,
     ka.flag_count = flag_count;
     ka.flag_list = flag_list;
     launch_knn(ka, st);
-    add_count_kernel<<<nblocks(morek, 128), 128, 0, st>>>(cnt, morek, cur.k); count_launch();
+    add_count_kernel<<<nblocks(morek, 128), 128, 0, st>>>(cnt, morek, cur.k, q_r, cur.cnt); count_launch();
     GBV_CUDA(cudaGetLastError());
     ListSet nx;
     nx.lists = lists;

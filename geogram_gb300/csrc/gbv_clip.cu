@@ -350,7 +350,12 @@ __global__ void __launch_bounds__(kClipThreads) clip_kernel(ClipArgs a) {
 
   const uint32_t cnt_raw = a.nbr_cnt[row];
   const bool dup = (cnt_raw >> 31) != 0;
-  const uint32_t cnt = dup ? 0u : cnt_raw;
+  const uint32_t copies = (cnt_raw >> 24) & 0x7Fu;
+  // a seed with higher-index copies: the reference stops growing its list
+  // at reference_list_cap, certified or not
+  const uint32_t cap = copies ? reference_list_cap(a.k0, a.n_total, copies, a.check_sr != 0)
+                              : 0xFFFFFFFFu;
+  const uint32_t cnt = dup ? 0u : min(cnt_raw & kCntMask, cap);
   int32_t st = -1;
   uint32_t jj = 0;
   unsigned long long n_exact = 0;
@@ -614,8 +619,9 @@ __global__ void __launch_bounds__(kClipThreads) clip_kernel(ClipArgs a) {
     }
     if (st < 0) {
       // list exhausted without certification
-      const bool complete = (cnt < a.list_k) || (a.list_k >= a.n_total - 1);
+      const bool complete = ((cnt_raw & kCntMask) < a.list_k) || (a.list_k >= a.n_total - 1);
       if (!a.check_sr) st = CELL_CERTIFIED;
+      else if (copies && cnt == cap) st = (cap == 0) ? CELL_DUPLICATE : CELL_STALLED;
       else st = complete ? CELL_ALL_NEIGHBOURS : CELL_NEED_MORE_K;
     }
   }

@@ -34,6 +34,7 @@ struct ClipArgs {
   const uint32_t* nbr_cnt;    // per row; bit 31 = lower-index duplicate
   uint32_t list_k;            // capacity of the lists
   uint32_t n_total;           // number of seeds
+  uint32_t k0;                // first list length asked (reference_list_cap)
   const uint32_t* qlist;      // sorted slots to process (nullptr: all)
   const uint32_t* qrow;       // list row of each query (nullptr: row = qi)
   uint32_t nq;

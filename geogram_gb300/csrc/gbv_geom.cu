@@ -108,7 +108,8 @@ __global__ void __launch_bounds__(kGeomWarps * 32) geom_kernel(GeomArgs a) {
   // ---- FP32 clipping: the reference stops at the same neighbour only if
   // d(stop) > 4.1 (R2 + h^2) and d(last clipped) <= 4.1 (R2 + h^2) with the
   // final cell's R2 (R2 only shrinks while clipping)
-  if (a.verify_sr && (st == CELL_CERTIFIED || st == CELL_ALL_NEIGHBOURS)) {
+  if (a.verify_sr &&
+      (st == CELL_CERTIFIED || st == CELL_ALL_NEIGHBOURS || st == CELL_STALLED)) {
     const uint32_t row = a.qrow ? a.qrow[ci] : ci;
     const uint32_t jj = a.nclip[s];
     const double thr = __dmul_rn(4.1, __dadd_rn(R2, __dmul_rn(pi.w, pi.w)));

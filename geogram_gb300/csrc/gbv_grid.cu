@@ -363,9 +363,9 @@ __device__ __forceinline__ bool after_lo(const QueryCtx& c, double d, uint32_t i
 
 __device__ __forceinline__ void write_outputs(const KnnArgs& a, const SortedSeeds& S,
                                               const QueryCtx& c, uint32_t qi, uint32_t cnt,
-                                              bool dup_lower, const double* ld, const uint32_t* ls,
-                                              uint32_t stride) {
-  if (a.cnt) a.cnt[qi] = (a.mode == KNN_CELLS && dup_lower) ? 0x80000000u : cnt;
+                                              uint32_t copies, bool dup_lower, const double* ld,
+                                              const uint32_t* ls, uint32_t stride) {
+  if (a.cnt) a.cnt[qi] = (a.mode == KNN_CELLS) ? pack_cnt(cnt, copies, dup_lower) : cnt;
   if (a.mode == KNN_CELLS && dup_lower) cnt = 0;
   if (a.nbr)
     for (uint32_t r = 0; r < cnt; ++r) a.nbr[(size_t)r * a.out_stride + qi] = ls[(size_t)r * stride];
@@ -415,7 +415,7 @@ knn_exact_kernel(KnnArgs a, SortedSeeds S, const GridDesc* __restrict__ gdp,
   const QueryCtx c = make_query(a, S, g, qi);
   const float delta = 8.0f * (float)aux[1] * 5.9604645e-8f + 1e-30f;
   const uint32_t K = a.k;
-  uint32_t cnt = 0;
+  uint32_t cnt = 0, copies = 0;
   double worst = DBL_MAX;
   float thr = FLT_MAX;
   bool dup_lower = false;
@@ -432,6 +432,7 @@ knn_exact_kernel(KnnArgs a, SortedSeeds S, const GridDesc* __restrict__ gdp,
       const uint32_t pj = S.perm[s2];
       if (a.mode == KNN_CELLS && d == 0.0) {
         if (pj < c.qperm) dup_lower = true;
+        else ++copies;
         continue;
       }
       if (!after_lo(c, d, pj)) continue;
@@ -458,7 +459,7 @@ knn_exact_kernel(KnnArgs a, SortedSeeds S, const GridDesc* __restrict__ gdp,
       }
     }
   });
-  write_outputs(a, S, c, qi, cnt, dup_lower, ld, ls, stride);
+  write_outputs(a, S, c, qi, cnt, copies, dup_lower, ld, ls, stride);
 }
 
 // ---- fast search: FP32 list of k + kKnnExtra, exact FP64 re-rank ---------
@@ -485,7 +486,7 @@ knn_fast_kernel(KnnArgs a, SortedSeeds S, const GridDesc* __restrict__ gdp,
   const uint32_t cap = K + kKnnExtra;
   // the FP32 distance lives in the low word of the list's double slot
   auto D32 = [&](uint32_t r) -> float& { return *reinterpret_cast<float*>(&s_d[r][tid]); };
-  uint32_t cnt = 0;
+  uint32_t cnt = 0, copies = 0;
   float thr = FLT_MAX;
   float dropped = FLT_MAX;
   bool dup_lower = false;
@@ -513,6 +514,7 @@ knn_fast_kernel(KnnArgs a, SortedSeeds S, const GridDesc* __restrict__ gdp,
       if (a.mode == KNN_CELLS && d32 <= 0.f) {
         if (dist2_exact(c.q, S.xd[s2]) == 0.0) {
           if (S.perm[s2] < c.qperm) dup_lower = true;
+          else ++copies;
           continue;
         }
       }
@@ -562,7 +564,7 @@ knn_fast_kernel(KnnArgs a, SortedSeeds S, const GridDesc* __restrict__ gdp,
     s_d[pos][tid] = d;
     s_s[pos][tid] = sl;
   }
-  write_outputs(a, S, c, qi, cnt < K ? cnt : K, dup_lower, &s_d[0][tid], &s_s[0][tid],
+  write_outputs(a, S, c, qi, cnt < K ? cnt : K, copies, dup_lower, &s_d[0][tid], &s_s[0][tid],
                 kKnnThreads);
 }
 

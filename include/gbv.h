@@ -43,6 +43,12 @@ enum {
     GBV_CELL_DUPLICATE = 2,       /* a lower-index seed at distance 0: the
                                      neighbour list is empty, the cell is
                                      the unclipped box (as the reference)   */
+    GBV_CELL_STALLED = 3,         /* the seed has higher-index copies: its
+                                     lists are shorter than asked for, their
+                                     growth stalls before certification and
+                                     the reference stops there (the cell is
+                                     not certified; delaunay_nn.cpp:104-145,
+                                     generic_RVD.h:2297-2299)               */
     GBV_CELL_NEED_MORE_K = 16,    /* internal: list exhausted, retried      */
     GBV_CELL_OVERFLOW = 17,       /* internal: capacity exceeded, retried   */
     GBV_CELL_RECHECK = 18,        /* internal: FP32 could not certify       */
