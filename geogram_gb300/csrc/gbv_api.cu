@@ -437,6 +437,7 @@ static void cells_device(gbv_context* c, const double* d_xyz, const double* d_w,
     g.qrow = qr;
     g.nq = nq;
     g.verify_sr = (f32 && o.check_sr) ? 1 : 0;
+    g.shape = kind == 2 ? CLIP_LARGE : CLIP_SMALL;
     launch_geometry(g, st);
     GBV_CUDA(last_launch_error);
   };

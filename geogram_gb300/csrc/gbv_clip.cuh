@@ -67,6 +67,7 @@ struct GeomArgs {
   uint32_t nq;
   double box[6];
   int verify_sr;              // FP32 clipping: check its stops in FP64
+  int shape;                  // ClipShape of the clipping pass
   CombBuf comb;
   int32_t* status;
   const uint32_t* nclip;

@@ -10,11 +10,13 @@
 //     first contributing one gives the fan origin t_origin, every other
 //     facet is fanned from v2t[v] around the plane;
 //   facet_area (convex_cell.cpp:1160-1191) for the seed facets.
-// The lanes compute corners and tetrahedron terms in parallel; one lane
-// adds the terms in the reference's order.  For cells clipped in FP32 the
-// kernel also checks, in FP64, that the reference's security-radius loop
-// would have stopped at the same neighbour, and sends the cell back to
-// FP64 clipping otherwise.
+// The FP64 work is spread over the lanes: one corner, one tetrahedron or
+// one facet triangle per lane, from fan sequences walked in shared memory;
+// four lanes then add the tetrahedron terms in the reference's order (one
+// accumulator each), one lane per facet adds its area terms.  For cells
+// clipped in FP32 the kernel also checks, in FP64, that the reference's
+// security-radius loop would have stopped at the same neighbour, and sends
+// the cell back to FP64 clipping otherwise.
 #include <cfloat>
 
 #include "gbv_clip.cuh"
@@ -22,29 +24,37 @@
 
 namespace gbv {
 
-constexpr int kGeomWarps = 4;
-constexpr int kMaxTerms = 2 * kTMax;  // tetrahedra of one cell, at most 2 nt - 4
+constexpr int kGeomWarps = 8;
 
+// T, P: the capacities of the clipping shape whose cells are processed.
+template <int T, int P>
 struct GeomWarpSmem {
-  double px[kTMax], py[kTMax], pz[kTMax];  // corners
-  double4 plane[kPMax];
-  int v2t[kPMax];                           // (eff + 32768) << 8 | triangle, -1: none
-  uint16_t prank[kPMax];                    // list position (0xFFFF: box face)
-  int16_t ntets[kPMax];                     // per rank
-  int16_t toff[kPMax + 1];                  // term offsets per rank
-  uint8_t order[kPMax];                     // contributing planes in creation order
-  double tm[kMaxTerms], tx[kMaxTerms], ty[kMaxTerms], tz[kMaxTerms];
+  static constexpr int kTerms = 2 * T;   // fan triangles of one cell, at most 2 nt - 4
+  double px[T], py[T], pz[T];            // corners
+  double4 plane[P];
+  double tm[kTerms], tx[kTerms], ty[kTerms], tz[kTerms];  // volume terms
+  double ta[kTerms];                     // area terms
+  uint32_t tv[T], tadj[T];               // the cell's triangles
+  int v2t[P];                            // (eff + 32768) << 8 | triangle, -1: none
+  uint16_t prank[P];                     // list position (0xFFFF: box face)
+  int16_t fstart[P + 1];                 // fan sequence offsets per rank
+  int16_t vofs[P + 1];                   // volume-term offsets per rank
+  int16_t aofs[P + 1];                   // area-term offsets per rank (seed facets)
+  uint8_t fan[3 * T];                    // fan sequences (triangles around planes)
+  uint8_t order[P];                      // contributing planes in creation order
+  uint8_t tlist[T];                      // used triangle slots, compacted
 };
 
-__device__ __forceinline__ double plane_from_owner_w(double qi, double qj) { return __dsub_rn(qi, qj); }
-
+template <int T, int P>
 __global__ void __launch_bounds__(kGeomWarps * 32) geom_kernel(GeomArgs a) {
+  constexpr int NH = (P + 31) / 32;  // planes (and ranks) per lane
+  using Sm = GeomWarpSmem<T, P>;
   extern __shared__ __align__(16) unsigned char geom_smem[];
-  GeomWarpSmem* smw = reinterpret_cast<GeomWarpSmem*>(geom_smem);
+  Sm* smw = reinterpret_cast<Sm*>(geom_smem);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t ci = blockIdx.x * kGeomWarps + warp;
   if (ci >= a.nq) return;
-  GeomWarpSmem& g = smw[warp];
+  Sm& g = smw[warp];
   const SortedSeeds& S = a.S;
   const uint32_t s = a.qlist ? a.qlist[ci] : ci;
   const int32_t st = a.status[s];
@@ -56,39 +66,52 @@ __global__ void __launch_bounds__(kGeomWarps * 32) geom_kernel(GeomArgs a) {
   const int parity = (cb.flags[s] & 1u) ? -1 : 1;
   const double4 pi = S.xd[s];
   const double qi = S.q[s];
+  const unsigned FULL = 0xFFFFFFFFu;
 
-  // ---- planes (FP64, the reference's global frame) and v2t init
-  for (int p = lane; p < kPMax; p += 32) {
+  // ---- used triangles, compacted; planes (FP64, the reference's frame)
+  const int nt0 = __popcll(tm2.x);
+  const int ntri = nt0 + (T > 64 ? __popcll(tm2.y) : 0);
+  for (int h = 0; h < (T > 64 ? 2 : 1); ++h) {
+    const uint64_t w = h ? tm2.y : tm2.x;
+    for (int b = 2 * lane; b < 2 * lane + 2; ++b) {
+      if (!((w >> b) & 1ull)) continue;
+      const int pos = (h ? nt0 : 0) + __popcll(w & ((1ull << b) - 1ull));
+      const int t = 64 * h + b;
+      g.tlist[pos] = (uint8_t)t;
+      g.tv[t] = cb.tv[tb + t];
+      g.tadj[t] = cb.ta[tb + t];
+    }
+  }
+  for (int p = lane; p < P; p += 32) {
     g.v2t[p] = -1;
     g.prank[p] = 0xFFFF;
     if ((pm >> p) & 1ull) {
       g.prank[p] = cb.prank[pb + p];
       const uint32_t own = cb.pown[pb + p];
-      double4 P;
+      double4 Q;
       if (own >= kBoxBase) {
         switch (own - kBoxBase) {
-          case 0: P = make_double4(1.0, 0.0, 0.0, -a.box[0]); break;
-          case 1: P = make_double4(-1.0, 0.0, 0.0, a.box[3]); break;
-          case 2: P = make_double4(0.0, 1.0, 0.0, -a.box[1]); break;
-          case 3: P = make_double4(0.0, -1.0, 0.0, a.box[4]); break;
-          case 4: P = make_double4(0.0, 0.0, 1.0, -a.box[2]); break;
-          default: P = make_double4(0.0, 0.0, -1.0, a.box[5]); break;
+          case 0: Q = make_double4(1.0, 0.0, 0.0, -a.box[0]); break;
+          case 1: Q = make_double4(-1.0, 0.0, 0.0, a.box[3]); break;
+          case 2: Q = make_double4(0.0, 1.0, 0.0, -a.box[1]); break;
+          case 3: Q = make_double4(0.0, -1.0, 0.0, a.box[4]); break;
+          case 4: Q = make_double4(0.0, 0.0, 1.0, -a.box[2]); break;
+          default: Q = make_double4(0.0, 0.0, -1.0, a.box[5]); break;
         }
       } else {
         const double4 pj = S.xd[own];
-        P = make_double4(2.0 * __dsub_rn(pi.x, pj.x), 2.0 * __dsub_rn(pi.y, pj.y),
-                         2.0 * __dsub_rn(pi.z, pj.z), plane_from_owner_w(qi, S.q[own]));
+        Q = make_double4(2.0 * __dsub_rn(pi.x, pj.x), 2.0 * __dsub_rn(pi.y, pj.y),
+                         2.0 * __dsub_rn(pi.z, pj.z), __dsub_rn(qi, S.q[own]));
       }
-      g.plane[p] = P;
+      g.plane[p] = Q;
     }
   }
   __syncwarp();
   // ---- corners (compute_geometry) and v2t
   double R2 = 0.0;
-  for (int t = lane; t < kTMax; t += 32) {
-    const uint64_t w = (t < 64) ? tm2.x : tm2.y;
-    if (!((w >> (t & 63)) & 1ull)) continue;
-    const uint32_t v = cb.tv[tb + t];
+  for (int i = lane; i < ntri; i += 32) {
+    const int t = g.tlist[i];
+    const uint32_t v = g.tv[t];
     const int a0 = v & 0xFF, a1 = v >> 8 & 0xFF, a2 = v >> 16 & 0xFF;
     const double3 c = r_corner(g.plane[a0], g.plane[a1], g.plane[a2]);
     g.px[t] = c.x;
@@ -102,7 +125,7 @@ __global__ void __launch_bounds__(kGeomWarps * 32) geom_kernel(GeomArgs a) {
     atomicMax(&g.v2t[a2], packed);
   }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) R2 = fmax(R2, __shfl_xor_sync(0xFFFFFFFFu, R2, o));
+  for (int o = 16; o > 0; o >>= 1) R2 = fmax(R2, __shfl_xor_sync(FULL, R2, o));
   __syncwarp();
 
   // ---- FP32 clipping: the reference stops at the same neighbour only if
@@ -130,27 +153,31 @@ __global__ void __launch_bounds__(kGeomWarps * 32) geom_kernel(GeomArgs a) {
 
   // ---- planes in the reference's creation order: box faces 0-5 (their
   // slots), then the seeds in clipping order (list position)
-  int rank_of[2] = {-1, -1};
-  int nseed_before[2] = {0, 0};
-  bool is_seed[2] = {false, false};
+  int rank_of[NH], nseed_before[NH];
+  bool is_seed[NH];
   int ncontrib = 0;
   {
-    int cidx[2] = {0x7FFFFFFF, 0x7FFFFFFF};
-    for (int h = 0; h < 2; ++h) {
+    int cidx[NH];
+#pragma unroll
+    for (int h = 0; h < NH; ++h) {
       const int p = lane + 32 * h;
-      if (g.v2t[p] >= 0) {
+      rank_of[h] = -1;
+      nseed_before[h] = 0;
+      is_seed[h] = false;
+      cidx[h] = 0x7FFFFFFF;
+      if (p < P && g.v2t[p] >= 0) {
         is_seed[h] = g.prank[p] != 0xFFFF;
         cidx[h] = is_seed[h] ? 6 + g.prank[p] : p;
         rank_of[h] = 0;
       }
     }
-    for (int q = 0; q < kPMax; ++q) {
+    for (int q = 0; q < P; ++q) {
       if (g.v2t[q] < 0) continue;
       ++ncontrib;
       const bool qseed = g.prank[q] != 0xFFFF;
       const int iq = qseed ? 6 + g.prank[q] : q;
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
+      for (int h = 0; h < NH; ++h) {
         if (rank_of[h] < 0) continue;
         if (iq < cidx[h]) {
           ++rank_of[h];
@@ -159,7 +186,7 @@ __global__ void __launch_bounds__(kGeomWarps * 32) geom_kernel(GeomArgs a) {
       }
     }
 #pragma unroll
-    for (int h = 0; h < 2; ++h)
+    for (int h = 0; h < NH; ++h)
       if (rank_of[h] >= 0) g.order[rank_of[h]] = (uint8_t)(lane + 32 * h);
   }
   __syncwarp();
@@ -173,124 +200,158 @@ __global__ void __launch_bounds__(kGeomWarps * 32) geom_kernel(GeomArgs a) {
     }
     return;
   }
-  const int t_origin = g.v2t[g.order[0]] & 0xFF;
-  auto find_vertex = [&](uint32_t t, uint32_t v) -> int {
-    const uint32_t x = cb.tv[tb + t];
-    return ((x >> 8 & 0xFF) == v) + 2 * ((x >> 16 & 0xFF) == v);
+  auto next_around = [&](uint32_t t, uint32_t v) -> uint32_t {
+    const uint32_t x = g.tv[t];
+    const int lv = ((x >> 8 & 0xFF) == v) + 2 * ((x >> 16 & 0xFF) == v);
+    return (g.tadj[t] >> (8 * ((lv + 1) % 3))) & 0xFF;
   };
-  auto adjacent = [&](uint32_t t, int e) -> uint32_t {
-    return (cb.ta[tb + t] >> (8 * e)) & 0xFF;
-  };
-  auto corner = [&](int t) { return make_double3(g.px[t], g.py[t], g.pz[t]); };
-
-  // ---- fan sizes per rank (the origin facet, rank 0, adds no term)
-  for (int r = lane; r < kPMax; r += 32) {
-    int cnt = 0;
-    if (r >= 1 && r < ncontrib) {
+  // ---- fan lengths per rank
+  int deg_r[NH], vol_r[NH], area_r[NH];
+#pragma unroll
+  for (int h = 0; h < NH; ++h) {
+    const int r = lane + 32 * h;
+    deg_r[h] = 0;
+    if (r < ncontrib) {
       const int p = g.order[r];
-      const int t0 = g.v2t[p] & 0xFF;
-      int t = t0, deg = 0;
+      const uint32_t t0 = g.v2t[p] & 0xFF;
+      uint32_t t = t0;
+      int deg = 0;
       do {
         ++deg;
-        t = adjacent(t, (find_vertex(t, p) + 1) % 3);
-      } while (t != t0 && deg < 2 * kTMax);
-      cnt = deg - 2;
+        t = next_around(t, p);
+      } while (t != t0 && deg < 3 * T);
+      deg_r[h] = deg;
     }
-    g.ntets[r] = (int16_t)cnt;
+    vol_r[h] = (r < ncontrib && r > 0) ? deg_r[h] - 2 : 0;
+    area_r[h] = (r < ncontrib && g.prank[g.order[r]] != 0xFFFF) ? deg_r[h] - 2 : 0;
   }
-  __syncwarp();
-  if (lane == 0) {
-    int acc = 0;
-    for (int r = 0; r < ncontrib; ++r) {
-      g.toff[r] = (int16_t)acc;
-      acc += g.ntets[r];
-    }
-    g.toff[ncontrib] = (int16_t)min(acc, kMaxTerms);
-  }
-  __syncwarp();
-  // ---- tetrahedron terms of compute_mg, written at their sequence position
-  const double3 po = corner(t_origin);
-  for (int r = lane; r < ncontrib; r += 32) {
-    if (r == 0) continue;
-    const int p = g.order[r];
-    const int t0 = g.v2t[p] & 0xFF;
-    int t = t0, cur = 0, k = g.toff[r];
-    double3 q1 = po, q2 = po;
-    int guard = 0;
-    do {
-      const double3 pt = corner(t);
-      if (cur == 0) {
-        q1 = pt;
-      } else if (cur == 1) {
-        q2 = pt;
-      } else if (k < kMaxTerms) {
-        const double cm = r_tet_volume(po, q1, q2, pt);
-        g.tm[k] = cm;
-        g.tx[k] = __ddiv_rn(__dmul_rn(cm, __dadd_rn(__dadd_rn(__dadd_rn(po.x, q1.x), q2.x), pt.x)), 4.0);
-        g.ty[k] = __ddiv_rn(__dmul_rn(cm, __dadd_rn(__dadd_rn(__dadd_rn(po.y, q1.y), q2.y), pt.y)), 4.0);
-        g.tz[k] = __ddiv_rn(__dmul_rn(cm, __dadd_rn(__dadd_rn(__dadd_rn(po.z, q1.z), q2.z), pt.z)), 4.0);
-        ++k;
-        q2 = pt;
+  // exclusive scans over the ranks of: fan length, volume terms, area terms
+  {
+    int base_f = 0, base_v = 0, base_a = 0;
+#pragma unroll
+    for (int h = 0; h < NH; ++h) {
+      int f = deg_r[h], v = vol_r[h], ar = area_r[h];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int yf = __shfl_up_sync(FULL, f, o), yv = __shfl_up_sync(FULL, v, o),
+                  ya = __shfl_up_sync(FULL, ar, o);
+        if (lane >= o) {
+          f += yf;
+          v += yv;
+          ar += ya;
+        }
       }
-      ++cur;
-      t = adjacent(t, (find_vertex(t, p) + 1) % 3);
-    } while (t != t0 && ++guard < 2 * kTMax);
+      const int r = lane + 32 * h;
+      if (r < P) {
+        g.fstart[r] = (int16_t)(base_f + f - deg_r[h]);
+        g.vofs[r] = (int16_t)(base_v + v - vol_r[h]);
+        g.aofs[r] = (int16_t)(base_a + ar - area_r[h]);
+      }
+      base_f += __shfl_sync(FULL, f, 31);
+      base_v += __shfl_sync(FULL, v, 31);
+      base_a += __shfl_sync(FULL, ar, 31);
+    }
+    if (lane == 0) {
+      g.fstart[P] = (int16_t)base_f;
+      g.vofs[P] = (int16_t)base_v;
+      g.aofs[P] = (int16_t)base_a;
+    }
   }
   __syncwarp();
-  if (lane == 0) {
-    double m = 0.0, gx = 0.0, gy = 0.0, gz = 0.0;
-    const int nterm = g.toff[ncontrib];
-    for (int k = 0; k < nterm; ++k) {
-      m = __dadd_rn(m, g.tm[k]);
-      gx = __dadd_rn(gx, g.tx[k]);
-      gy = __dadd_rn(gy, g.ty[k]);
-      gz = __dadd_rn(gz, g.tz[k]);
-    }
-    a.vol[s] = m;
-    a.mg[s] = gx;
-    a.mg[(size_t)a.out_stride + s] = gy;
-    a.mg[2 * (size_t)a.out_stride + s] = gz;
+  // ---- fan sequences (triangles around each plane from v2t)
+#pragma unroll
+  for (int h = 0; h < NH; ++h) {
+    const int r = lane + 32 * h;
+    if (r >= ncontrib) continue;
+    const int p = g.order[r];
+    const uint32_t t0 = g.v2t[p] & 0xFF;
+    uint32_t t = t0;
+    int k = g.fstart[r];
+    const int kend = k + deg_r[h];
+    do {
+      g.fan[k++] = (uint8_t)t;
+      t = next_around(t, p);
+    } while (t != t0 && k < kend);
   }
-  // ---- facets shared with other seeds (facet_area), clipping order
+  __syncwarp();
+  const int nvol = min((int)g.vofs[P], Sm::kTerms), narea = min((int)g.aofs[P], Sm::kTerms);
+  const int t_origin = g.v2t[g.order[0]] & 0xFF;
+  const double3 po = make_double3(g.px[t_origin], g.py[t_origin], g.pz[t_origin]);
+  auto corner = [&](int t) { return make_double3(g.px[t], g.py[t], g.pz[t]); };
+  // the rank owning term k: the last rank whose offset is <= k
+  auto rank_of_term = [&](const int16_t* ofs, int k) -> int {
+    int lo = 0, hi = ncontrib - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (ofs[mid] <= k) lo = mid;
+      else hi = mid - 1;
+    }
+    return lo;
+  };
+  // ---- tetrahedron terms of compute_mg: tet j of rank r is
+  // (t_origin, fan[0], fan[j+1], fan[j+2])
+  for (int k = lane; k < nvol; k += 32) {
+    const int r = rank_of_term(g.vofs, k);
+    const int j = k - g.vofs[r];
+    const uint8_t* fan = &g.fan[g.fstart[r]];
+    const double3 q1 = corner(fan[0]), q2 = corner(fan[j + 1]), q3 = corner(fan[j + 2]);
+    const double cm = r_tet_volume(po, q1, q2, q3);
+    g.tm[k] = cm;
+    // cm * (p + q + r + s) / 4.0: the division by 4 is the exact product by 0.25
+    g.tx[k] = __dmul_rn(__dmul_rn(cm, __dadd_rn(__dadd_rn(__dadd_rn(po.x, q1.x), q2.x), q3.x)), 0.25);
+    g.ty[k] = __dmul_rn(__dmul_rn(cm, __dadd_rn(__dadd_rn(__dadd_rn(po.y, q1.y), q2.y), q3.y)), 0.25);
+    g.tz[k] = __dmul_rn(__dmul_rn(cm, __dadd_rn(__dadd_rn(__dadd_rn(po.z, q1.z), q2.z), q3.z)), 0.25);
+  }
+  // ---- facet-area terms: triangle j of a seed facet is (fan[0], fan[j+1], fan[j+2])
+  for (int k = lane; k < narea; k += 32) {
+    const int r = rank_of_term(g.aofs, k);
+    const int j = k - g.aofs[r];
+    const uint8_t* fan = &g.fan[g.fstart[r]];
+    g.ta[k] = r_triangle_area(corner(fan[0]), corner(fan[j + 1]), corner(fan[j + 2]));
+  }
+  __syncwarp();
+  // ---- sums in the reference's order: one accumulator per lane 0-3
+  if (lane < 4) {
+    const double* src = lane == 0 ? g.tm : (lane == 1 ? g.tx : (lane == 2 ? g.ty : g.tz));
+    double acc = 0.0;
+    for (int k = 0; k < nvol; ++k) acc = __dadd_rn(acc, src[k]);
+    if (lane == 0) a.vol[s] = acc;
+    else a.mg[(size_t)(lane - 1) * a.out_stride + s] = acc;
+  }
+  // ---- facets shared with other seeds, in clipping order
   int nfac_lane = 0;
-  for (int h = 0; h < 2; ++h) {
+#pragma unroll
+  for (int h = 0; h < NH; ++h) {
     const int p = lane + 32 * h;
     if (rank_of[h] < 0 || !is_seed[h]) continue;
     ++nfac_lane;
-    const int t0 = g.v2t[p] & 0xFF;
-    int t = t0, cur = 0, guard = 0;
-    double3 q0 = po, q1 = po;
+    const int r = rank_of[h];
     double area = 0.0;
-    do {
-      const double3 pt = corner(t);
-      if (cur == 0) {
-        q0 = pt;
-      } else if (cur == 1) {
-        q1 = pt;
-      } else {
-        area = __dadd_rn(area, r_triangle_area(q0, q1, pt));
-        q1 = pt;
-      }
-      ++cur;
-      t = adjacent(t, (find_vertex(t, p) + 1) % 3);
-    } while (t != t0 && ++guard < 2 * kTMax);
+    const int k1 = min((int)g.aofs[r + 1], narea);
+    for (int k = g.aofs[r]; k < k1; ++k) area = __dadd_rn(area, g.ta[k]);
     const int pos = nseed_before[h];
     a.f_nbr[(size_t)pos * a.out_stride + s] = S.perm[cb.pown[pb + p]];
     a.f_area[(size_t)pos * a.out_stride + s] = area;
   }
   int nfac = nfac_lane;
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) nfac += __shfl_xor_sync(0xFFFFFFFFu, nfac, o);
+  for (int o = 16; o > 0; o >>= 1) nfac += __shfl_xor_sync(FULL, nfac, o);
   if (lane == 0) a.nf[s] = (uint32_t)nfac;
+}
+
+template <int T, int P>
+static void launch_geom(const GeomArgs& a, cudaStream_t st) {
+  const size_t sh = sizeof(GeomWarpSmem<T, P>) * kGeomWarps;
+  cudaFuncSetAttribute(geom_kernel<T, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh);
+  const unsigned nb = (a.nq + kGeomWarps - 1) / kGeomWarps;
+  geom_kernel<T, P><<<nb, kGeomWarps * 32, sh, st>>>(a); count_launch();
+  last_launch_error = cudaGetLastError();
 }
 
 void launch_geometry(const GeomArgs& a, cudaStream_t st) {
   if (a.nq == 0) return;
-  const size_t sh = sizeof(GeomWarpSmem) * kGeomWarps;
-  cudaFuncSetAttribute(geom_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh);
-  const unsigned nb = (a.nq + kGeomWarps - 1) / kGeomWarps;
-  geom_kernel<<<nb, kGeomWarps * 32, sh, st>>>(a); count_launch();
-  last_launch_error = cudaGetLastError();
+  if (a.shape == CLIP_LARGE) launch_geom<kLargeT, kLargeP>(a, st);
+  else launch_geom<kSmallT, kSmallP>(a, st);
 }
 
 }  // namespace gbv

@@ -462,13 +462,14 @@ knn_exact_kernel(KnnArgs a, SortedSeeds S, const GridDesc* __restrict__ gdp,
   write_outputs(a, S, c, qi, cnt, copies, dup_lower, ld, ls, stride);
 }
 
-// ---- fast search: FP32 list of k + kKnnExtra, exact FP64 re-rank ---------
-// Every seed of the true k nearest (in exact (d2, index) order) lies within
-// FP32 distance sqrt(d32_k) + 2 delta of the query, where d32_k is the k-th
-// FP32 distance found and delta bounds |FP32 - FP64| distance.  The list
-// keeps every candidate under that threshold up to k + kKnnExtra entries;
-// if a candidate under the final threshold had to be dropped, the query is
-// flagged and redone by the exact search.
+// ---- fast search: FP32 selection of k + kKnnExtra, exact FP64 re-rank ------
+// The k + kKnnExtra nearest by FP32 distance are kept in a bounded max-heap
+// (its root is the pruning threshold).  Every seed of the true k nearest
+// (exact (d2, index) order) lies within FP32 distance sqrt(d32_k) + 2 delta
+// of the query, where d32_k is the k-th FP32 distance and delta bounds
+// |FP32 - FP64| distance; if the heap's root is not beyond that, a seed of
+// the true k nearest may have been dropped and the query is flagged for the
+// exact search.  The kept seeds are heap-sorted, then re-ranked in FP64.
 __global__ void __launch_bounds__(kKnnThreads)
 knn_fast_kernel(KnnArgs a, SortedSeeds S, const GridDesc* __restrict__ gdp,
                 const double* __restrict__ aux) {
@@ -488,7 +489,6 @@ knn_fast_kernel(KnnArgs a, SortedSeeds S, const GridDesc* __restrict__ gdp,
   auto D32 = [&](uint32_t r) -> float& { return *reinterpret_cast<float*>(&s_d[r][tid]); };
   uint32_t cnt = 0, copies = 0;
   float thr = FLT_MAX;
-  float dropped = FLT_MAX;
   bool dup_lower = false;
   // lower bound: candidates surely before it are skipped, those near it are
   // compared exactly
@@ -500,12 +500,34 @@ knn_fast_kernel(KnnArgs a, SortedSeeds S, const GridDesc* __restrict__ gdp,
     lo_skip = r1 * r1 * 0.9999924f;
     lo_check = r2 * r2 * 1.0000076f;
   }
+  auto sift_down = [&](uint32_t i, uint32_t n) {
+    const float d = D32(i);
+    const uint32_t sl = s_s[i][tid];
+    for (;;) {
+      uint32_t c1 = 2 * i + 1;
+      if (c1 >= n) break;
+      float dc = D32(c1);
+      if (c1 + 1 < n) {
+        const float d2 = D32(c1 + 1);
+        if (d2 > dc) {
+          dc = d2;
+          ++c1;
+        }
+      }
+      if (dc <= d) break;
+      D32(i) = dc;
+      s_s[i][tid] = s_s[c1][tid];
+      i = c1;
+    }
+    D32(i) = d;
+    s_s[i][tid] = sl;
+  };
   traverse(S, g, c.ux, c.uy, c.uz, [&]() { return thr; }, [&](uint32_t b, uint32_t en) {
     for (uint32_t s2 = b; s2 < en; ++s2) {
       const float4 p = S.xf[s2];
       const float dx = p.x - c.qf.x, dy = p.y - c.qf.y, dz = p.z - c.qf.z, dh = p.w - c.qf.w;
       const float d32 = dx * dx + dy * dy + dz * dz + dh * dh;
-      if (d32 > thr) continue;
+      if (d32 >= thr) continue;
       if (a.mode == KNN_CELLS && s2 == c.qslot) continue;
       if (c.has_lo) {
         if (d32 < lo_skip) continue;
@@ -518,34 +540,48 @@ knn_fast_kernel(KnnArgs a, SortedSeeds S, const GridDesc* __restrict__ gdp,
           continue;
         }
       }
-      if (cnt == cap) {
-        if (d32 >= D32(cap - 1)) {
-          dropped = fminf(dropped, d32);
-          continue;
+      if (cnt < cap) {
+        // push and sift up
+        uint32_t i = cnt++;
+        while (i > 0) {
+          const uint32_t par = (i - 1) >> 1;
+          const float dp = D32(par);
+          if (dp >= d32) break;
+          D32(i) = dp;
+          s_s[i][tid] = s_s[par][tid];
+          i = par;
         }
-        dropped = fminf(dropped, D32(cap - 1));
-      }
-      uint32_t pos = (cnt < cap) ? cnt : cap - 1;
-      while (pos > 0 && D32(pos - 1) > d32) {
-        D32(pos) = D32(pos - 1);
-        s_s[pos][tid] = s_s[pos - 1][tid];
-        --pos;
-      }
-      D32(pos) = d32;
-      s_s[pos][tid] = s2;
-      if (cnt < cap) ++cnt;
-      if (cnt >= K) {
-        const float r = sqrtf(D32(K - 1)) * 1.0000076f + 2.f * delta;
-        thr = r * r * 1.0000076f;
+        D32(i) = d32;
+        s_s[i][tid] = s2;
+        if (cnt == cap) thr = D32(0);
+      } else {
+        // replace the root (the farthest kept) and sift down
+        D32(0) = d32;
+        s_s[0][tid] = s2;
+        sift_down(0, cap);
+        thr = D32(0);
       }
     }
   });
-  if (dropped <= thr) {
-    // a candidate that may belong to the k nearest was dropped
-    const uint32_t k = atomicAdd(a.flag_count, 1u);
-    a.flag_list[k] = qi;
-    if (a.cnt) a.cnt[qi] = 0;
-    return;
+  // heap sort: ascending FP32 distance
+  for (uint32_t n = cnt; n > 1; --n) {
+    const float dr = D32(0);
+    const uint32_t sr = s_s[0][tid];
+    D32(0) = D32(n - 1);
+    s_s[0][tid] = s_s[n - 1][tid];
+    D32(n - 1) = dr;
+    s_s[n - 1][tid] = sr;
+    sift_down(0, n - 1);
+  }
+  if (cnt == cap) {
+    const float r = sqrtf(D32(K - 1)) * 1.0000076f + 2.f * delta;
+    if (!(D32(cap - 1) > r * r * 1.0000076f)) {
+      // a seed that may belong to the k nearest could have been dropped
+      const uint32_t k = atomicAdd(a.flag_count, 1u);
+      a.flag_list[k] = qi;
+      if (a.cnt) a.cnt[qi] = 0;
+      return;
+    }
   }
   // exact distances, then insertion sort by (d2, original index)
   for (uint32_t r = 0; r < cnt; ++r) s_d[r][tid] = dist2_exact(c.q, S.xd[s_s[r][tid]]);
