@@ -90,6 +90,7 @@ SIGNATURES = {
                                       ctypes.POINTER(CellReport)]),
     "gbv_lloyd_device": (ctypes.c_int, [_P, _P, _P, _U32, _U32, ctypes.POINTER(CellOptions), _P,
                                         ctypes.POINTER(CellReport)]),
+    "gbv_knn_noalloc": (ctypes.c_int, [_P, _U32, _U32, _U32, _U32, _P, _P, _P]),
 }
 
 _lib = None

@@ -100,6 +100,7 @@ namespace gbv {
 
 static std::atomic<unsigned long long> g_launches{0};
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void set_last_error(const char* msg) { g_last_error = msg; }
 
 // ---------------------------------------------------------------------
 // Small kernels of the orchestration

@@ -61,6 +61,8 @@ __host__ __device__ inline uint32_t reference_list_cap(uint32_t k0, uint32_t n, 
 
 // Host-side count of this library's kernel launches (gbv_kernel_launches).
 void count_launch();
+// Sets the calling thread's gbv_last_error() message.
+void set_last_error(const char* msg);
 
 // Exact FP64 squared distance with the reference's evaluation order
 // (geometry_nd.h:65-73): ((((0 + dx^2) + dy^2) + dz^2) + dh^2), no fusion.

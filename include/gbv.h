@@ -196,6 +196,34 @@ gbv_status gbv_lloyd_device(gbv_context* ctx, double* d_xyz, const double* d_w,
                             const gbv_cell_options* opt, void* stream,
                             gbv_cell_report* report);
 
+/* ---------------------------------------------------------------- */
+/* Allocation-free kNN                                               */
+/* ---------------------------------------------------------------- */
+
+/* Largest point count gbv_knn_noalloc accepts. */
+#define GBV_NOALLOC_MAX_POINTS 32768u
+
+/* No counterpart in the reference: an allocation-free variant of the kNN
+ * search for callers that must not allocate GPU memory while they run
+ * (code under a strict device-memory budget or using its own memory pool,
+ * regions where an allocation's implicit synchronisation is not allowed,
+ * latency-bound loops).  Same result as gbv_nn_set_points followed by
+ * gbv_nn_get_nearest_neighbors_all: row i of d_idx / d_d2 (n rows of k)
+ * holds the k nearest of point i, the point itself included, ascending
+ * (d2, index).  All arrays are device pointers; the work is enqueued on
+ * `stream` (a cudaStream_t, NULL = the legacy default stream) and the call
+ * does not wait for it.  It calls no cudaMalloc or cudaFree: its scratch is
+ * a fixed array inside the library (about 3.2 MB, held on every device that
+ * loads the library until the process exits).  Limits: 1 <= n <=
+ * GBV_NOALLOC_MAX_POINTS (larger n returns GBV_ERR_CAPACITY), dim 3 or 4,
+ * stride >= dim doubles, 1 <= k <= min(n, 64).  The scratch is shared by
+ * every call and keeps the last call's contents: calls whose work overlaps
+ * on the GPU race and corrupt each other's results, so order them on one
+ * stream.  The first call on a device looks up the scratch's address on
+ * that device; make that first call before any stream capture. */
+gbv_status gbv_knn_noalloc(const double* d_pts, uint32_t n, uint32_t dim, uint32_t stride,
+                           uint32_t k, uint32_t* d_idx, double* d_d2, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
