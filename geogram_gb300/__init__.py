@@ -13,6 +13,12 @@ reference's C++ one:
   lloyd_step / lloyd_iterations
                           CentroidalVoronoiTesselation::Lloyd_iterations
                           (voronoi/CVT.cpp:133-167) on meshless cells
+  ot_solve / ot_gradient_hessian
+                          semi-discrete optimal transport to the uniform
+                          measure on a box (exploragram OptimalTransportMap3d,
+                          driven by compute_OTM/main.cpp:280-296): damped
+                          Newton on the weights, the dual's gradient and
+                          Laguerre Hessian
 
 Everything runs on the GPU through libgbv.so (C ABI in include/gbv.h).
 Host arrays are numpy; device arrays are torch CUDA tensors.
@@ -26,14 +32,15 @@ import numpy as np
 
 from . import _lib
 from ._lib import (CELL_ALL_NEIGHBOURS, CELL_CERTIFIED, CELL_DUPLICATE, CELL_STALLED,
-                   PRECISION_FP32_RECHECK,
-                   PRECISION_FP64, CellOptions, CellReport, GbvError)
+                   CERTIFY_POWER_RANGE, CERTIFY_SECURITY_RADIUS, PRECISION_FP32_RECHECK,
+                   PRECISION_FP64, CellOptions, CellReport, GbvError, OtOptions, OtReport)
 
 __all__ = [
     "Context", "NearestNeighborSearch", "Cells", "compute_cells", "lloyd_step",
     "lloyd_iterations", "compute_cells_device", "device_results", "GbvError", "CELL_CERTIFIED", "CELL_ALL_NEIGHBOURS", "CELL_DUPLICATE",
     "CELL_STALLED",
-    "PRECISION_FP64", "PRECISION_FP32_RECHECK", "cell_options",
+    "PRECISION_FP64", "PRECISION_FP32_RECHECK", "cell_options", "CERTIFY_SECURITY_RADIUS",
+    "CERTIFY_POWER_RANGE", "ot_options", "ot_solve", "ot_solve_device", "ot_gradient_hessian",
 ]
 
 
@@ -75,8 +82,16 @@ def default_context() -> Context:
     return _default_ctx
 
 
+def _precision(precision: str | int) -> int:
+    if isinstance(precision, str):
+        return {"fp64": PRECISION_FP64, "fp32": PRECISION_FP32_RECHECK,
+                "fp32_recheck": PRECISION_FP32_RECHECK}[precision]
+    return int(precision)
+
+
 def cell_options(box=((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)), k0: int = 20, check_sr: bool = True,
-                 precision: str | int = "fp64") -> CellOptions:
+                 precision: str | int = "fp64", certification: str = "security_radius"
+                 ) -> CellOptions:
     o = CellOptions()
     _lib.load().gbv_cell_options_default(ctypes.byref(o))
     for c in range(3):
@@ -84,10 +99,25 @@ def cell_options(box=((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)), k0: int = 20, check_sr:
         o.box_max[c] = float(box[1][c])
     o.k0 = int(k0)
     o.check_sr = 1 if check_sr else 0
-    if isinstance(precision, str):
-        precision = {"fp64": PRECISION_FP64, "fp32": PRECISION_FP32_RECHECK,
-                     "fp32_recheck": PRECISION_FP32_RECHECK}[precision]
-    o.precision = int(precision)
+    o.precision = _precision(precision)
+    o.certification = {"security_radius": CERTIFY_SECURITY_RADIUS,
+                       "power_range": CERTIFY_POWER_RANGE}[certification]
+    return o
+
+
+def ot_options(box=((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)), tol: float = 1e-6, max_newton: int = 100,
+               max_cg: int = 4000, precision: str | int = "fp32", cg_rtol: float = 1e-3
+               ) -> OtOptions:
+    o = OtOptions()
+    _lib.load().gbv_ot_options_default(ctypes.byref(o))
+    for c in range(3):
+        o.box_min[c] = float(box[0][c])
+        o.box_max[c] = float(box[1][c])
+    o.tol = float(tol)
+    o.max_newton = int(max_newton)
+    o.max_cg = int(max_cg)
+    o.precision = _precision(precision)
+    o.cg_rtol = float(cg_rtol)
     return o
 
 
@@ -169,13 +199,18 @@ class Cells:
 
 def compute_cells(xyz: np.ndarray, weights: np.ndarray | None = None, *,
                   box=((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)), k0: int = 20, check_sr: bool = True,
-                  precision: str | int = "fp64", ctx: Context | None = None) -> Cells:
-    """Certified Laguerre cells of the seeds xyz (n x 3) with weights (n)."""
+                  precision: str | int = "fp64", certification: str = "security_radius",
+                  ctx: Context | None = None) -> Cells:
+    """Certified Laguerre cells of the seeds xyz (n x 3) with weights (n).
+
+    certification "security_radius" reproduces the reference's clipping
+    loop; "power_range" finds every seed that can cut a cell by a range
+    query on the power distance (for widely spread weights)."""
     ctx = ctx or default_context()
     x = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
     n = len(x)
     w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float64).reshape(n)
-    o = cell_options(box, k0, check_sr, precision)
+    o = cell_options(box, k0, check_sr, precision, certification)
     rep = CellReport()
     L = ctx._lib
     _lib.check(L.gbv_cells_compute(ctx.handle, _lib.ptr(x), _lib.ptr(w), n, ctypes.byref(o),
@@ -249,3 +284,64 @@ def lloyd_iterations(xyz_dev, iters: int, weights_dev=None, *,
                                          xyz_dev.shape[0], iters, ctypes.byref(o), st,
                                          ctypes.byref(rep)))
     return rep.as_dict()
+
+
+def ot_solve(xyz: np.ndarray, nu: np.ndarray | None = None, w0: np.ndarray | None = None, *,
+             box=((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)), tol: float = 1e-6, max_newton: int = 100,
+             max_cg: int = 4000, precision="fp32", cg_rtol: float = 1e-3,
+             ctx: Context | None = None) -> tuple[np.ndarray, dict]:
+    """Weights of the seeds whose Laguerre cells in the box have volumes nu
+    (default: box volume / n each), starting from w0 (default zeros)."""
+    ctx = ctx or default_context()
+    x = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+    n = len(x)
+    w = np.zeros(n) if w0 is None else np.array(w0, dtype=np.float64, copy=True).reshape(n)
+    m = None if nu is None else np.ascontiguousarray(nu, dtype=np.float64).reshape(n)
+    o = ot_options(box, tol, max_newton, max_cg, precision, cg_rtol)
+    rep = OtReport()
+    _lib.check(ctx._lib.gbv_ot_solve(ctx.handle, _lib.ptr(x), _lib.ptr(m), n, ctypes.byref(o),
+                                     _lib.ptr(w), ctypes.byref(rep)))
+    return w, rep.as_dict()
+
+
+def ot_solve_device(xyz_dev, w_dev, nu_dev=None, *, box=((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)),
+                    tol: float = 1e-6, max_newton: int = 100, max_cg: int = 4000,
+                    precision="fp32", cg_rtol: float = 1e-3, stream=None,
+                    ctx: Context | None = None) -> dict:
+    """ot_solve on torch CUDA tensors; w_dev (float64, n) is updated in place."""
+    ctx = ctx or default_context()
+    o = ot_options(box, tol, max_newton, max_cg, precision, cg_rtol)
+    rep = OtReport()
+    st = ctypes.c_void_p(stream.cuda_stream) if stream is not None else None
+    _lib.check(ctx._lib.gbv_ot_solve_device(ctx.handle, _lib.ptr(xyz_dev), _lib.ptr(nu_dev),
+                                            xyz_dev.shape[0], ctypes.byref(o), _lib.ptr(w_dev),
+                                            st, ctypes.byref(rep)))
+    return rep.as_dict()
+
+
+def ot_gradient_hessian(xyz: np.ndarray, w: np.ndarray, nu: np.ndarray | None = None, *,
+                        box=((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)), precision="fp32",
+                        ctx: Context | None = None):
+    """Gradient nu - vol and CSR Hessian (rowptr, col, val, diag) of the dual."""
+    ctx = ctx or default_context()
+    x = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+    n = len(x)
+    ww = np.ascontiguousarray(w, dtype=np.float64).reshape(n)
+    m = None if nu is None else np.ascontiguousarray(nu, dtype=np.float64).reshape(n)
+    o = ot_options(box, precision=precision)
+    nnz = ctypes.c_uint64()
+    L = ctx._lib
+    _lib.check(L.gbv_ot_gradient_hessian(ctx.handle, _lib.ptr(x), _lib.ptr(ww), _lib.ptr(m), n,
+                                         ctypes.byref(o), None, None, None, None, None, 0,
+                                         ctypes.byref(nnz)))
+    k = max(nnz.value, 1)
+    g = np.empty(n)
+    rp = np.empty(n + 1, np.uint32)
+    col = np.empty(k, np.uint32)
+    val = np.empty(k)
+    diag = np.empty(n)
+    _lib.check(L.gbv_ot_gradient_hessian(ctx.handle, _lib.ptr(x), _lib.ptr(ww), _lib.ptr(m), n,
+                                         ctypes.byref(o), _lib.ptr(g), _lib.ptr(rp),
+                                         _lib.ptr(col), _lib.ptr(val), _lib.ptr(diag), k,
+                                         ctypes.byref(nnz)))
+    return g, (rp, col[:nnz.value], val[:nnz.value], diag)

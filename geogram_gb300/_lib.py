@@ -40,8 +40,45 @@ class CellOptions(ctypes.Structure):
         ("k0", ctypes.c_uint32),
         ("check_sr", ctypes.c_uint32),
         ("precision", ctypes.c_uint32),
-        ("reserved", ctypes.c_uint32),
+        ("certification", ctypes.c_uint32),
     ]
+
+
+CERTIFY_SECURITY_RADIUS = 0
+CERTIFY_POWER_RANGE = 1
+
+
+class OtOptions(ctypes.Structure):
+    _fields_ = [
+        ("box_min", ctypes.c_double * 3),
+        ("box_max", ctypes.c_double * 3),
+        ("tol", ctypes.c_double),
+        ("max_newton", ctypes.c_uint32),
+        ("max_cg", ctypes.c_uint32),
+        ("precision", ctypes.c_uint32),
+        ("reserved", ctypes.c_uint32),
+        ("cg_rtol", ctypes.c_double),
+    ]
+
+
+class OtReport(ctypes.Structure):
+    _fields_ = [
+        ("converged", ctypes.c_uint32),
+        ("newton_iters", ctypes.c_uint32),
+        ("cg_iters", ctypes.c_uint32),
+        ("halvings", ctypes.c_uint32),
+        ("cell_calls", ctypes.c_uint32),
+        ("reserved", ctypes.c_uint32),
+        ("mass_error_inf", ctypes.c_double),
+        ("mass_error_l2", ctypes.c_double),
+        ("min_volume", ctypes.c_double),
+        ("ms_total", ctypes.c_double),
+        ("ms_cells", ctypes.c_double),
+        ("ms_linear", ctypes.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
 
 
 class CellReport(ctypes.Structure):
@@ -61,6 +98,8 @@ class CellReport(ctypes.Structure):
         ("ms_clip", ctypes.c_double),
         ("ms_retry", ctypes.c_double),
         ("ms_total", ctypes.c_double),
+        ("n_huge", ctypes.c_uint32),
+        ("reserved", ctypes.c_uint32),
     ]
 
     def as_dict(self) -> dict:
@@ -90,6 +129,14 @@ SIGNATURES = {
                                       ctypes.POINTER(CellReport)]),
     "gbv_lloyd_device": (ctypes.c_int, [_P, _P, _P, _U32, _U32, ctypes.POINTER(CellOptions), _P,
                                         ctypes.POINTER(CellReport)]),
+    "gbv_ot_options_default": (None, [ctypes.POINTER(OtOptions)]),
+    "gbv_ot_solve": (ctypes.c_int, [_P, _P, _P, _U32, ctypes.POINTER(OtOptions), _P,
+                                    ctypes.POINTER(OtReport)]),
+    "gbv_ot_solve_device": (ctypes.c_int, [_P, _P, _P, _U32, ctypes.POINTER(OtOptions), _P, _P,
+                                           ctypes.POINTER(OtReport)]),
+    "gbv_ot_gradient_hessian": (ctypes.c_int, [_P, _P, _P, _P, _U32, ctypes.POINTER(OtOptions),
+                                               _P, _P, _P, _P, _P, ctypes.c_uint64,
+                                               ctypes.POINTER(ctypes.c_uint64)]),
     "gbv_knn_noalloc": (ctypes.c_int, [_P, _U32, _U32, _U32, _U32, _P, _P, _P]),
 }
 

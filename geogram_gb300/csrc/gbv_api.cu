@@ -16,6 +16,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cfloat>
+#include <chrono>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -25,6 +27,7 @@
 #include <vector>
 
 #include "gbv_clip.cuh"
+#include "gbv_ot.cuh"
 
 namespace {
 
@@ -165,7 +168,7 @@ __global__ void facet_count_kernel(const uint32_t* __restrict__ slot_of,
                                    const uint32_t* __restrict__ nf, uint32_t n,
                                    uint32_t* __restrict__ rowptr) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) rowptr[i] = nf[slot_of[i]];
+  if (i < n) rowptr[i] = nf[slot_of[i]] & ~kHugeFacets;
   if (i == n) rowptr[n] = 0;
 }
 
@@ -175,6 +178,8 @@ __global__ void unsort_kernel(const uint32_t* __restrict__ slot_of, uint32_t n,
                               const int32_t* __restrict__ st_s, const uint32_t* __restrict__ nf,
                               const uint32_t* __restrict__ f_nbr,
                               const double* __restrict__ f_area,
+                              uint32_t* const* __restrict__ hp_nbr,
+                              double* const* __restrict__ hp_area,
                               const uint32_t* __restrict__ rowptr, double* __restrict__ vol,
                               double* __restrict__ mg, int32_t* __restrict__ status,
                               uint32_t* __restrict__ nbr, double* __restrict__ area) {
@@ -187,6 +192,15 @@ __global__ void unsort_kernel(const uint32_t* __restrict__ slot_of, uint32_t n,
   mg[3 * (size_t)i + 2] = mg_s[2 * (size_t)n + s];
   status[i] = st_s[s];
   const uint32_t b = rowptr[i], c = nf[s];
+  if (c & kHugeFacets) {
+    const uint32_t* hn = hp_nbr[s];
+    const double* ha = hp_area[s];
+    for (uint32_t f = 0; f < (c & ~kHugeFacets); ++f) {
+      nbr[b + f] = hn[f];
+      area[b + f] = ha[f];
+    }
+    return;
+  }
   for (uint32_t f = 0; f < c; ++f) {
     nbr[b + f] = f_nbr[(size_t)f * n + s];
     area[b + f] = f_area[(size_t)f * n + s];
@@ -308,102 +322,187 @@ struct ListSet {
   const uint32_t* last_idx = nullptr;
 };
 
-// The whole cell computation on device inputs.
-static void cells_device(gbv_context* c, const double* d_xyz, const double* d_w, uint32_t n,
-                         const gbv_cell_options& o, cudaStream_t st, gbv_cell_report* rep) {
-  if (n == 0) throw StatusError{GBV_ERR_INVALID_ARGUMENT, "n must be > 0"};
-  const bool fp32 = o.precision == GBV_PRECISION_FP32_RECHECK;
-  setup_seeds(c, n, d_w != nullptr);
-  c->nn_ready = false;
-  SortedSeeds& S = c->S;
-  GBV_CUDA(cudaEventRecord(c->ev[0], st));
-  build_grid(d_xyz, 3, 3, d_w, n, S.L, S, c->scr, st);
-  GBV_CUDA(cudaEventRecord(c->ev[1], st));
+// Cells with extra candidates from the certification: their slots, list
+// rows and counts.
+__global__ void collect_extra_kernel(const uint32_t* __restrict__ qlist, uint32_t nq,
+                                     const uint32_t* __restrict__ extra_cnt,
+                                     const int32_t* __restrict__ status,
+                                     uint32_t* __restrict__ count, uint32_t* __restrict__ out_s,
+                                     uint32_t* __restrict__ out_r) {
+  const uint32_t qi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (qi >= nq) return;
+  const uint32_t s = qlist ? qlist[qi] : qi;
+  if (status[s] >= CELL_NEED_MORE_K) return;
+  if (extra_cnt[qi] == 0) return;
+  const uint32_t k = atomicAdd(count, 1u);
+  out_s[k] = s;
+  out_r[k] = qi;
+}
 
-  // per-cell results by slot, and the combinatorics records
-  int32_t* status_s = c->buf<int32_t>("status_s", n);
-  double* vol_s = c->buf<double>("vol_s", n);
-  double* mg_s = c->buf<double>("mg_s", 3 * (size_t)n);
-  uint32_t* nf = c->buf<uint32_t>("nf", n);
-  uint32_t* nclip = c->buf<uint32_t>("nclip", n);
-  uint32_t* f_nbr = c->buf<uint32_t>("f_nbr", (size_t)kMaxFacets * n);
-  double* f_area = c->buf<double>("f_area", (size_t)kMaxFacets * n);
-  CombBuf cb;
-  cb.tv = c->buf<uint32_t>("cb_tv", (size_t)kTMax * n);
-  cb.ta = c->buf<uint32_t>("cb_ta", (size_t)kTMax * n);
-  cb.key = c->buf<int16_t>("cb_key", (size_t)kTMax * n);
-  cb.pown = c->buf<uint32_t>("cb_pown", (size_t)kPMax * n);
-  cb.prank = c->buf<uint16_t>("cb_prank", (size_t)kPMax * n);
-  cb.tmask = c->buf<ulonglong2>("cb_tmask", n);
-  cb.pmask = c->buf<uint64_t>("cb_pmask", n);
-  cb.flags = c->buf<uint32_t>("cb_flags", n);
-  GBV_CUDA(cudaMemsetAsync(c->counters, 0, 2 * sizeof(unsigned long long), st));
-  uint32_t* flag_count = c->buf<uint32_t>("knn_flag_count", 1);
-  uint32_t* flag_list = c->buf<uint32_t>("knn_flag_list", n);
-
-  // first lists
-  const uint32_t nm1 = n > 1 ? n - 1 : 0;
-  uint32_t K = o.check_sr ? std::min<uint32_t>(kKnnSmemK, nm1) : std::min<uint32_t>(o.k0, nm1);
-  const bool long_first = K > kKnnSmemK;  // only without the security radius
-  uint32_t* knn = c->buf<uint32_t>("knn", (size_t)std::max<uint32_t>(K, 1) * n);
-  uint32_t* kcnt = c->buf<uint32_t>("kcnt", n);
-  double* klast_d = c->buf<double>("klast_d", n);
-  uint32_t* klast_i = c->buf<uint32_t>("klast_i", n);
-  {
-    KnnArgs ka{};
-    ka.S = &S;
-    ka.nq = n;
-    ka.k = K;
-    ka.mode = KNN_CELLS;
-    ka.nbr = knn;
-    ka.out_stride = n;
-    ka.cnt = kcnt;
-    ka.last_d2 = klast_d;
-    ka.last_idx = klast_i;
-    ka.flag_count = flag_count;
-    ka.flag_list = flag_list;
-    if (long_first) {
-      ka.gl_d2 = c->buf<double>("knn_gd2", (size_t)K * n);
-      ka.gl_slot = c->buf<uint32_t>("knn_gslot", (size_t)K * n);
+// New lists = old list of the row, then the certification's extras sorted
+// by (distance to the seed, original index).  The range query meets the
+// extras in slot order, and slots within a grid cell depend on the order of
+// the counting sort's atomics; sorting makes the clipping order, hence the
+// results, deterministic (and clips nearer seeds first).
+__global__ void append_extra_kernel(const uint32_t* __restrict__ sl, const uint32_t* __restrict__ rows,
+                                    uint32_t m, const uint32_t* __restrict__ old_lists,
+                                    uint32_t old_stride, const uint32_t* __restrict__ old_cnt,
+                                    const uint32_t* __restrict__ extra,
+                                    const uint32_t* __restrict__ extra_cnt, uint32_t ex_stride,
+                                    uint32_t max_extra, const double4* __restrict__ xd,
+                                    const uint32_t* __restrict__ perm,
+                                    uint32_t* __restrict__ new_lists,
+                                    uint32_t* __restrict__ new_cnt) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const uint32_t r = rows[i], s = sl[i];
+  const uint32_t c0 = old_cnt[r] & kCntMask;
+  for (uint32_t j = 0; j < c0; ++j) new_lists[(size_t)j * m + i] = old_lists[(size_t)j * old_stride + r];
+  const uint32_t ce = min(extra_cnt[r] & 0x7FFFFFFFu, max_extra);
+  const double4 pi = xd[s];
+  auto key_of = [&](uint32_t j, double& d, uint32_t& o) {
+    const double4 p = xd[j];
+    const double dx = p.x - pi.x, dy = p.y - pi.y, dz = p.z - pi.z;
+    d = dx * dx + dy * dy + dz * dz;
+    o = perm[j];
+  };
+  // insertion sort into place (few extras per cell; a handful of cells
+  // next to dense clusters have hundreds)
+  for (uint32_t j = 0; j < ce; ++j) {
+    const uint32_t v = extra[(size_t)j * ex_stride + r];
+    double dv;
+    uint32_t ov;
+    key_of(v, dv, ov);
+    uint32_t k = j;
+    while (k > 0) {
+      const uint32_t u = new_lists[(size_t)(c0 + k - 1) * m + i];
+      double du;
+      uint32_t ou;
+      key_of(u, du, ou);
+      if (du < dv || (du == dv && ou < ov)) break;
+      new_lists[(size_t)(c0 + k) * m + i] = u;
+      --k;
     }
-    if (K > 0) launch_knn(ka, st);
-    else GBV_CUDA(cudaMemsetAsync(kcnt, 0, sizeof(uint32_t) * n, st));
-    GBV_CUDA(cudaGetLastError());
+    new_lists[(size_t)(c0 + k) * m + i] = v;
   }
-  GBV_CUDA(cudaEventRecord(c->ev[2], st));
+  new_cnt[i] = c0 + ce;
+}
 
+// Candidate lists from a CSR adjacency in the caller's order.
+__global__ void csr_to_lists_kernel(const uint32_t* __restrict__ rowptr,
+                                    const uint32_t* __restrict__ idx,
+                                    const uint32_t* __restrict__ slot_of, uint32_t n, uint32_t k,
+                                    uint32_t* __restrict__ lists, uint32_t* __restrict__ cnt) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t s = slot_of[i];
+  const uint32_t b = rowptr[i];
+  const uint32_t c = min(rowptr[i + 1] - b, k);
+  for (uint32_t j = 0; j < c; ++j) lists[(size_t)j * n + s] = slot_of[idx[b + j]];
+  cnt[s] = c;
+}
+
+__global__ void max_degree_kernel(const uint32_t* __restrict__ rowptr, uint32_t n,
+                                  uint32_t* __restrict__ out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t d = (i < n) ? rowptr[i + 1] - rowptr[i] : 0u;
+  d = __reduce_max_sync(0xFFFFFFFFu, d);
+  if ((threadIdx.x & 31) == 0) atomicMax(out, d);
+}
+
+// The passes that take every seed to a final cell: clipping, geometry,
+// the FP64 fixes, and the caller-order outputs.
+struct Pipeline {
+  gbv_context* c;
+  cudaStream_t st;
+  uint32_t n;
+  bool fp32;
+  bool check_sr;
+  SortedSeeds S;
   ClipArgs cbase{};
-  cbase.S = S;
-  cbase.n_total = n;
-  cbase.k0 = o.k0;
   GeomArgs gbase{};
-  gbase.S = S;
-  for (int k = 0; k < 3; ++k) {
-    cbase.box[k] = gbase.box[k] = o.box_min[k];
-    cbase.box[3 + k] = gbase.box[3 + k] = o.box_max[k];
-  }
-  cbase.check_sr = o.check_sr ? 1 : 0;
-  cbase.status = gbase.status = status_s;
-  cbase.nclip = nclip;
-  gbase.nclip = nclip;
-  cbase.comb = gbase.comb = cb;
-  cbase.counters = c->counters;
-  gbase.vol = vol_s;
-  gbase.mg = mg_s;
-  gbase.nf = nf;
-  gbase.f_nbr = f_nbr;
-  gbase.f_area = f_area;
-  gbase.out_stride = n;
-
-  uint32_t* rs = c->buf<uint32_t>("cls_rs", n);
-  uint32_t* rr = c->buf<uint32_t>("cls_rr", n);
-  uint32_t* os = c->buf<uint32_t>("cls_os", n);
-  uint32_t* orw = c->buf<uint32_t>("cls_or", n);
-  uint32_t* ms = c->buf<uint32_t>("cls_ms", n);
-  uint32_t* mr = c->buf<uint32_t>("cls_mr", n);
+  int32_t* status_s;
+  double* vol_s;
+  double* mg_s;
+  uint32_t* nf;
+  uint32_t* nclip;
+  uint32_t* f_nbr;
+  double* f_area;
+  uint32_t *rs, *rr, *os, *orw, *ms, *mr, *mk_s, *mk_r;
   uint32_t n_recheck = 0, n_over = 0, n_morek = 0;
+  // certification (Laguerre mode)
+  const double* node_wmax = nullptr;
+  uint32_t* extra = nullptr;
+  uint32_t* extra_cnt = nullptr;
+  uint32_t max_extra = 32;
+  // cells beyond the large shape
+  uint32_t n_huge = 0;
+  uint32_t** hp_nbr = nullptr;
+  double** hp_area = nullptr;
+  int huge_chunks = 0;
 
-  auto classify = [&](const uint32_t* ql, const uint32_t* qr, uint32_t nq, uint32_t out[4]) {
+  Pipeline(gbv_context* ctx, uint32_t n_, const double* box_min, const double* box_max,
+           bool fp32_, bool check_sr_, uint32_t k0, cudaStream_t st_)
+      : c(ctx), st(st_), n(n_), fp32(fp32_), check_sr(check_sr_) {
+    S = c->S;
+    status_s = c->buf<int32_t>("status_s", n);
+    vol_s = c->buf<double>("vol_s", n);
+    mg_s = c->buf<double>("mg_s", 3 * (size_t)n);
+    nf = c->buf<uint32_t>("nf", n);
+    nclip = c->buf<uint32_t>("nclip", n);
+    f_nbr = c->buf<uint32_t>("f_nbr", (size_t)kMaxFacets * n);
+    f_area = c->buf<double>("f_area", (size_t)kMaxFacets * n);
+    CombBuf cb;
+    cb.tv = c->buf<uint32_t>("cb_tv", (size_t)kTMax * n);
+    cb.ta = c->buf<uint32_t>("cb_ta", (size_t)kTMax * n);
+    cb.key = c->buf<int16_t>("cb_key", (size_t)kTMax * n);
+    cb.pown = c->buf<uint32_t>("cb_pown", (size_t)kPMax * n);
+    cb.prank = c->buf<uint16_t>("cb_prank", (size_t)kPMax * n);
+    cb.tmask = c->buf<ulonglong2>("cb_tmask", n);
+    cb.pmask = c->buf<uint64_t>("cb_pmask", n);
+    cb.flags = c->buf<uint32_t>("cb_flags", n);
+    cbase.S = S;
+    cbase.n_total = n;
+    cbase.k0 = k0;
+    gbase.S = S;
+    for (int k = 0; k < 3; ++k) {
+      cbase.box[k] = gbase.box[k] = box_min[k];
+      cbase.box[3 + k] = gbase.box[3 + k] = box_max[k];
+    }
+    cbase.check_sr = check_sr ? 1 : 0;
+    cbase.status = gbase.status = status_s;
+    cbase.nclip = nclip;
+    gbase.nclip = nclip;
+    cbase.comb = gbase.comb = cb;
+    cbase.counters = c->counters;
+    gbase.vol = vol_s;
+    gbase.mg = mg_s;
+    gbase.nf = nf;
+    gbase.f_nbr = f_nbr;
+    gbase.f_area = f_area;
+    gbase.out_stride = n;
+    rs = c->buf<uint32_t>("cls_rs", n);
+    rr = c->buf<uint32_t>("cls_rr", n);
+    os = c->buf<uint32_t>("cls_os", n);
+    orw = c->buf<uint32_t>("cls_or", n);
+    ms = c->buf<uint32_t>("cls_ms", n);
+    mr = c->buf<uint32_t>("cls_mr", n);
+    mk_s = c->buf<uint32_t>("mk_s", n);
+    mk_r = c->buf<uint32_t>("mk_r", n);
+    GBV_CUDA(cudaMemsetAsync(c->counters, 0, 2 * sizeof(unsigned long long), st));
+  }
+
+  void enable_certification(const double* wmax) { node_wmax = wmax; }
+
+  // Room for up to `per_row` extra candidates of each of `rows` list rows.
+  void size_extras(uint32_t per_row, uint32_t rows) {
+    max_extra = per_row;
+    extra = c->buf<uint32_t>("cert_extra", (size_t)per_row * rows);
+    extra_cnt = c->buf<uint32_t>("cert_extra_cnt", rows);
+    GBV_CUDA(cudaMemsetAsync(extra_cnt, 0, sizeof(uint32_t) * rows, st));
+  }
+
+  void classify(const uint32_t* ql, const uint32_t* qr, uint32_t nq, uint32_t out[4]) {
     GBV_CUDA(cudaMemsetAsync(c->list_counts, 0, 4 * sizeof(uint32_t), st));
     classify_kernel<<<nblocks(nq, 256), 256, 0, st>>>(ql, qr, nq, status_s, c->list_counts, rs,
                                                       rr, os, orw, ms, mr); count_launch();
@@ -415,10 +514,11 @@ static void cells_device(gbv_context* c, const double* d_xyz, const double* d_w,
       throw StatusError{GBV_ERR_STATE, "inconsistent polytope in " + std::to_string(out[3]) +
                                            " cell(s) (conflict zone not a disk)"};
     }
-  };
+  }
+
   // clip + geometry of a set of cells with the given lists
-  auto run = [&](const ListSet& L, const uint32_t* ql, const uint32_t* qr, uint32_t nq,
-                 int kind /* 0: mode, 1: FP64 small, 2: FP64 large */) {
+  // (kind 0: the pipeline's precision, 1: FP64 small, 2: FP64 large)
+  void run(const ListSet& L, const uint32_t* ql, const uint32_t* qr, uint32_t nq, int kind) {
     ClipArgs a = cbase;
     a.nbr = L.lists;
     a.nbr_stride = L.stride;
@@ -437,17 +537,75 @@ static void cells_device(gbv_context* c, const double* d_xyz, const double* d_w,
     g.qlist = ql;
     g.qrow = qr;
     g.nq = nq;
-    g.verify_sr = (f32 && o.check_sr) ? 1 : 0;
+    g.verify_sr = (f32 && check_sr) ? 1 : 0;
     g.shape = kind == 2 ? CLIP_LARGE : CLIP_SMALL;
+    if (node_wmax) {
+      g.node_wmax = node_wmax;
+      g.cand_cnt = L.cnt;
+      g.extra = extra;
+      g.extra_cnt = extra_cnt;
+      g.max_extra = max_extra;
+    }
     launch_geometry(g, st);
     GBV_CUDA(last_launch_error);
-  };
-  // runs a pass and its FP64 fixes; returns the cells that still need a
-  // longer list (slots in mk_s, rows of L in mk_r)
-  uint32_t* mk_s = c->buf<uint32_t>("mk_s", n);
-  uint32_t* mk_r = c->buf<uint32_t>("mk_r", n);
-  auto process = [&](const ListSet& L, const uint32_t* ql, const uint32_t* qr,
-                     uint32_t nq) -> uint32_t {
+  }
+
+  // Cells beyond the large shape (slots hs, rows hr of L), in chunks.
+  void run_huge(const ListSet& L, const uint32_t* hs, const uint32_t* hr, uint32_t m) {
+    if (!hp_nbr) {
+      hp_nbr = c->buf<uint32_t*>("huge_hp_nbr", n);
+      hp_area = c->buf<double*>("huge_hp_area", n);
+    }
+    constexpr uint32_t kChunk = 1024;
+    const size_t cap = std::min<uint32_t>(m, kChunk);
+    for (uint32_t off = 0; off < m; off += kChunk) {
+      const uint32_t cm = std::min<uint32_t>(kChunk, m - off);
+      HugeArgs h{};
+      h.S = S;
+      h.nbr = L.lists;
+      h.nbr_stride = L.stride;
+      h.nbr_cnt = L.cnt;
+      h.list_k = L.k;
+      h.n_total = n;
+      h.k0 = cbase.k0;
+      h.qlist = hs + off;
+      h.qrow = hr ? hr + off : nullptr;
+      h.nq = cm;
+      for (int k = 0; k < 6; ++k) h.box[k] = cbase.box[k];
+      h.check_sr = cbase.check_sr;
+      h.status = status_s;
+      h.nclip = nclip;
+      h.counters = c->counters;
+      h.scr_t = c->buf<ushort4>("huge_t", cap * kHugeT);
+      h.scr_adj = c->buf<ushort4>("huge_adj", cap * kHugeT);
+      h.scr_cor = c->buf<double4>("huge_cor", cap * kHugeT);
+      h.scr_pl = c->buf<double4>("huge_pl", cap * kHugeV);
+      h.scr_vg = c->buf<uint32_t>("huge_vg", cap * kHugeV);
+      h.scr_v2t = c->buf<uint16_t>("huge_v2t", cap * kHugeV);
+      h.scr_v2e = c->buf<uint8_t>("huge_v2e", cap * kHugeV);
+      h.vol = vol_s;
+      h.mg = mg_s;
+      h.nf = nf;
+      h.out_stride = n;
+      const std::string tag = std::to_string(huge_chunks++);
+      h.fac_nbr = c->buf<uint32_t>("huge_fn" + tag, (size_t)cm * kHugeV);
+      h.fac_area = c->buf<double>("huge_fa" + tag, (size_t)cm * kHugeV);
+      h.hp_nbr = hp_nbr;
+      h.hp_area = hp_area;
+      if (node_wmax) {
+        h.node_wmax = node_wmax;
+        h.extra = extra;
+        h.extra_cnt = extra_cnt;
+        h.max_extra = max_extra;
+      }
+      launch_huge(h, st);
+      GBV_CUDA(last_launch_error);
+    }
+  }
+
+  // A pass and its FP64 fixes; returns the cells that still need a longer
+  // list (slots in mk_s, rows of L in mk_r).
+  uint32_t process(const ListSet& L, const uint32_t* ql, const uint32_t* qr, uint32_t nq) {
     uint32_t* rc_s = c->buf<uint32_t>("rc_s", n);
     uint32_t* rc_r = c->buf<uint32_t>("rc_r", n);
     uint32_t* ov_s = c->buf<uint32_t>("ov_s", n);
@@ -483,18 +641,143 @@ static void cells_device(gbv_context* c, const double* d_xyz, const double* d_w,
       run(L, ov_s, ov_r, nov, 2);
       uint32_t c3[4];
       classify(ov_s, ov_r, nov, c3);
-      if (c3[0] || c3[1]) {
-        throw StatusError{GBV_ERR_CAPACITY, std::to_string(c3[1]) +
-                                                " cell(s) exceed the large capacity (" +
-                                                std::to_string(kLargeT) + " corners, " +
-                                                std::to_string(kLargeP) + " planes)"};
-      }
+      if (c3[0]) throw StatusError{GBV_ERR_STATE, "FP64 clipping asked for a recheck"};
       append(mk_s, nmk, ms, c3[2]);
       append(mk_r, nmk, mr, c3[2]);
       nmk += c3[2];
+      if (c3[1]) {
+        const uint32_t nh = c3[1];
+        uint32_t* hg_s = c->buf<uint32_t>("hg_s", n);
+        uint32_t* hg_r = c->buf<uint32_t>("hg_r", n);
+        append(hg_s, 0, os, nh);
+        append(hg_r, 0, orw, nh);
+        n_huge += nh;
+        run_huge(L, hg_s, hg_r, nh);
+        uint32_t c4[4];
+        classify(hg_s, hg_r, nh, c4);
+        if (c4[0] || c4[1]) {
+          throw StatusError{GBV_ERR_CAPACITY, std::to_string(c4[1]) + " cell(s) exceed " +
+                                                  std::to_string(kHugeT) + " corners or " +
+                                                  std::to_string(kHugeV) + " planes"};
+        }
+        append(mk_s, nmk, ms, c4[2]);
+        append(mk_r, nmk, mr, c4[2]);
+        nmk += c4[2];
+      }
     }
     return nmk;
-  };
+  }
+
+  // Caller-order results and CSR into the context.
+  void finish() {
+    c->vol = c->buf<double>("vol", n);
+    c->mg = c->buf<double>("mg", 3 * (size_t)n);
+    c->status = c->buf<int32_t>("status", n);
+    c->rowptr = c->buf<uint32_t>("rowptr", (size_t)n + 1);
+    facet_count_kernel<<<nblocks((size_t)n + 1, 256), 256, 0, st>>>(S.slot_of, nf, n, c->rowptr); count_launch();
+    uint32_t* stmp = c->buf<uint32_t>("csr_scan_tmp", scan_tmp_elems((size_t)n + 1));
+    exclusive_scan_u32(c->rowptr, (size_t)n + 1, stmp, st);
+    GBV_CUDA(cudaMemcpyAsync(&c->h_counts[0], c->rowptr + n, 4, cudaMemcpyDeviceToHost, st));
+    GBV_CUDA(cudaStreamSynchronize(st));
+    const uint32_t nnz32 = c->h_counts[0];
+    c->nnz = nnz32;
+    c->nbr = c->buf<uint32_t>("nbr", std::max<uint32_t>(nnz32, 1));
+    c->area = c->buf<double>("area", std::max<uint32_t>(nnz32, 1));
+    unsort_kernel<<<nblocks(n, 256), 256, 0, st>>>(S.slot_of, n, vol_s, mg_s, status_s, nf,
+                                                   f_nbr, f_area, hp_nbr, hp_area, c->rowptr,
+                                                   c->vol, c->mg,
+                                                   c->status, c->nbr, c->area); count_launch();
+    c->n = n;
+    c->has_cells = true;
+  }
+
+  void report(gbv_cell_report* rep, uint32_t K, float t_grid, float t_knn, float t_clip,
+              float t_retry, float t_total) {
+    double* part = c->buf<double>("sum_part", 2 * 256);
+    double* out = c->buf<double>("sum_out", 1);
+    sum_partial_kernel<<<256, kSumThreads, 0, st>>>(c->vol, n, part); count_launch();
+    sum_final_kernel<<<1, 32, 0, st>>>(part, 256, out); count_launch();
+    unsigned long long* clips = c->buf<unsigned long long>("clip_sum", 1);
+    GBV_CUDA(cudaMemsetAsync(clips, 0, 8, st));
+    sum_u32_kernel<<<256, 256, 0, st>>>(nclip, n, clips); count_launch();
+    double vs = 0;
+    unsigned long long cs = 0, hc[2] = {0, 0};
+    GBV_CUDA(cudaMemcpyAsync(&vs, out, 8, cudaMemcpyDeviceToHost, st));
+    GBV_CUDA(cudaMemcpyAsync(&cs, clips, 8, cudaMemcpyDeviceToHost, st));
+    GBV_CUDA(cudaMemcpyAsync(hc, c->counters, 16, cudaMemcpyDeviceToHost, st));
+    GBV_CUDA(cudaStreamSynchronize(st));
+    rep->nnz = c->nnz;
+    rep->n_cells = n;
+    rep->n_recheck_fp64 = n_recheck;
+    rep->n_more_k = n_morek;
+    rep->n_overflow = n_over;
+    rep->max_clips = (uint32_t)hc[1];
+    rep->knn_k = K;
+    rep->mean_clips = (double)cs / n;
+    rep->volume_sum = vs;
+    rep->n_exact = hc[0];
+    rep->ms_grid = t_grid;
+    rep->ms_knn = t_knn;
+    rep->ms_clip = t_clip;
+    rep->ms_retry = t_retry;
+    rep->ms_total = t_total;
+    rep->n_huge = n_huge;
+    rep->reserved = 0;
+  }
+};
+
+static float elapsed(cudaEvent_t a, cudaEvent_t b) {
+  float t = 0.f;
+  GBV_CUDA(cudaEventElapsedTime(&t, a, b));
+  return t;
+}
+
+// The whole cell computation on device inputs (the reference's
+// security-radius semantics).
+static void cells_device(gbv_context* c, const double* d_xyz, const double* d_w, uint32_t n,
+                         const gbv_cell_options& o, cudaStream_t st, gbv_cell_report* rep) {
+  if (n == 0) throw StatusError{GBV_ERR_INVALID_ARGUMENT, "n must be > 0"};
+  setup_seeds(c, n, d_w != nullptr);
+  c->nn_ready = false;
+  SortedSeeds& S = c->S;
+  GBV_CUDA(cudaEventRecord(c->ev[0], st));
+  build_grid(d_xyz, 3, 3, d_w, n, S.L, S, c->scr, st);
+  GBV_CUDA(cudaEventRecord(c->ev[1], st));
+  Pipeline P(c, n, o.box_min, o.box_max, o.precision == GBV_PRECISION_FP32_RECHECK,
+             o.check_sr != 0, o.k0, st);
+  uint32_t* flag_count = c->buf<uint32_t>("knn_flag_count", 1);
+  uint32_t* flag_list = c->buf<uint32_t>("knn_flag_list", n);
+
+  // first lists
+  const uint32_t nm1 = n > 1 ? n - 1 : 0;
+  const uint32_t K = o.check_sr ? std::min<uint32_t>(kKnnSmemK, nm1)
+                                : std::min<uint32_t>(o.k0, nm1);
+  uint32_t* knn = c->buf<uint32_t>("knn", (size_t)std::max<uint32_t>(K, 1) * n);
+  uint32_t* kcnt = c->buf<uint32_t>("kcnt", n);
+  double* klast_d = c->buf<double>("klast_d", n);
+  uint32_t* klast_i = c->buf<uint32_t>("klast_i", n);
+  {
+    KnnArgs ka{};
+    ka.S = &S;
+    ka.nq = n;
+    ka.k = K;
+    ka.mode = KNN_CELLS;
+    ka.nbr = knn;
+    ka.out_stride = n;
+    ka.cnt = kcnt;
+    ka.last_d2 = klast_d;
+    ka.last_idx = klast_i;
+    ka.flag_count = flag_count;
+    ka.flag_list = flag_list;
+    if (K > kKnnSmemK) {  // only without the security radius
+      ka.gl_d2 = c->buf<double>("knn_gd2", (size_t)K * n);
+      ka.gl_slot = c->buf<uint32_t>("knn_gslot", (size_t)K * n);
+    }
+    if (K > 0) launch_knn(ka, st);
+    else GBV_CUDA(cudaMemsetAsync(kcnt, 0, sizeof(uint32_t) * n, st));
+    GBV_CUDA(cudaGetLastError());
+  }
+  GBV_CUDA(cudaEventRecord(c->ev[2], st));
 
   ListSet L0;
   L0.lists = knn;
@@ -503,20 +786,20 @@ static void cells_device(gbv_context* c, const double* d_xyz, const double* d_w,
   L0.k = K;
   L0.last_d2 = klast_d;
   L0.last_idx = klast_i;
-  uint32_t morek = process(L0, nullptr, nullptr, n);
+  uint32_t morek = P.process(L0, nullptr, nullptr, n);
   GBV_CUDA(cudaEventRecord(c->ev[5], st));
   ListSet cur = L0;
   int round = 0;
   while (morek > 0) {
-    n_morek += morek;
+    P.n_morek += morek;
     if (cur.k >= nm1) throw StatusError{GBV_ERR_STATE, "list growth did not terminate"};
     const uint32_t batch = std::min<uint32_t>(kKnnSmemK, nm1 - cur.k);
     const uint32_t newk = cur.k + batch;
     const std::string tag = std::to_string(round & 1);
     uint32_t* q_s = c->buf<uint32_t>("ext_s" + tag, morek);
     uint32_t* q_r = c->buf<uint32_t>("ext_r" + tag, morek);
-    GBV_CUDA(cudaMemcpyAsync(q_s, mk_s, morek * 4, cudaMemcpyDeviceToDevice, st));
-    GBV_CUDA(cudaMemcpyAsync(q_r, mk_r, morek * 4, cudaMemcpyDeviceToDevice, st));
+    GBV_CUDA(cudaMemcpyAsync(q_s, P.mk_s, morek * 4, cudaMemcpyDeviceToDevice, st));
+    GBV_CUDA(cudaMemcpyAsync(q_r, P.mk_r, morek * 4, cudaMemcpyDeviceToDevice, st));
     uint32_t* lists = c->buf<uint32_t>("ext_lists" + tag, (size_t)newk * morek);
     uint32_t* cnt = c->buf<uint32_t>("ext_cnt" + tag, morek);
     double* lo_d = c->buf<double>("ext_lo_d" + tag, morek);
@@ -551,72 +834,349 @@ static void cells_device(gbv_context* c, const double* d_xyz, const double* d_w,
     nx.k = newk;
     nx.last_d2 = last_d;
     nx.last_idx = last_i;
-    morek = process(nx, q_s, nullptr, morek);
+    morek = P.process(nx, q_s, nullptr, morek);
     cur = nx;
     ++round;
   }
   GBV_CUDA(cudaEventRecord(c->ev[3], st));
-
-  // unsort + CSR
-  c->vol = c->buf<double>("vol", n);
-  c->mg = c->buf<double>("mg", 3 * (size_t)n);
-  c->status = c->buf<int32_t>("status", n);
-  c->rowptr = c->buf<uint32_t>("rowptr", (size_t)n + 1);
-  facet_count_kernel<<<nblocks((size_t)n + 1, 256), 256, 0, st>>>(S.slot_of, nf, n, c->rowptr); count_launch();
-  uint32_t* stmp = c->buf<uint32_t>("csr_scan_tmp", scan_tmp_elems((size_t)n + 1));
-  exclusive_scan_u32(c->rowptr, (size_t)n + 1, stmp, st);
-  GBV_CUDA(cudaMemcpyAsync(&c->h_counts[0], c->rowptr + n, 4, cudaMemcpyDeviceToHost, st));
-  GBV_CUDA(cudaStreamSynchronize(st));
-  const uint32_t nnz32 = c->h_counts[0];
-  c->nnz = nnz32;
-  c->nbr = c->buf<uint32_t>("nbr", std::max<uint32_t>(nnz32, 1));
-  c->area = c->buf<double>("area", std::max<uint32_t>(nnz32, 1));
-  unsort_kernel<<<nblocks(n, 256), 256, 0, st>>>(S.slot_of, n, vol_s, mg_s, status_s, nf, f_nbr,
-                                                 f_area, c->rowptr, c->vol, c->mg, c->status,
-                                                 c->nbr, c->area); count_launch();
+  P.finish();
   GBV_CUDA(cudaEventRecord(c->ev[4], st));
-  c->n = n;
-  c->has_cells = true;
-
   if (rep) {
-    double* part = c->buf<double>("sum_part", 2 * 256);
-    double* out = c->buf<double>("sum_out", 1);
-    sum_partial_kernel<<<256, kSumThreads, 0, st>>>(c->vol, n, part); count_launch();
-    sum_final_kernel<<<1, 32, 0, st>>>(part, 256, out); count_launch();
-    unsigned long long* clips = c->buf<unsigned long long>("clip_sum", 1);
-    GBV_CUDA(cudaMemsetAsync(clips, 0, 8, st));
-    sum_u32_kernel<<<256, 256, 0, st>>>(nclip, n, clips); count_launch();
-    double vs = 0;
-    unsigned long long cs = 0, hc[2] = {0, 0};
-    GBV_CUDA(cudaMemcpyAsync(&vs, out, 8, cudaMemcpyDeviceToHost, st));
-    GBV_CUDA(cudaMemcpyAsync(&cs, clips, 8, cudaMemcpyDeviceToHost, st));
-    GBV_CUDA(cudaMemcpyAsync(hc, c->counters, 16, cudaMemcpyDeviceToHost, st));
-    GBV_CUDA(cudaStreamSynchronize(st));
-    float t01 = 0, t12 = 0, t25 = 0, t53 = 0, t04 = 0;
-    GBV_CUDA(cudaEventElapsedTime(&t01, c->ev[0], c->ev[1]));
-    GBV_CUDA(cudaEventElapsedTime(&t12, c->ev[1], c->ev[2]));
-    GBV_CUDA(cudaEventElapsedTime(&t25, c->ev[2], c->ev[5]));
-    GBV_CUDA(cudaEventElapsedTime(&t53, c->ev[5], c->ev[3]));
-    GBV_CUDA(cudaEventElapsedTime(&t04, c->ev[0], c->ev[4]));
-    rep->nnz = c->nnz;
-    rep->n_cells = n;
-    rep->n_recheck_fp64 = n_recheck;
-    rep->n_more_k = n_morek;
-    rep->n_overflow = n_over;
-    rep->max_clips = (uint32_t)hc[1];
-    rep->knn_k = K;
-    rep->mean_clips = (double)cs / n;
-    rep->volume_sum = vs;
-    rep->n_exact = hc[0];
-    rep->ms_grid = t01;
-    rep->ms_knn = t12;
-    rep->ms_clip = t25;
-    rep->ms_retry = t53;
-    rep->ms_total = t04;
+    GBV_CUDA(cudaEventSynchronize(c->ev[4]));
+    P.report(rep, K, elapsed(c->ev[0], c->ev[1]), elapsed(c->ev[1], c->ev[2]),
+             elapsed(c->ev[2], c->ev[5]), elapsed(c->ev[5], c->ev[3]),
+             elapsed(c->ev[0], c->ev[4]));
   } else {
     GBV_CUDA(cudaStreamSynchronize(st));
   }
   GBV_CUDA(cudaGetLastError());
+}
+
+// Laguerre cells certified by the cell-centred power range query (no
+// security radius): the path of the optimal-transport solver, whose weights
+// vary too much for the 4-d lift's radius to stop.  Candidates come from a
+// CSR adjacency in the caller's order (e.g. the previous Newton iterate's
+// cells) or, when none is given, from the kNN (lifted when weighted).
+static void laguerre_device(gbv_context* c, const double* d_xyz, const double* d_w, uint32_t n,
+                            const double* box_min, const double* box_max, bool fp32,
+                            const uint32_t* cand_rowptr, const uint32_t* cand_idx,
+                            cudaStream_t st, gbv_cell_report* rep) {
+  if (n < 2) throw StatusError{GBV_ERR_INVALID_ARGUMENT, "n must be >= 2"};
+  setup_seeds(c, n, d_w != nullptr);
+  c->nn_ready = false;
+  SortedSeeds& S = c->S;
+  GBV_CUDA(cudaEventRecord(c->ev[0], st));
+  build_grid(d_xyz, 3, 3, d_w, n, S.L, S, c->scr, st);
+  double* wmax = c->buf<double>("node_wmax", node_count(S.L));
+  build_node_wmax(S, wmax, st);
+  GBV_CUDA(cudaEventRecord(c->ev[1], st));
+  // no list cap for seeds with copies (the security-radius loop is not used)
+  Pipeline P(c, n, box_min, box_max, fp32, false, n, st);
+  P.enable_certification(wmax);
+  uint32_t K;
+  uint32_t* lists;
+  uint32_t* cnt = c->buf<uint32_t>("lag_cnt", n);
+  if (cand_rowptr) {
+    uint32_t* dmax = c->buf<uint32_t>("lag_maxdeg", 1);
+    GBV_CUDA(cudaMemsetAsync(dmax, 0, 4, st));
+    max_degree_kernel<<<nblocks(n, 256), 256, 0, st>>>(cand_rowptr, n, dmax); count_launch();
+    GBV_CUDA(cudaMemcpyAsync(&c->h_counts[0], dmax, 4, cudaMemcpyDeviceToHost, st));
+    GBV_CUDA(cudaStreamSynchronize(st));
+    K = std::max<uint32_t>(1, std::min<uint32_t>(c->h_counts[0], 96));
+    lists = c->buf<uint32_t>("lag_lists", (size_t)K * n);
+    csr_to_lists_kernel<<<nblocks(n, 256), 256, 0, st>>>(cand_rowptr, cand_idx, S.slot_of, n, K,
+                                                         lists, cnt); count_launch();
+  } else {
+    K = std::min<uint32_t>(32, n - 1);
+    lists = c->buf<uint32_t>("lag_lists", (size_t)K * n);
+    KnnArgs ka{};
+    ka.S = &S;
+    ka.nq = n;
+    ka.k = K;
+    ka.mode = KNN_CELLS;
+    ka.nbr = lists;
+    ka.out_stride = n;
+    ka.cnt = cnt;
+    ka.flag_count = c->buf<uint32_t>("knn_flag_count", 1);
+    ka.flag_list = c->buf<uint32_t>("knn_flag_list", n);
+    launch_knn(ka, st);
+  }
+  GBV_CUDA(cudaGetLastError());
+  GBV_CUDA(cudaEventRecord(c->ev[2], st));
+  ListSet cur;
+  cur.lists = lists;
+  cur.stride = n;
+  cur.cnt = cnt;
+  cur.k = K;
+  const uint32_t* ql = nullptr;
+  uint32_t nq = n;
+  uint32_t* ex_s = c->buf<uint32_t>("lag_ex_s", n);
+  uint32_t* ex_r = c->buf<uint32_t>("lag_ex_r", n);
+  uint32_t* ex_count = c->buf<uint32_t>("lag_ex_count", 1);
+  for (int round = 0;; ++round) {
+    // cells far from their final shape (e.g. next to dense clusters) may
+    // need hundreds of extra candidates: the room per cell doubles each round
+    P.size_extras(std::min<uint32_t>(32u << std::min(round, 6), kHugeV), cur.stride);
+    if (P.process(cur, ql, nullptr, nq) != 0)
+      throw StatusError{GBV_ERR_STATE, "unexpected list exhaustion in Laguerre mode"};
+    if (round == 0) GBV_CUDA(cudaEventRecord(c->ev[5], st));
+    GBV_CUDA(cudaMemsetAsync(ex_count, 0, 4, st));
+    collect_extra_kernel<<<nblocks(nq, 256), 256, 0, st>>>(ql, nq, P.extra_cnt, P.status_s,
+                                                           ex_count, ex_s, ex_r); count_launch();
+    GBV_CUDA(cudaMemcpyAsync(&c->h_counts[0], ex_count, 4, cudaMemcpyDeviceToHost, st));
+    GBV_CUDA(cudaStreamSynchronize(st));
+    const uint32_t m = c->h_counts[0];
+    if (m == 0) break;
+    P.n_morek += m;
+    if (round >= 24) throw StatusError{GBV_ERR_NOT_CONVERGED, "certification did not settle"};
+    const std::string tag = std::to_string(round & 1);
+    const uint32_t newk = cur.k + P.max_extra;
+    uint32_t* q_s = c->buf<uint32_t>("lag_q" + tag, m);
+    uint32_t* nl = c->buf<uint32_t>("lag_nl" + tag, (size_t)newk * m);
+    uint32_t* nc = c->buf<uint32_t>("lag_nc" + tag, m);
+    GBV_CUDA(cudaMemcpyAsync(q_s, ex_s, m * 4, cudaMemcpyDeviceToDevice, st));
+    append_extra_kernel<<<nblocks(m, 128), 128, 0, st>>>(ex_s, ex_r, m, cur.lists, cur.stride,
+                                                         cur.cnt, P.extra, P.extra_cnt,
+                                                         cur.stride, P.max_extra, S.xd, S.perm,
+                                                         nl, nc); count_launch();
+    cur.lists = nl;
+    cur.stride = m;
+    cur.cnt = nc;
+    cur.k = newk;
+    ql = q_s;
+    nq = m;
+  }
+  GBV_CUDA(cudaEventRecord(c->ev[3], st));
+  P.finish();
+  GBV_CUDA(cudaEventRecord(c->ev[4], st));
+  if (rep) {
+    GBV_CUDA(cudaEventSynchronize(c->ev[4]));
+    P.report(rep, K, elapsed(c->ev[0], c->ev[1]), elapsed(c->ev[1], c->ev[2]),
+             elapsed(c->ev[2], c->ev[5]), elapsed(c->ev[5], c->ev[3]),
+             elapsed(c->ev[0], c->ev[4]));
+  } else {
+    GBV_CUDA(cudaStreamSynchronize(st));
+  }
+  GBV_CUDA(cudaGetLastError());
+}
+
+// ---------------------------------------------------------------------
+// Semi-discrete optimal transport: damped Newton with FP64 PCG
+// ---------------------------------------------------------------------
+struct OtWork {
+  gbv_context* c;
+  cudaStream_t st;
+  uint32_t n;
+  double* part;      // device partials
+  std::vector<double> hpart;
+  explicit OtWork(gbv_context* ctx, uint32_t n_, cudaStream_t s) : c(ctx), st(s), n(n_) {
+    part = c->buf<double>("ot_part", 4 * kOtParts);
+    hpart.resize(4 * kOtParts);
+  }
+  // Neumaier sum of the (s, c) pairs of the first 2*kOtParts partials
+  double fetch_sum() {
+    GBV_CUDA(cudaMemcpyAsync(hpart.data(), part, sizeof(double) * 2 * kOtParts,
+                             cudaMemcpyDeviceToHost, st));
+    GBV_CUDA(cudaStreamSynchronize(st));
+    double S = 0.0, C = 0.0;
+    for (int b = 0; b < kOtParts; ++b) {
+      const double x = hpart[2 * b], t = S + x;
+      if (std::fabs(S) >= std::fabs(x)) C += (S - t) + x;
+      else C += (x - t) + S;
+      S = t;
+      C += hpart[2 * b + 1];
+    }
+    return S + C;
+  }
+  double dot(const double* a, const double* b) {
+    dot_parts(a, b, n, part, st);
+    return fetch_sum();
+  }
+  // residual r = vol - nu; returns ||r||^2, max |r_i|/nu_i, min vol
+  void residual_stats(const double* vol, const double* nu, double* r, double& r2, double& rel_inf,
+                      double& vmin) {
+    residual(vol, nu, n, r, part, st);
+    GBV_CUDA(cudaMemcpyAsync(hpart.data(), part, sizeof(double) * 4 * kOtParts,
+                             cudaMemcpyDeviceToHost, st));
+    GBV_CUDA(cudaStreamSynchronize(st));
+    double S = 0.0, C = 0.0;
+    rel_inf = 0.0;
+    vmin = DBL_MAX;
+    for (int b = 0; b < kOtParts; ++b) {
+      const double x = hpart[2 * b], t = S + x;
+      if (std::fabs(S) >= std::fabs(x)) C += (S - t) + x;
+      else C += (x - t) + S;
+      S = t;
+      C += hpart[2 * b + 1];
+      rel_inf = std::max(rel_inf, hpart[2 * kOtParts + b]);
+      vmin = std::min(vmin, hpart[3 * kOtParts + b]);
+    }
+    r2 = S + C;
+  }
+};
+
+__global__ void fill_kernel(double* __restrict__ y, double v, uint32_t n) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = v;
+}
+
+// Laguerre cells at weights w with the given candidates (CSR in caller
+// order, may be null); results in the context.
+static void ot_cells(gbv_context* c, const double* xyz, const double* w, uint32_t n,
+                     const gbv_ot_options& o, const uint32_t* cand_rp, const uint32_t* cand_ix,
+                     cudaStream_t st) {
+  laguerre_device(c, xyz, w, n, o.box_min, o.box_max, o.precision == GBV_PRECISION_FP32_RECHECK,
+                  cand_rp, cand_ix, st, nullptr);
+}
+
+// Saves the current cells' adjacency as the next call's candidates.
+static void save_adjacency(gbv_context* c, uint32_t n, cudaStream_t st, uint32_t** rp,
+                           uint32_t** ix) {
+  *rp = c->buf<uint32_t>("ot_adj_rp", (size_t)n + 1);
+  *ix = c->buf<uint32_t>("ot_adj_ix", std::max<uint64_t>(c->nnz, 1));
+  GBV_CUDA(cudaMemcpyAsync(*rp, c->rowptr, sizeof(uint32_t) * ((size_t)n + 1),
+                           cudaMemcpyDeviceToDevice, st));
+  if (c->nnz)
+    GBV_CUDA(cudaMemcpyAsync(*ix, c->nbr, sizeof(uint32_t) * c->nnz, cudaMemcpyDeviceToDevice, st));
+}
+
+// Hessian of the current cells, in buffers of the context.
+static Hessian current_hessian(gbv_context* c, const double* xyz, uint32_t n, cudaStream_t st) {
+  Hessian H;
+  uint32_t* rp = c->buf<uint32_t>("ot_h_rp", (size_t)n + 1);
+  uint32_t* col = c->buf<uint32_t>("ot_h_col", std::max<uint64_t>(c->nnz, 1));
+  GBV_CUDA(cudaMemcpyAsync(rp, c->rowptr, sizeof(uint32_t) * ((size_t)n + 1),
+                           cudaMemcpyDeviceToDevice, st));
+  if (c->nnz)
+    GBV_CUDA(cudaMemcpyAsync(col, c->nbr, sizeof(uint32_t) * c->nnz, cudaMemcpyDeviceToDevice, st));
+  H.val = c->buf<double>("ot_h_val", std::max<uint64_t>(c->nnz, 1));
+  H.diag = c->buf<double>("ot_h_diag", n);
+  assemble_hessian(xyz, rp, col, c->area, n, H, st);
+  return H;
+}
+
+static void ot_solve(gbv_context* c, const double* xyz, const double* nu_in, uint32_t n,
+                     const gbv_ot_options& o, double* w, cudaStream_t st, gbv_ot_report* rep) {
+  if (n < 2) throw StatusError{GBV_ERR_INVALID_ARGUMENT, "n must be >= 2"};
+  const auto t0 = std::chrono::steady_clock::now();
+  double ms_cells = 0.0, ms_lin = 0.0;
+  auto now_ms = [&](std::chrono::steady_clock::time_point a) {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - a).count();
+  };
+  OtWork W(c, n, st);
+  const double boxvol = (o.box_max[0] - o.box_min[0]) * (o.box_max[1] - o.box_min[1]) *
+                        (o.box_max[2] - o.box_min[2]);
+  double* nu = c->buf<double>("ot_nu", n);
+  if (nu_in) {
+    GBV_CUDA(cudaMemcpyAsync(nu, nu_in, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+  } else {
+    fill_kernel<<<nblocks(n, 256), 256, 0, st>>>(nu, boxvol / n, n); count_launch();
+  }
+  double* r = c->buf<double>("ot_r", n);
+  double* x = c->buf<double>("ot_x", n);
+  double* rr = c->buf<double>("ot_cg_r", n);
+  double* p = c->buf<double>("ot_cg_p", n);
+  double* Ap = c->buf<double>("ot_cg_ap", n);
+  double* z = c->buf<double>("ot_cg_z", n);
+  double* ones = c->buf<double>("ot_ones", n);
+  double* wt = c->buf<double>("ot_wt", n);
+  fill_kernel<<<nblocks(n, 256), 256, 0, st>>>(ones, 1.0, n); count_launch();
+  const double nu_norm = std::sqrt(W.dot(nu, nu));
+
+  uint32_t *adj_rp = nullptr, *adj_ix = nullptr;
+  uint32_t cell_calls = 0, cg_total = 0, halvings = 0, it = 0;
+  auto cells = [&](const double* ww, bool with_adj) {
+    const auto tc = std::chrono::steady_clock::now();
+    ot_cells(c, xyz, ww, n, o, with_adj ? adj_rp : nullptr, with_adj ? adj_ix : nullptr, st);
+    ++cell_calls;
+    ms_cells += now_ms(tc);
+  };
+  cells(w, false);
+  double r2, rel_inf, vmin;
+  W.residual_stats(c->vol, nu, r, r2, rel_inf, vmin);
+  double nu_min = DBL_MAX;
+  {
+    // min nu through the residual of ones * nu: reuse the min-vol slot
+    double a, b2, m;
+    W.residual_stats(nu, ones, Ap, a, b2, m);
+    nu_min = m;
+  }
+  const double eps0 = 0.5 * std::min(nu_min, vmin);
+  bool converged = rel_inf < o.tol;
+  for (it = 0; it < o.max_newton && !converged; ++it) {
+    save_adjacency(c, n, st, &adj_rp, &adj_ix);
+    const auto tl = std::chrono::steady_clock::now();
+    Hessian H = current_hessian(c, xyz, n, st);
+    // b = -(vol - nu), projected on mean zero (H has the constants as kernel)
+    scale_copy(rr, r, -1.0, n, st);
+    const double mean = W.dot(rr, ones) / n;
+    add_scalar(rr, -mean, n, st);
+    const double bnorm = std::sqrt(W.dot(rr, rr));
+    const double eta = o.cg_rtol > 0.0 ? o.cg_rtol : 1e-3;
+    GBV_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, st));
+    cg_precond(rr, H.diag, z, n, st);
+    GBV_CUDA(cudaMemcpyAsync(p, z, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+    double rz = W.dot(rr, z);
+    for (uint32_t k = 0; k < o.max_cg; ++k) {
+      spmv_dot(H, p, Ap, W.part, kOtParts, st);
+      const double pAp = W.fetch_sum();
+      if (!(pAp > 0.0)) break;
+      const double alpha = rz / pAp;
+      cg_update_xr(x, rr, p, Ap, alpha, n, st);
+      ++cg_total;
+      const double rnorm = std::sqrt(W.dot(rr, rr));
+      if (rnorm <= eta * bnorm) break;
+      cg_precond(rr, H.diag, z, n, st);
+      const double rz_new = W.dot(rr, z);
+      cg_update_p(p, z, rz_new / rz, n, st);
+      rz = rz_new;
+    }
+    const double xmean = W.dot(x, ones) / n;
+    add_scalar(x, -xmean, n, st);
+    ms_lin += now_ms(tl);
+    // damped step (Kitagawa-Merigot-Thibert): halve until every cell keeps
+    // at least eps0 and the residual drops by (1 - alpha / 2)
+    double alpha = 1.0;
+    bool accepted = false;
+    for (int h = 0; h < 30; ++h) {
+      GBV_CUDA(cudaMemcpyAsync(wt, w, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+      axpy(wt, x, alpha, n, st);
+      cells(wt, true);
+      double r2t, relt, vmint;
+      W.residual_stats(c->vol, nu, r, r2t, relt, vmint);
+      if (vmint >= eps0 && std::sqrt(r2t) <= (1.0 - 0.5 * alpha) * std::sqrt(r2)) {
+        GBV_CUDA(cudaMemcpyAsync(w, wt, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+        r2 = r2t;
+        rel_inf = relt;
+        vmin = vmint;
+        accepted = true;
+        break;
+      }
+      alpha *= 0.5;
+      ++halvings;
+    }
+    if (!accepted) {
+      // restore the cells of the current weights and stop
+      cells(w, true);
+      W.residual_stats(c->vol, nu, r, r2, rel_inf, vmin);
+      break;
+    }
+    converged = rel_inf < o.tol;
+  }
+  GBV_CUDA(cudaStreamSynchronize(st));
+  if (rep) {
+    rep->converged = converged ? 1 : 0;
+    rep->newton_iters = it;
+    rep->cg_iters = cg_total;
+    rep->halvings = halvings;
+    rep->cell_calls = cell_calls;
+    rep->mass_error_inf = rel_inf;
+    rep->mass_error_l2 = std::sqrt(r2) / nu_norm;
+    rep->min_volume = vmin;
+    rep->ms_total = now_ms(t0);
+    rep->ms_cells = ms_cells;
+    rep->ms_linear = ms_lin;
+  }
 }
 
 template <class F>
@@ -640,6 +1200,19 @@ static gbv_status check_opts(const gbv_cell_options* o) {
   for (int k = 0; k < 3; ++k)
     if (!(o->box_max[k] > o->box_min[k])) return fail(GBV_ERR_INVALID_ARGUMENT, "empty box");
   if (o->k0 == 0) return fail(GBV_ERR_INVALID_ARGUMENT, "k0 must be > 0");
+  if (o->certification != GBV_CERTIFY_SECURITY_RADIUS &&
+      o->certification != GBV_CERTIFY_POWER_RANGE)
+    return fail(GBV_ERR_INVALID_ARGUMENT, "unknown certification");
+  return GBV_OK;
+}
+
+static gbv_status check_ot_opts(const gbv_ot_options* o) {
+  if (!o) return fail(GBV_ERR_INVALID_ARGUMENT, "options is NULL");
+  if (o->precision != GBV_PRECISION_FP64 && o->precision != GBV_PRECISION_FP32_RECHECK)
+    return fail(GBV_ERR_INVALID_ARGUMENT, "unknown precision");
+  for (int k = 0; k < 3; ++k)
+    if (!(o->box_max[k] > o->box_min[k])) return fail(GBV_ERR_INVALID_ARGUMENT, "empty box");
+  if (!(o->tol > 0.0)) return fail(GBV_ERR_INVALID_ARGUMENT, "tol must be > 0");
   return GBV_OK;
 }
 
@@ -712,7 +1285,11 @@ gbv_status gbv_cells_compute_device(gbv_context* c, const double* d_xyz, const d
   return guarded([&] {
     GBV_CUDA(cudaSetDevice(c->device));
     cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
-    cells_device(c, d_xyz, d_w, n, *opt, st, report);
+    if (opt->certification == GBV_CERTIFY_POWER_RANGE)
+      laguerre_device(c, d_xyz, d_w, n, opt->box_min, opt->box_max,
+                      opt->precision == GBV_PRECISION_FP32_RECHECK, nullptr, nullptr, st, report);
+    else
+      cells_device(c, d_xyz, d_w, n, *opt, st, report);
   });
 }
 
@@ -727,7 +1304,12 @@ gbv_status gbv_cells_compute(gbv_context* c, const double* xyz, const double* w,
     double* dw = w ? c->buf<double>("in_w", n) : nullptr;
     GBV_CUDA(cudaMemcpyAsync(dx, xyz, 3 * sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
     if (w) GBV_CUDA(cudaMemcpyAsync(dw, w, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
-    cells_device(c, dx, dw, n, *opt, c->stream, report);
+    if (opt->certification == GBV_CERTIFY_POWER_RANGE)
+      laguerre_device(c, dx, dw, n, opt->box_min, opt->box_max,
+                      opt->precision == GBV_PRECISION_FP32_RECHECK, nullptr, nullptr, c->stream,
+                      report);
+    else
+      cells_device(c, dx, dw, n, *opt, c->stream, report);
   });
 }
 
@@ -885,6 +1467,92 @@ gbv_status gbv_nn_get_nearest_neighbors_all(gbv_context* c, uint32_t k, uint32_t
     if (d2) GBV_CUDA(cudaMemcpyAsync(d2, od, 8 * (size_t)n * k, cudaMemcpyDeviceToHost, st));
     GBV_CUDA(cudaStreamSynchronize(st));
     GBV_CUDA(cudaGetLastError());
+  });
+}
+
+void gbv_ot_options_default(gbv_ot_options* o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  for (int k = 0; k < 3; ++k) {
+    o->box_min[k] = 0.0;
+    o->box_max[k] = 1.0;
+  }
+  o->tol = 1e-6;
+  o->max_newton = 100;
+  o->max_cg = 4000;
+  o->precision = GBV_PRECISION_FP32_RECHECK;
+  o->cg_rtol = 1e-3;
+}
+
+gbv_status gbv_ot_solve_device(gbv_context* c, const double* d_xyz, const double* d_nu, uint32_t n,
+                               const gbv_ot_options* opt, double* d_w, void* stream,
+                               gbv_ot_report* report) {
+  if (!c || !d_xyz || !d_w) return fail(GBV_ERR_INVALID_ARGUMENT, "NULL argument");
+  gbv_status s = check_ot_opts(opt);
+  if (s != GBV_OK) return s;
+  return guarded([&] {
+    GBV_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    ot_solve(c, d_xyz, d_nu, n, *opt, d_w, st, report);
+  });
+}
+
+gbv_status gbv_ot_solve(gbv_context* c, const double* xyz, const double* nu, uint32_t n,
+                        const gbv_ot_options* opt, double* w, gbv_ot_report* report) {
+  if (!c || !xyz || !w) return fail(GBV_ERR_INVALID_ARGUMENT, "NULL argument");
+  gbv_status s = check_ot_opts(opt);
+  if (s != GBV_OK) return s;
+  return guarded([&] {
+    GBV_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = c->stream;
+    double* dx = c->buf<double>("ot_in_xyz", 3 * (size_t)n);
+    double* dw = c->buf<double>("ot_in_w", n);
+    double* dnu = nu ? c->buf<double>("ot_in_nu", n) : nullptr;
+    GBV_CUDA(cudaMemcpyAsync(dx, xyz, 24 * (size_t)n, cudaMemcpyHostToDevice, st));
+    GBV_CUDA(cudaMemcpyAsync(dw, w, 8 * (size_t)n, cudaMemcpyHostToDevice, st));
+    if (nu) GBV_CUDA(cudaMemcpyAsync(dnu, nu, 8 * (size_t)n, cudaMemcpyHostToDevice, st));
+    ot_solve(c, dx, dnu, n, *opt, dw, st, report);
+    GBV_CUDA(cudaMemcpyAsync(w, dw, 8 * (size_t)n, cudaMemcpyDeviceToHost, st));
+    GBV_CUDA(cudaStreamSynchronize(st));
+  });
+}
+
+gbv_status gbv_ot_gradient_hessian(gbv_context* c, const double* xyz, const double* w,
+                                   const double* nu, uint32_t n, const gbv_ot_options* opt,
+                                   double* g, uint32_t* h_rowptr, uint32_t* h_col, double* h_val,
+                                   double* h_diag, uint64_t h_capacity, uint64_t* nnz) {
+  if (!c || !xyz || !w) return fail(GBV_ERR_INVALID_ARGUMENT, "NULL argument");
+  gbv_status s = check_ot_opts(opt);
+  if (s != GBV_OK) return s;
+  return guarded([&] {
+    GBV_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = c->stream;
+    double* dx = c->buf<double>("ot_in_xyz", 3 * (size_t)n);
+    double* dw = c->buf<double>("ot_in_w", n);
+    double* dnu = c->buf<double>("ot_in_nu", n);
+    GBV_CUDA(cudaMemcpyAsync(dx, xyz, 24 * (size_t)n, cudaMemcpyHostToDevice, st));
+    GBV_CUDA(cudaMemcpyAsync(dw, w, 8 * (size_t)n, cudaMemcpyHostToDevice, st));
+    const double boxvol = (opt->box_max[0] - opt->box_min[0]) * (opt->box_max[1] - opt->box_min[1]) *
+                          (opt->box_max[2] - opt->box_min[2]);
+    if (nu) GBV_CUDA(cudaMemcpyAsync(dnu, nu, 8 * (size_t)n, cudaMemcpyHostToDevice, st));
+    else { fill_kernel<<<nblocks(n, 256), 256, 0, st>>>(dnu, boxvol / n, n); count_launch(); }
+    ot_cells(c, dx, dw, n, *opt, nullptr, nullptr, st);
+    if (nnz) *nnz = c->nnz;
+    if (g) {
+      double* dg = c->buf<double>("ot_grad", n);
+      residual(c->vol, dnu, n, dg, c->buf<double>("ot_part", 4 * kOtParts), st);
+      scale_copy(dg, dg, -1.0, n, st);  // g = nu - vol
+      GBV_CUDA(cudaMemcpyAsync(g, dg, 8 * (size_t)n, cudaMemcpyDeviceToHost, st));
+    }
+    if (h_capacity > 0) {
+      if (h_capacity < c->nnz) throw StatusError{GBV_ERR_CAPACITY, "Hessian capacity too small"};
+      Hessian H = current_hessian(c, dx, n, st);
+      if (h_rowptr) GBV_CUDA(cudaMemcpyAsync(h_rowptr, H.rowptr, 4 * ((size_t)n + 1), cudaMemcpyDeviceToHost, st));
+      if (h_col) GBV_CUDA(cudaMemcpyAsync(h_col, H.col, 4 * c->nnz, cudaMemcpyDeviceToHost, st));
+      if (h_val) GBV_CUDA(cudaMemcpyAsync(h_val, H.val, 8 * c->nnz, cudaMemcpyDeviceToHost, st));
+      if (h_diag) GBV_CUDA(cudaMemcpyAsync(h_diag, H.diag, 8 * (size_t)n, cudaMemcpyDeviceToHost, st));
+    }
+    GBV_CUDA(cudaStreamSynchronize(st));
   });
 }
 

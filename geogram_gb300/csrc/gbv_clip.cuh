@@ -78,10 +78,70 @@ struct GeomArgs {
   uint32_t* f_nbr;            // [kMaxFacets][n] original index
   double* f_area;             // [kMaxFacets][n]
   uint32_t out_stride;
+  // Cell-centred certification (off when node_wmax is null): every seed
+  // that could still cut the cell and is not in its candidate list is
+  // written to extra[k * nbr_stride + row], k < max_extra (row: the cell's
+  // list row), and counted in extra_cnt[row] (bit 31: more were found than
+  // fit).
+  const double* node_wmax;
+  const uint32_t* cand_cnt;   // candidate list lengths, per list row
+  uint32_t* extra;
+  uint32_t* extra_cnt;
+  uint32_t max_extra;
 };
 
 // FP64 geometry of the final cells, one warp per cell, with the reference's
 // formulas and summation order.
 void launch_geometry(const GeomArgs& a, cudaStream_t st);
+
+// Cells beyond the large shape: one thread per cell, polytope in global
+// memory (kHugeT corners, kHugeV planes), clipping and geometry in one
+// kernel.  Their facets go to a separate area: nf[slot] carries
+// kHugeFacets and hp_nbr[slot] / hp_area[slot] point at the cell's
+// neighbours and areas.
+constexpr uint32_t kHugeT = 4096, kHugeV = 2048;
+constexpr uint32_t kHugeFacets = 0x80000000u;
+
+struct HugeArgs {
+  SortedSeeds S;
+  const uint32_t* nbr;
+  uint32_t nbr_stride;
+  const uint32_t* nbr_cnt;
+  uint32_t list_k;
+  uint32_t n_total;
+  uint32_t k0;
+  const uint32_t* qlist;      // sorted slots (required)
+  const uint32_t* qrow;       // list rows (nullptr: row = qi)
+  uint32_t nq;
+  double box[6];
+  int check_sr;
+  int32_t* status;
+  uint32_t* nclip;
+  unsigned long long* counters;
+  // scratch, per query: [nq][kHugeT] and [nq][kHugeV]
+  ushort4* scr_t;
+  ushort4* scr_adj;
+  double4* scr_cor;
+  double4* scr_pl;
+  uint32_t* scr_vg;
+  uint16_t* scr_v2t;
+  uint8_t* scr_v2e;
+  // outputs by sorted slot (as GeomArgs) and the facet area [nq][kHugeV]
+  double* vol;
+  double* mg;
+  uint32_t* nf;
+  uint32_t out_stride;
+  uint32_t* fac_nbr;
+  double* fac_area;
+  uint32_t** hp_nbr;
+  double** hp_area;
+  // certification (as GeomArgs; off when node_wmax is null)
+  const double* node_wmax;
+  uint32_t* extra;
+  uint32_t* extra_cnt;
+  uint32_t max_extra;
+};
+
+void launch_huge(const HugeArgs& a, cudaStream_t st);
 
 }  // namespace gbv

@@ -74,7 +74,7 @@ __device__ __forceinline__ int x_scale(int en, const double* e, double b, double
 // rows 0-1, 3x3 minors of rows 0-2 expanded along row 2, the 4x4
 // determinant expanded along row 3.  Kept out of line: it only runs when
 // the floating-point filter of the clipping kernel cannot decide.
-__device__ __noinline__ int det4_sign_exact(const double* r0, const double* r1,
+static __device__ __noinline__ int det4_sign_exact(const double* r0, const double* r1,
                                             const double* r2, const double* r3) {
   double m[6][4];
   int mn[6];

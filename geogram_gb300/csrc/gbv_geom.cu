@@ -43,7 +43,161 @@ struct GeomWarpSmem {
   uint8_t fan[3 * T];                    // fan sequences (triangles around planes)
   uint8_t order[P];                      // contributing planes in creation order
   uint8_t tlist[T];                      // used triangle slots, compacted
+  float4 cf[T];                          // corners (FP32) and their best power bound
+  uint32_t cbest[T];                     // best seed of each corner (certification)
+  uint32_t stk[96];                      // octree traversal stack
 };
+
+// Cell-centred certification.  A seed j cuts the cell only if for some
+// corner c its power pi_j(c) = |c - p_j|^2 - w_j is below the seed's own,
+// pi_i(c) = |c - p_i|^2 - w_i.  For every corner the warp looks for the
+// seed of least power at c among those below pi_i(c) and not yet in the
+// candidate list -- the seed whose Laguerre cell holds c, hence a neighbour
+// of the final cell -- and reports the distinct ones as extra candidates.
+// Clipping by them and certifying again ends in a few rounds; a round that
+// finds none certifies the cell.
+//
+// The octree walk is a best-bound search shared by the warp: a node whose
+// seeds all have w <= W_B cannot improve corner c when dist(c, box)^2 - W_B
+// >= best(c), and is skipped when that holds for every corner (each lane
+// tests its own corners).  Leaves are scanned one seed per lane against
+// every corner; each seed that improves a corner is then broadcast and the
+// corners' owners update their bounds.  best(c) starts at pi_i(c) plus an
+// FP32 margin, so a seed that may cut is never missed; a candidate that only
+// looks like a cutter within the margin is not reported.
+template <int T, int NCL>
+__device__ __forceinline__ void certify_cell(const GeomArgs& a, const SortedSeeds& S,
+                                             const GridDesc& gd, uint32_t s, uint32_t row,
+                                             int ntri, float4 (&mine)[NCL], float4* cf,
+                                             uint32_t* cbest, uint32_t* stk, int lane) {
+  const unsigned FULL = 0xFFFFFFFFu;
+  const float hf = gd.h_f;
+  const uint32_t ncand = a.cand_cnt[row] & kCntMask;
+  const double4 pi_d = S.xd[s];
+  uint32_t bj[NCL];
+#pragma unroll
+  for (int q = 0; q < NCL; ++q) {
+    bj[q] = kNone;
+    if (mine[q].w > -INFINITY) {
+      mine[q].w += 1e-5f * fabsf(mine[q].w) + 1e-7f;
+      cf[lane + 32 * q].w = mine[q].w;
+    }
+  }
+  bool overflow = false;
+  int sp = 0;
+  if (lane == 0) stk[0] = 0u;
+  sp = 1;
+  __syncwarp();
+  while (sp > 0) {
+    const uint32_t e = stk[sp - 1];
+    __syncwarp();
+    --sp;
+    const int lev = (int)(e & 15u);
+    const uint32_t code = e >> 4;
+    const int shift = gd.L - lev;
+    const uint32_t b = S.cell_start[code << (3 * shift)];
+    const uint32_t en = S.cell_start[(code + 1u) << (3 * shift)];
+    if (b == en) continue;
+    const float WB = (float)a.node_wmax[node_offset(lev) + code];
+    const float side = hf * (float)(1u << shift);
+    const float bx = gd.lo_f[0] + (float)compact3(code) * side;
+    const float by = gd.lo_f[1] + (float)compact3(code >> 1) * side;
+    const float bz = gd.lo_f[2] + (float)compact3(code >> 2) * side;
+    const float pad = 1e-6f * (1.f + fabsf(bx) + fabsf(by) + fabsf(bz)) + 1e-5f * side;
+    bool ok = true;
+#pragma unroll
+    for (int q = 0; q < NCL; ++q) {
+      const float4 c = mine[q];
+      if (!(c.w > -INFINITY)) continue;  // unused slot
+      const float dx = fmaxf(fmaxf(bx - pad - c.x, c.x - (bx + side + pad)), 0.f);
+      const float dy = fmaxf(fmaxf(by - pad - c.y, c.y - (by + side + pad)), 0.f);
+      const float dz = fmaxf(fmaxf(bz - pad - c.z, c.z - (bz + side + pad)), 0.f);
+      const float d2 = dx * dx + dy * dy + dz * dz;
+      const float need = (c.w + WB) + 1e-5f * (fabsf(c.w) + fabsf(WB) + d2) + 1e-7f;
+      ok = ok && (d2 >= need);
+    }
+    if (__all_sync(FULL, ok)) continue;
+    if (en - b <= 32u || lev == gd.L) {
+      for (uint32_t base = b; base < en; base += 32) {
+        const uint32_t j = base + lane;
+        bool cut = false;
+        float jx = 0.f, jy = 0.f, jz = 0.f, wj = 0.f;
+        if (j < en && j != s) {
+          const double4 pj = S.xd[j];
+          // a copy of the seed is no neighbour (delaunay_nn.cpp:126-133)
+          const bool same = pj.x == pi_d.x && pj.y == pi_d.y && pj.z == pi_d.z;
+          jx = (float)pj.x;
+          jy = (float)pj.y;
+          jz = (float)pj.z;
+          wj = S.ws ? (float)S.ws[j] : 0.f;
+          for (int k = 0; k < ntri && !cut && !same; ++k) {
+            const float4 c = cf[k];
+            const float dx = c.x - jx, dy = c.y - jy, dz = c.z - jz;
+            cut = dx * dx + dy * dy + dz * dz - wj < c.w;
+          }
+          if (cut) {
+            // already in the candidate list (clipped, cutting or not)?
+            for (uint32_t k = 0; k < ncand && cut; ++k)
+              if (a.nbr[(size_t)k * a.nbr_stride + row] == j) cut = false;
+          }
+        }
+        unsigned m = __ballot_sync(FULL, cut);
+        while (m) {
+          const int src = __ffs(m) - 1;
+          m &= m - 1;
+          const float sx = __shfl_sync(FULL, jx, src), sy = __shfl_sync(FULL, jy, src),
+                      sz = __shfl_sync(FULL, jz, src), sw = __shfl_sync(FULL, wj, src);
+          const uint32_t sj = __shfl_sync(FULL, j, src);
+#pragma unroll
+          for (int q = 0; q < NCL; ++q) {
+            if (!(mine[q].w > -INFINITY)) continue;
+            const float dx = mine[q].x - sx, dy = mine[q].y - sy, dz = mine[q].z - sz;
+            const float d = dx * dx + dy * dy + dz * dz - sw;
+            if (d < mine[q].w) {
+              mine[q].w = d;
+              bj[q] = sj;
+              cf[lane + 32 * q].w = d;
+            }
+          }
+        }
+        __syncwarp();
+      }
+      continue;
+    }
+    if (sp + 8 > 96) {
+      overflow = true;
+      break;
+    }
+    if (lane < 8) stk[sp + lane] = (((code << 3) | (uint32_t)lane) << 4) | (uint32_t)(lev + 1);
+    __syncwarp();
+    sp += 8;
+  }
+  // the distinct best seeds, in corner order
+#pragma unroll
+  for (int q = 0; q < NCL; ++q)
+    if (lane + 32 * q < T) cbest[lane + 32 * q] = (lane + 32 * q < ntri) ? bj[q] : kNone;
+  __syncwarp();
+  uint32_t found = 0;
+#pragma unroll
+  for (int q = 0; q < NCL; ++q) {
+    const int i = lane + 32 * q;
+    const uint32_t v = (i < ntri) ? bj[q] : kNone;
+    bool take = v != kNone;
+    for (int k = 0; k < i && take; ++k)
+      if (cbest[k] == v) take = false;
+    const unsigned m = __ballot_sync(FULL, take);
+    if (take) {
+      const uint32_t pos = found + __popc(m & ((1u << lane) - 1u));
+      if (pos < a.max_extra) a.extra[(size_t)pos * a.nbr_stride + row] = v;
+    }
+    found += __popc(m);
+  }
+  if (lane == 0) {
+    const bool more = overflow || found > a.max_extra;
+    a.extra_cnt[row] = (found < a.max_extra ? found : a.max_extra) | (more ? 0x80000000u : 0u);
+  }
+  __syncwarp();
+}
 
 template <int T, int P>
 __global__ void __launch_bounds__(kGeomWarps * 32) geom_kernel(GeomArgs a) {
@@ -127,6 +281,30 @@ __global__ void __launch_bounds__(kGeomWarps * 32) geom_kernel(GeomArgs a) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) R2 = fmax(R2, __shfl_xor_sync(FULL, R2, o));
   __syncwarp();
+
+  // ---- cell-centred certification (power range query)
+  if (a.node_wmax) {
+    constexpr int NCL = (T + 31) / 32;
+    const double wi = S.ws ? S.ws[s] : 0.0;
+    float4 mine[NCL];
+#pragma unroll
+    for (int q = 0; q < NCL; ++q) {
+      const int i = lane + 32 * q;
+      mine[q] = make_float4(0.f, 0.f, 0.f, -INFINITY);
+      if (i < ntri) {
+        const int t = g.tlist[i];
+        const double dx = g.px[t] - pi.x, dy = g.py[t] - pi.y, dz = g.pz[t] - pi.z;
+        const float rho = (float)(dx * dx + dy * dy + dz * dz - wi);
+        mine[q] = make_float4((float)g.px[t], (float)g.py[t], (float)g.pz[t], rho);
+        g.cf[i] = mine[q];
+      }
+    }
+    __syncwarp();
+    const GridDesc gd = *S.gd;
+    const uint32_t row = a.qrow ? a.qrow[ci] : ci;
+    certify_cell<T, NCL>(a, S, gd, s, row, ntri, mine, g.cf, g.cbest, g.stk, lane);
+    __syncwarp();
+  }
 
   // ---- FP32 clipping: the reference stops at the same neighbour only if
   // d(stop) > 4.1 (R2 + h^2) and d(last clipped) <= 4.1 (R2 + h^2) with the

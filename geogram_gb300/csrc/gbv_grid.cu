@@ -217,6 +217,42 @@ __global__ void scatter_kernel(const double* __restrict__ xyz, uint32_t stride,
   S.slot_of[i] = s;
 }
 
+// ---------------------------------------------------------------------
+// Max weight per octree node
+// ---------------------------------------------------------------------
+__global__ void wmax_fine_kernel(const uint32_t* __restrict__ cell_start,
+                                 const double* __restrict__ ws, size_t ncells,
+                                 double* __restrict__ out) {
+  const size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncells) return;
+  const uint32_t b = cell_start[c], e = cell_start[c + 1];
+  double m = -INFINITY;
+  for (uint32_t s = b; s < e; ++s) m = fmax(m, ws ? ws[s] : 0.0);
+  out[c] = m;
+}
+
+__global__ void wmax_up_kernel(const double* __restrict__ child, size_t nparent,
+                               double* __restrict__ parent) {
+  const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= nparent) return;
+  double m = child[8 * p];
+#pragma unroll
+  for (int k = 1; k < 8; ++k) m = fmax(m, child[8 * p + k]);
+  parent[p] = m;
+}
+
+void build_node_wmax(const SortedSeeds& S, double* wmax, cudaStream_t st) {
+  const int L = S.L;
+  const size_t nf = (size_t)1 << (3 * L);
+  wmax_fine_kernel<<<(unsigned)((nf + 255) / 256), 256, 0, st>>>(S.cell_start, S.ws, nf,
+                                                                  wmax + node_offset(L)); count_launch();
+  for (int l = L - 1; l >= 0; --l) {
+    const size_t np = (size_t)1 << (3 * l);
+    wmax_up_kernel<<<(unsigned)((np + 255) / 256), 256, 0, st>>>(wmax + node_offset(l + 1), np,
+                                                                  wmax + node_offset(l)); count_launch();
+  }
+}
+
 int choose_levels(uint32_t n) {
   int L = 1;
   while (L < 9 && (double)(1u << (3 * L)) < (double)n) ++L;

@@ -46,6 +46,15 @@ int choose_levels(uint32_t n);
 void build_grid(const double* xyz, uint32_t stride, uint32_t dim, const double* w,
                 uint32_t n, int L, SortedSeeds& S, GridScratch& scr, cudaStream_t st);
 
+// Max weight of the seeds in every node of the implicit octree, all levels:
+// level l occupies [node_offset(l), node_offset(l) + 8^l), empty nodes hold
+// -inf (weights are 0 for Voronoi diagrams).
+__host__ __device__ inline size_t node_offset(int l) {
+  return (((size_t)1 << (3 * l)) - 1) / 7;
+}
+inline size_t node_count(int L) { return node_offset(L + 1); }
+void build_node_wmax(const SortedSeeds& S, double* wmax, cudaStream_t st);
+
 enum KnnMode : int {
   KNN_CELLS = 0,  // exclude self and zero-distance seeds (delaunay_nn rule)
   KNN_ALL = 1,    // all stored points, self included (get_nearest_neighbors)

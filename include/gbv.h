@@ -72,8 +72,20 @@ typedef struct {
     uint32_t k0;         /* first neighbour list length (20, delaunay_nn.cpp:50) */
     uint32_t check_sr;   /* 1: grow the list until certified (set_check_SR) */
     uint32_t precision;  /* gbv_precision */
-    uint32_t reserved;
+    uint32_t certification; /* gbv_certification */
 } gbv_cell_options;
+
+typedef enum {
+    /* the reference's security-radius loop (generic_RVD.h:2278-2352) on
+     * the 4-d lift for weights: its results, bit for bit */
+    GBV_CERTIFY_SECURITY_RADIUS = 0,
+    /* no security radius: candidates from the kNN, then every seed that
+     * could still cut the cell is found by a power range query around the
+     * cell's corners (octree with per-node maximum weight) and clipped.
+     * Same cells in exact arithmetic; needed when weights vary widely (the
+     * lifted radius then spans most seeds), e.g. optimal transport. */
+    GBV_CERTIFY_POWER_RANGE = 1
+} gbv_certification;
 
 typedef struct {
     uint64_t nnz;              /* facets between seeds (CSR entries)        */
@@ -87,6 +99,8 @@ typedef struct {
     double volume_sum;         /* compensated FP64 sum of cell volumes      */
     uint64_t n_exact;          /* exact (expansion) predicate evaluations   */
     double ms_grid, ms_knn, ms_clip, ms_retry, ms_total;
+    uint32_t n_huge;     /* cells beyond 128 corners / 64 planes (one-thread path) */
+    uint32_t reserved;
 } gbv_cell_report;
 
 /* ---------------------------------------------------------------- */
@@ -195,6 +209,64 @@ gbv_status gbv_lloyd_device(gbv_context* ctx, double* d_xyz, const double* d_w,
                             uint32_t n, uint32_t iters,
                             const gbv_cell_options* opt, void* stream,
                             gbv_cell_report* report);
+
+/* ---------------------------------------------------------------- */
+/* Semi-discrete optimal transport (OptimalTransportMap3d, exploragram;
+ * driver compute_OTM/main.cpp:280-296).  The exploragram sources are not in
+ * the reference checkout; the solver follows the published method it
+ * implements: damped Newton on the Kantorovich dual with FP64 conjugate
+ * gradient on the Laguerre Hessian.                                  */
+/* ---------------------------------------------------------------- */
+
+typedef struct {
+    double box_min[3];   /* source: uniform density on this machine */
+    double box_max[3];
+    double tol;          /* stop when max_i |vol_i - nu_i| / nu_i < tol (1e-6) */
+    uint32_t max_newton; /* Newton iterations (100) */
+    uint32_t max_cg;     /* CG iterations per Newton step (4000) */
+    uint32_t precision;  /* gbv_precision of the cell computations */
+    uint32_t reserved;
+    /* CG stops at ||r|| <= cg_rtol ||b|| (default and 0: 1e-3) */
+    double cg_rtol;
+} gbv_ot_options;
+
+typedef struct {
+    uint32_t converged;
+    uint32_t newton_iters;
+    uint32_t cg_iters;        /* total */
+    uint32_t halvings;        /* damping steps of the line search */
+    uint32_t cell_calls;      /* Laguerre diagrams computed */
+    uint32_t reserved;
+    double mass_error_inf;    /* max_i |vol_i - nu_i| / nu_i at the end */
+    double mass_error_l2;     /* ||vol - nu|| / ||nu|| at the end */
+    double min_volume;
+    double ms_total, ms_cells, ms_linear;
+} gbv_ot_report;
+
+void gbv_ot_options_default(gbv_ot_options* opt);
+
+/* Weights w such that every Laguerre cell of seed i (clipped to the box)
+ * has volume nu_i (nu NULL: box volume / n each; sum nu must equal the box
+ * volume).  w_inout holds the starting weights (zeros, or a warm start) and
+ * receives the solution.  Host arrays; the report may be NULL. */
+gbv_status gbv_ot_solve(gbv_context* ctx, const double* xyz, const double* nu, uint32_t n,
+                        const gbv_ot_options* opt, double* w_inout, gbv_ot_report* report);
+
+/* Same on device arrays, ordered on `stream` (NULL: the context's). */
+gbv_status gbv_ot_solve_device(gbv_context* ctx, const double* d_xyz, const double* d_nu,
+                               uint32_t n, const gbv_ot_options* opt, double* d_w_inout,
+                               void* stream, gbv_ot_report* report);
+
+/* The callback of OptimalTransportMap3d's optimiser at weights w: the
+ * gradient g_i = nu_i - |Lag_i(w)| and the Hessian of the dual (CSR in
+ * the caller's seed order, off-diagonal -A_ij / (2 |p_i - p_j|), diagonal
+ * minus the row sum).  Host arrays.  Call with h_capacity = 0 to get *nnz;
+ * GBV_ERR_CAPACITY when h_capacity < *nnz. */
+gbv_status gbv_ot_gradient_hessian(gbv_context* ctx, const double* xyz, const double* w,
+                                   const double* nu, uint32_t n, const gbv_ot_options* opt,
+                                   double* g, uint32_t* h_rowptr, uint32_t* h_col,
+                                   double* h_val, double* h_diag, uint64_t h_capacity,
+                                   uint64_t* nnz);
 
 /* ---------------------------------------------------------------- */
 /* Allocation-free kNN                                               */

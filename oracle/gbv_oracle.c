@@ -752,7 +752,8 @@ static void cells_range(void* vctx, unsigned b, unsigned e) {
     cells_ctx* c = (cells_ctx*)vctx;
     cell_t C;
     cell_init(&C);
-    unsigned cap = 64;
+    /* room for the first request (k0 + 1 points) and then some */
+    unsigned cap = c->k0 + 2 > 64 ? c->k0 + 2 : 64;
     uint32_t* ix = (uint32_t*)malloc(sizeof(uint32_t) * (cap + 1));
     double* dd = (double*)malloc(sizeof(double) * (cap + 1));
     uint32_t* nb = (uint32_t*)malloc(sizeof(uint32_t) * (cap + 1));

@@ -120,7 +120,8 @@ def cells(xyz: np.ndarray, w: np.ndarray | None = None, k0: int = 20, check_sr: 
         raise RuntimeError("cells failed")
     cnt = out["cnt"].astype(np.int64)
     if (out["status"] == 4).any():
-        raise RuntimeError("max_nbr too small")
+        # a cell with more facets than max_nbr: again with room for all
+        return cells(x, wa, k0, check_sr, exact, nthreads, which, int(cnt.max()) + 1)
     rowptr = np.zeros(n + 1, np.int64)
     rowptr[1:] = np.cumsum(cnt)
     mask = np.arange(max_nbr)[None, :] < cnt[:, None]

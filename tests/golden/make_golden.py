@@ -6,7 +6,7 @@ small seeded inputs and saves inputs and outputs as compressed .npz files.
 Needs the reference checkout; the fixtures are committed so that the tests
 run without it.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case names]
 """
 from __future__ import annotations
 
@@ -47,18 +47,40 @@ def cases():
     yield "lattice_216", np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3), None
     x = np.random.default_rng(2).random((400, 3))
     yield "duplicates_405", np.concatenate([x, x[[3, 17, 17, 99, 250]]]), None
+    # a seed at the centre of a thin spherical shell of m seeds (radii
+    # jittered by 2% so that no five seeds are co-spherical): its cell has
+    # hundreds of facets, beyond the fixed-capacity clipping shapes
+    yield "shell_901", shell(300, 600, 300), None
+    yield "shell_1601", shell(1000, 600, 1000), None
 
 
-def main():
+def shell(m, n_background, seed):
+    rng = np.random.default_rng(seed)
+    k = np.arange(m) + 0.5
+    phi = np.arccos(1 - 2 * k / m)
+    th = np.pi * (1 + 5 ** 0.5) * k
+    d = np.stack([np.cos(th) * np.sin(phi), np.sin(th) * np.sin(phi), np.cos(phi)], 1)
+    r = 0.1 * (1 + 0.02 * rng.random(m))
+    bg = rng.random((3 * n_background, 3))
+    bg = bg[np.linalg.norm(bg - 0.5, axis=1) > 0.2][:n_background]
+    return np.concatenate([[[0.5, 0.5, 0.5]], 0.5 + d * r[:, None], bg])
+
+
+def main(only=None):
+    """Writes every fixture, or only those whose names are listed."""
     oracle.build_ref()
     for name, x, w in cases():
+        if only and name not in only:
+            continue
         x = np.ascontiguousarray(x)
-        r = oracle.cells(x, w, nthreads=8, which="ref")
+        r = oracle.cells(x, w, nthreads=8, which="ref", max_nbr=2100)
         np.savez_compressed(os.path.join(HERE, f"cells_{name}.npz"), x=x,
                             w=np.zeros(0) if w is None else w, vol=r["vol"], mg=r["mg"],
                             rowptr=r["rowptr"], nbr=r["nbr"], area=r["area"],
                             status=r["status"], n_clip=r["n_clip"], k_list=r["k_list"])
         print(name, len(x), "cells, nnz", len(r["nbr"]))
+    if only:
+        return
     x = np.random.default_rng(3).random((2000, 3))
     idx, d2 = oracle.knn(x, 21, nthreads=8, which="ref")
     np.savez_compressed(os.path.join(HERE, "knn_2000.npz"), x=x, idx=idx, d2=d2)
@@ -69,4 +91,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

@@ -13,7 +13,7 @@ from conftest import canonical_ids, load_golden
 
 pytestmark = pytest.mark.gpu
 
-EXACT_CASES = ["uniform_1500", "power_1500", "clustered_1500"]
+EXACT_CASES = ["uniform_1500", "power_1500", "clustered_1500", "shell_901", "shell_1601"]
 PRECISIONS = ["fp64", "fp32"]
 
 
@@ -157,3 +157,14 @@ def test_duplicates_status(g):
     assert np.allclose(c.volume[dup], 1.0, rtol=0, atol=1e-15)
     # seed 17 has two copies: the reference's list growth stalls at 18
     assert c.status[17] == g.CELL_STALLED and ref["status"][17] == 3
+
+
+@pytest.mark.parametrize("prec", PRECISIONS)
+def test_cells_beyond_fixed_capacity(g, prec):
+    """The shell's centre cell (hundreds of facets) and the outer cells with
+    more than 64 facets take the unbounded path; results stay bit-exact."""
+    ref = load_golden("cells_shell_1601.npz")
+    c = g.compute_cells(ref["x"], precision=prec)
+    assert c.report["n_huge"] >= 1
+    assert np.diff(c.rowptr.astype(np.int64)).max() == np.diff(ref["rowptr"]).max() > 600
+    assert_cells_equal(c, ref)

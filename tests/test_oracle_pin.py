@@ -11,7 +11,7 @@ import pytest
 
 from conftest import canonical_ids, load_golden
 
-EXACT_CASES = ["uniform_1500", "power_1500", "clustered_1500"]
+EXACT_CASES = ["uniform_1500", "power_1500", "clustered_1500", "shell_901", "shell_1601"]
 
 
 @pytest.mark.parametrize("name", EXACT_CASES)
