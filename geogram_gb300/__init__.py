@@ -106,8 +106,8 @@ def cell_options(box=((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)), k0: int = 20, check_sr:
 
 
 def ot_options(box=((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)), tol: float = 1e-6, max_newton: int = 100,
-               max_cg: int = 4000, precision: str | int = "fp32", cg_rtol: float = 1e-3
-               ) -> OtOptions:
+               max_cg: int = 4000, precision: str | int = "fp32", cg_rtol: float = 1e-3,
+               step_growth: float = 4.0) -> OtOptions:
     o = OtOptions()
     _lib.load().gbv_ot_options_default(ctypes.byref(o))
     for c in range(3):
@@ -118,6 +118,7 @@ def ot_options(box=((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)), tol: float = 1e-6, max_ne
     o.max_cg = int(max_cg)
     o.precision = _precision(precision)
     o.cg_rtol = float(cg_rtol)
+    o.step_growth = float(step_growth)
     return o
 
 
@@ -289,7 +290,8 @@ def lloyd_iterations(xyz_dev, iters: int, weights_dev=None, *,
 def ot_solve(xyz: np.ndarray, nu: np.ndarray | None = None, w0: np.ndarray | None = None, *,
              box=((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)), tol: float = 1e-6, max_newton: int = 100,
              max_cg: int = 4000, precision="fp32", cg_rtol: float = 1e-3,
-             ctx: Context | None = None) -> tuple[np.ndarray, dict]:
+             step_growth: float = 4.0, ctx: Context | None = None
+             ) -> tuple[np.ndarray, dict]:
     """Weights of the seeds whose Laguerre cells in the box have volumes nu
     (default: box volume / n each), starting from w0 (default zeros)."""
     ctx = ctx or default_context()
@@ -297,7 +299,7 @@ def ot_solve(xyz: np.ndarray, nu: np.ndarray | None = None, w0: np.ndarray | Non
     n = len(x)
     w = np.zeros(n) if w0 is None else np.array(w0, dtype=np.float64, copy=True).reshape(n)
     m = None if nu is None else np.ascontiguousarray(nu, dtype=np.float64).reshape(n)
-    o = ot_options(box, tol, max_newton, max_cg, precision, cg_rtol)
+    o = ot_options(box, tol, max_newton, max_cg, precision, cg_rtol, step_growth)
     rep = OtReport()
     _lib.check(ctx._lib.gbv_ot_solve(ctx.handle, _lib.ptr(x), _lib.ptr(m), n, ctypes.byref(o),
                                      _lib.ptr(w), ctypes.byref(rep)))
@@ -306,11 +308,11 @@ def ot_solve(xyz: np.ndarray, nu: np.ndarray | None = None, w0: np.ndarray | Non
 
 def ot_solve_device(xyz_dev, w_dev, nu_dev=None, *, box=((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)),
                     tol: float = 1e-6, max_newton: int = 100, max_cg: int = 4000,
-                    precision="fp32", cg_rtol: float = 1e-3, stream=None,
-                    ctx: Context | None = None) -> dict:
+                    precision="fp32", cg_rtol: float = 1e-3, step_growth: float = 4.0,
+                    stream=None, ctx: Context | None = None) -> dict:
     """ot_solve on torch CUDA tensors; w_dev (float64, n) is updated in place."""
     ctx = ctx or default_context()
-    o = ot_options(box, tol, max_newton, max_cg, precision, cg_rtol)
+    o = ot_options(box, tol, max_newton, max_cg, precision, cg_rtol, step_growth)
     rep = OtReport()
     st = ctypes.c_void_p(stream.cuda_stream) if stream is not None else None
     _lib.check(ctx._lib.gbv_ot_solve_device(ctx.handle, _lib.ptr(xyz_dev), _lib.ptr(nu_dev),

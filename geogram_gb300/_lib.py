@@ -58,6 +58,7 @@ class OtOptions(ctypes.Structure):
         ("precision", ctypes.c_uint32),
         ("reserved", ctypes.c_uint32),
         ("cg_rtol", ctypes.c_double),
+        ("step_growth", ctypes.c_double),
     ]
 
 

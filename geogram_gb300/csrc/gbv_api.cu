@@ -21,6 +21,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <string>
@@ -322,6 +323,20 @@ struct ListSet {
   const uint32_t* last_idx = nullptr;
 };
 
+// Order of candidates in Laguerre mode: twice the distance from the seed
+// to the power bisector, (|d|^2 + w_i - w_j) / |d|, ties by original index.
+// Clipping the nearest planes first keeps the intermediate polytopes small.
+__device__ __forceinline__ float plane_key(const double4& pi, double wi, const double4& pj,
+                                           double wj) {
+  const float dx = (float)(pj.x - pi.x), dy = (float)(pj.y - pi.y), dz = (float)(pj.z - pi.z);
+  const float d2 = dx * dx + dy * dy + dz * dz;
+  return (d2 + (float)(wi - wj)) * rsqrtf(fmaxf(d2, 1e-30f));
+}
+
+__device__ __forceinline__ bool key_less(float ka, uint32_t oa, float kb, uint32_t ob) {
+  return ka < kb || (ka == kb && oa < ob);
+}
+
 // Cells with extra candidates from the certification: their slots, list
 // rows and counts.
 __global__ void collect_extra_kernel(const uint32_t* __restrict__ qlist, uint32_t nq,
@@ -339,17 +354,17 @@ __global__ void collect_extra_kernel(const uint32_t* __restrict__ qlist, uint32_
   out_r[k] = qi;
 }
 
-// New lists = old list of the row, then the certification's extras sorted
-// by (distance to the seed, original index).  The range query meets the
-// extras in slot order, and slots within a grid cell depend on the order of
-// the counting sort's atomics; sorting makes the clipping order, hence the
-// results, deterministic (and clips nearer seeds first).
+// New lists = old list of the row, then the certification's extras in
+// plane order.  The range query meets the extras in slot order, and slots
+// within a grid cell depend on the order of the counting sort's atomics;
+// sorting makes the clipping order, hence the results, deterministic.
 __global__ void append_extra_kernel(const uint32_t* __restrict__ sl, const uint32_t* __restrict__ rows,
                                     uint32_t m, const uint32_t* __restrict__ old_lists,
                                     uint32_t old_stride, const uint32_t* __restrict__ old_cnt,
                                     const uint32_t* __restrict__ extra,
                                     const uint32_t* __restrict__ extra_cnt, uint32_t ex_stride,
                                     uint32_t max_extra, const double4* __restrict__ xd,
+                                    const double* __restrict__ ws,
                                     const uint32_t* __restrict__ perm,
                                     uint32_t* __restrict__ new_lists,
                                     uint32_t* __restrict__ new_cnt) {
@@ -360,26 +375,17 @@ __global__ void append_extra_kernel(const uint32_t* __restrict__ sl, const uint3
   for (uint32_t j = 0; j < c0; ++j) new_lists[(size_t)j * m + i] = old_lists[(size_t)j * old_stride + r];
   const uint32_t ce = min(extra_cnt[r] & 0x7FFFFFFFu, max_extra);
   const double4 pi = xd[s];
-  auto key_of = [&](uint32_t j, double& d, uint32_t& o) {
-    const double4 p = xd[j];
-    const double dx = p.x - pi.x, dy = p.y - pi.y, dz = p.z - pi.z;
-    d = dx * dx + dy * dy + dz * dz;
-    o = perm[j];
-  };
+  const double wi = ws ? ws[s] : 0.0;
   // insertion sort into place (few extras per cell; a handful of cells
   // next to dense clusters have hundreds)
   for (uint32_t j = 0; j < ce; ++j) {
     const uint32_t v = extra[(size_t)j * ex_stride + r];
-    double dv;
-    uint32_t ov;
-    key_of(v, dv, ov);
+    const float kv = plane_key(pi, wi, xd[v], ws ? ws[v] : 0.0);
+    const uint32_t ov = perm[v];
     uint32_t k = j;
     while (k > 0) {
       const uint32_t u = new_lists[(size_t)(c0 + k - 1) * m + i];
-      double du;
-      uint32_t ou;
-      key_of(u, du, ou);
-      if (du < dv || (du == dv && ou < ov)) break;
+      if (key_less(plane_key(pi, wi, xd[u], ws ? ws[u] : 0.0), perm[u], kv, ov)) break;
       new_lists[(size_t)(c0 + k) * m + i] = u;
       --k;
     }
@@ -388,17 +394,40 @@ __global__ void append_extra_kernel(const uint32_t* __restrict__ sl, const uint3
   new_cnt[i] = c0 + ce;
 }
 
-// Candidate lists from a CSR adjacency in the caller's order.
+// Candidate lists from a CSR adjacency in the caller's order (at most k
+// per row, k <= kMaxCsrCandidates), in plane order.
+constexpr uint32_t kMaxCsrCandidates = 96;
+
 __global__ void csr_to_lists_kernel(const uint32_t* __restrict__ rowptr,
                                     const uint32_t* __restrict__ idx,
                                     const uint32_t* __restrict__ slot_of, uint32_t n, uint32_t k,
+                                    const double4* __restrict__ xd,
+                                    const double* __restrict__ ws,
                                     uint32_t* __restrict__ lists, uint32_t* __restrict__ cnt) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const uint32_t s = slot_of[i];
   const uint32_t b = rowptr[i];
-  const uint32_t c = min(rowptr[i + 1] - b, k);
-  for (uint32_t j = 0; j < c; ++j) lists[(size_t)j * n + s] = slot_of[idx[b + j]];
+  const uint32_t c = min(min(rowptr[i + 1] - b, k), kMaxCsrCandidates);
+  const double4 pi = xd[s];
+  const double wi = ws ? ws[s] : 0.0;
+  float key[kMaxCsrCandidates];
+  uint32_t ord[kMaxCsrCandidates];
+  // insertion sort by (plane key, original index); the previous cells'
+  // facets come in their clipping order, so rows are nearly sorted
+  for (uint32_t j = 0; j < c; ++j) {
+    const uint32_t o = idx[b + j];
+    const float kv = plane_key(pi, wi, xd[slot_of[o]], ws ? ws[slot_of[o]] : 0.0);
+    uint32_t q = j;
+    while (q > 0 && key_less(kv, o, key[q - 1], ord[q - 1])) {
+      key[q] = key[q - 1];
+      ord[q] = ord[q - 1];
+      --q;
+    }
+    key[q] = kv;
+    ord[q] = o;
+  }
+  for (uint32_t j = 0; j < c; ++j) lists[(size_t)j * n + s] = slot_of[ord[j]];
   cnt[s] = c;
 }
 
@@ -579,6 +608,7 @@ struct Pipeline {
       h.scr_t = c->buf<ushort4>("huge_t", cap * kHugeT);
       h.scr_adj = c->buf<ushort4>("huge_adj", cap * kHugeT);
       h.scr_cor = c->buf<double4>("huge_cor", cap * kHugeT);
+      h.scr_eps = c->buf<float>("huge_eps", cap * kHugeT);
       h.scr_pl = c->buf<double4>("huge_pl", cap * kHugeV);
       h.scr_vg = c->buf<uint32_t>("huge_vg", cap * kHugeV);
       h.scr_v2t = c->buf<uint16_t>("huge_v2t", cap * kHugeV);
@@ -598,8 +628,33 @@ struct Pipeline {
         h.extra_cnt = extra_cnt;
         h.max_extra = max_extra;
       }
+      const bool stats = std::getenv("GBV_HUGE_STATS") != nullptr;
+      if (stats) {
+        h.stats = c->buf<unsigned long long>("huge_stats", (size_t)cm * kHugeStats);
+        GBV_CUDA(cudaMemsetAsync(h.stats, 0, sizeof(unsigned long long) * cm * kHugeStats, st));
+      }
       launch_huge(h, st);
       GBV_CUDA(last_launch_error);
+      if (stats) {
+        // per-phase cycles and work of the cells of this launch, on stderr
+        std::vector<unsigned long long> v((size_t)cm * kHugeStats);
+        GBV_CUDA(cudaMemcpyAsync(v.data(), h.stats, v.size() * 8, cudaMemcpyDeviceToHost, st));
+        GBV_CUDA(cudaStreamSynchronize(st));
+        unsigned long long mx[kHugeStats] = {}, sum[kHugeStats] = {};
+        for (uint32_t q = 0; q < cm; ++q)
+          for (int k = 0; k < kHugeStats; ++k) {
+            mx[k] = std::max(mx[k], v[(size_t)q * kHugeStats + k]);
+            sum[k] += v[(size_t)q * kHugeStats + k];
+          }
+        std::fprintf(stderr,
+                     "[huge] %u cells  max/mean: clip Mcyc %.1f/%.1f geom %.1f/%.1f certify "
+                     "%.1f/%.1f clips %llu/%.0f tests %llu/%.0f tri %llu/%.0f planes %llu/%.0f "
+                     "nodes %llu/%.0f seeds %llu/%.0f\n",
+                     cm, mx[0] * 1e-6, sum[0] * 1e-6 / cm, mx[1] * 1e-6, sum[1] * 1e-6 / cm,
+                     mx[2] * 1e-6, sum[2] * 1e-6 / cm, mx[3], (double)sum[3] / cm, mx[4],
+                     (double)sum[4] / cm, mx[5], (double)sum[5] / cm, mx[6], (double)sum[6] / cm,
+                     mx[7], (double)sum[7] / cm, mx[8], (double)sum[8] / cm);
+      }
     }
   }
 
@@ -857,10 +912,32 @@ static void cells_device(gbv_context* c, const double* d_xyz, const double* d_w,
 // vary too much for the 4-d lift's radius to stop.  Candidates come from a
 // CSR adjacency in the caller's order (e.g. the previous Newton iterate's
 // cells) or, when none is given, from the kNN (lifted when weighted).
-static void laguerre_device(gbv_context* c, const double* d_xyz, const double* d_w, uint32_t n,
+//
+// abort_below > 0: after the first pass every cell's volume bounds its final
+// volume from above (clipping by more seeds only removes volume), so when
+// one is below abort_below the call stops there and returns false -- the
+// line search of the optimal-transport solver rejects such steps, and
+// their cells are the costliest to certify.  Returns true when the cells
+// are complete.
+__global__ void min_partial_kernel(const double* __restrict__ v, uint32_t n,
+                                   double* __restrict__ part) {
+  __shared__ double sm[256];
+  double m = DBL_MAX;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    m = fmin(m, v[i]);
+  sm[threadIdx.x] = m;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sm[threadIdx.x] = fmin(sm[threadIdx.x], sm[threadIdx.x + o]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sm[0];
+}
+
+static bool laguerre_device(gbv_context* c, const double* d_xyz, const double* d_w, uint32_t n,
                             const double* box_min, const double* box_max, bool fp32,
                             const uint32_t* cand_rowptr, const uint32_t* cand_idx,
-                            cudaStream_t st, gbv_cell_report* rep) {
+                            cudaStream_t st, gbv_cell_report* rep, double abort_below = 0.0) {
   if (n < 2) throw StatusError{GBV_ERR_INVALID_ARGUMENT, "n must be >= 2"};
   setup_seeds(c, n, d_w != nullptr);
   c->nn_ready = false;
@@ -882,10 +959,10 @@ static void laguerre_device(gbv_context* c, const double* d_xyz, const double* d
     max_degree_kernel<<<nblocks(n, 256), 256, 0, st>>>(cand_rowptr, n, dmax); count_launch();
     GBV_CUDA(cudaMemcpyAsync(&c->h_counts[0], dmax, 4, cudaMemcpyDeviceToHost, st));
     GBV_CUDA(cudaStreamSynchronize(st));
-    K = std::max<uint32_t>(1, std::min<uint32_t>(c->h_counts[0], 96));
+    K = std::max<uint32_t>(1, std::min<uint32_t>(c->h_counts[0], kMaxCsrCandidates));
     lists = c->buf<uint32_t>("lag_lists", (size_t)K * n);
-    csr_to_lists_kernel<<<nblocks(n, 256), 256, 0, st>>>(cand_rowptr, cand_idx, S.slot_of, n, K,
-                                                         lists, cnt); count_launch();
+    csr_to_lists_kernel<<<nblocks(n, 128), 128, 0, st>>>(cand_rowptr, cand_idx, S.slot_of, n, K,
+                                                         S.xd, S.ws, lists, cnt); count_launch();
   } else {
     K = std::min<uint32_t>(32, n - 1);
     lists = c->buf<uint32_t>("lag_lists", (size_t)K * n);
@@ -919,7 +996,25 @@ static void laguerre_device(gbv_context* c, const double* d_xyz, const double* d
     P.size_extras(std::min<uint32_t>(32u << std::min(round, 6), kHugeV), cur.stride);
     if (P.process(cur, ql, nullptr, nq) != 0)
       throw StatusError{GBV_ERR_STATE, "unexpected list exhaustion in Laguerre mode"};
-    if (round == 0) GBV_CUDA(cudaEventRecord(c->ev[5], st));
+    if (round == 0) {
+      GBV_CUDA(cudaEventRecord(c->ev[5], st));
+      if (abort_below > 0.0) {
+        double* part = c->buf<double>("lag_min_part", 256);
+        min_partial_kernel<<<256, 256, 0, st>>>(P.vol_s, n, part); count_launch();
+        double hp[256];
+        GBV_CUDA(cudaMemcpyAsync(hp, part, sizeof(hp), cudaMemcpyDeviceToHost, st));
+        GBV_CUDA(cudaStreamSynchronize(st));
+        double mn = DBL_MAX;
+        for (double v : hp) mn = std::min(mn, v);
+        if (mn < abort_below) {
+          c->has_cells = false;
+          if (std::getenv("GBV_OT_LOG"))
+            std::fprintf(stderr, "[ot]   first-pass min volume %.3e < %.3e: stopped\n", mn,
+                         abort_below);
+          return false;
+        }
+      }
+    }
     GBV_CUDA(cudaMemsetAsync(ex_count, 0, 4, st));
     collect_extra_kernel<<<nblocks(nq, 256), 256, 0, st>>>(ql, nq, P.extra_cnt, P.status_s,
                                                            ex_count, ex_s, ex_r); count_launch();
@@ -928,6 +1023,9 @@ static void laguerre_device(gbv_context* c, const double* d_xyz, const double* d
     const uint32_t m = c->h_counts[0];
     if (m == 0) break;
     P.n_morek += m;
+    if (std::getenv("GBV_OT_LOG"))
+      std::fprintf(stderr, "[ot]   round %d: %u cells with extra candidates (room %u)\n", round, m,
+                   P.max_extra);
     if (round >= 24) throw StatusError{GBV_ERR_NOT_CONVERGED, "certification did not settle"};
     const std::string tag = std::to_string(round & 1);
     const uint32_t newk = cur.k + P.max_extra;
@@ -937,8 +1035,8 @@ static void laguerre_device(gbv_context* c, const double* d_xyz, const double* d
     GBV_CUDA(cudaMemcpyAsync(q_s, ex_s, m * 4, cudaMemcpyDeviceToDevice, st));
     append_extra_kernel<<<nblocks(m, 128), 128, 0, st>>>(ex_s, ex_r, m, cur.lists, cur.stride,
                                                          cur.cnt, P.extra, P.extra_cnt,
-                                                         cur.stride, P.max_extra, S.xd, S.perm,
-                                                         nl, nc); count_launch();
+                                                         cur.stride, P.max_extra, S.xd, S.ws,
+                                                         S.perm, nl, nc); count_launch();
     cur.lists = nl;
     cur.stride = m;
     cur.cnt = nc;
@@ -958,6 +1056,7 @@ static void laguerre_device(gbv_context* c, const double* d_xyz, const double* d
     GBV_CUDA(cudaStreamSynchronize(st));
   }
   GBV_CUDA(cudaGetLastError());
+  return true;
 }
 
 // ---------------------------------------------------------------------
@@ -1022,11 +1121,30 @@ __global__ void fill_kernel(double* __restrict__ y, double v, uint32_t n) {
 
 // Laguerre cells at weights w with the given candidates (CSR in caller
 // order, may be null); results in the context.
-static void ot_cells(gbv_context* c, const double* xyz, const double* w, uint32_t n,
+// Progress lines on stderr when the environment sets GBV_OT_LOG (the
+// solver's counterpart of the reference's Logger output).
+static bool ot_log_enabled() {
+  static const bool on = std::getenv("GBV_OT_LOG") != nullptr;
+  return on;
+}
+
+static bool ot_cells(gbv_context* c, const double* xyz, const double* w, uint32_t n,
                      const gbv_ot_options& o, const uint32_t* cand_rp, const uint32_t* cand_ix,
-                     cudaStream_t st) {
-  laguerre_device(c, xyz, w, n, o.box_min, o.box_max, o.precision == GBV_PRECISION_FP32_RECHECK,
-                  cand_rp, cand_ix, st, nullptr);
+                     cudaStream_t st, double abort_below = 0.0) {
+  gbv_cell_report rep{};
+  const bool log = ot_log_enabled();
+  const bool done =
+      laguerre_device(c, xyz, w, n, o.box_min, o.box_max, o.precision == GBV_PRECISION_FP32_RECHECK,
+                      cand_rp, cand_ix, st, log ? &rep : nullptr, abort_below);
+  if (!done) return false;
+  if (log)
+    std::fprintf(stderr,
+                 "[ot] cells: %.1f ms (knn %.1f, first pass %.1f, rounds %.1f) extra %u huge %u "
+                 "overflow %u recheck %u max_clips %u mean_clips %.1f candidates %u exact %llu\n",
+                 rep.ms_total, rep.ms_knn, rep.ms_clip, rep.ms_retry, rep.n_more_k, rep.n_huge,
+                 rep.n_overflow, rep.n_recheck_fp64, rep.max_clips, rep.mean_clips, rep.knn_k,
+                 (unsigned long long)rep.n_exact);
+  return true;
 }
 
 // Saves the current cells' adjacency as the next call's candidates.
@@ -1085,11 +1203,13 @@ static void ot_solve(gbv_context* c, const double* xyz, const double* nu_in, uin
 
   uint32_t *adj_rp = nullptr, *adj_ix = nullptr;
   uint32_t cell_calls = 0, cg_total = 0, halvings = 0, it = 0;
-  auto cells = [&](const double* ww, bool with_adj) {
+  auto cells = [&](const double* ww, bool with_adj, double abort_below = 0.0) {
     const auto tc = std::chrono::steady_clock::now();
-    ot_cells(c, xyz, ww, n, o, with_adj ? adj_rp : nullptr, with_adj ? adj_ix : nullptr, st);
+    const bool done = ot_cells(c, xyz, ww, n, o, with_adj ? adj_rp : nullptr,
+                               with_adj ? adj_ix : nullptr, st, abort_below);
     ++cell_calls;
     ms_cells += now_ms(tc);
+    return done;
   };
   cells(w, false);
   double r2, rel_inf, vmin;
@@ -1103,6 +1223,7 @@ static void ot_solve(gbv_context* c, const double* xyz, const double* nu_in, uin
   }
   const double eps0 = 0.5 * std::min(nu_min, vmin);
   bool converged = rel_inf < o.tol;
+  double alpha_prev = 1.0;
   for (it = 0; it < o.max_newton && !converged; ++it) {
     save_adjacency(c, n, st, &adj_rp, &adj_ix);
     const auto tl = std::chrono::steady_clock::now();
@@ -1135,21 +1256,35 @@ static void ot_solve(gbv_context* c, const double* xyz, const double* nu_in, uin
     add_scalar(x, -xmean, n, st);
     ms_lin += now_ms(tl);
     // damped step (Kitagawa-Merigot-Thibert): halve until every cell keeps
-    // at least eps0 and the residual drops by (1 - alpha / 2)
-    double alpha = 1.0;
+    // at least eps0 and the residual drops by (1 - alpha / 2); the first
+    // trial is min(1, step_growth * the previous step), which skips the
+    // full steps that early iterations always reject (and whose cells are
+    // the costliest to compute)
+    double alpha = o.step_growth > 0.0 ? std::min(1.0, o.step_growth * alpha_prev) : 1.0;
     bool accepted = false;
     for (int h = 0; h < 30; ++h) {
       GBV_CUDA(cudaMemcpyAsync(wt, w, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
       axpy(wt, x, alpha, n, st);
-      cells(wt, true);
+      // a cell already below eps0 after the first pass rejects the step
+      if (!cells(wt, true, eps0)) {
+        if (ot_log_enabled())
+          std::fprintf(stderr, "[ot] newton %u alpha %g rejected: a cell below eps0\n", it, alpha);
+        alpha *= 0.5;
+        ++halvings;
+        continue;
+      }
       double r2t, relt, vmint;
       W.residual_stats(c->vol, nu, r, r2t, relt, vmint);
+      if (ot_log_enabled())
+        std::fprintf(stderr, "[ot] newton %u alpha %g |r| %.3e -> %.3e max rel %.3e min vol %.3e (eps0 %.3e)\n",
+                     it, alpha, std::sqrt(r2), std::sqrt(r2t), relt, vmint, eps0);
       if (vmint >= eps0 && std::sqrt(r2t) <= (1.0 - 0.5 * alpha) * std::sqrt(r2)) {
         GBV_CUDA(cudaMemcpyAsync(w, wt, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
         r2 = r2t;
         rel_inf = relt;
         vmin = vmint;
         accepted = true;
+        alpha_prev = alpha;
         break;
       }
       alpha *= 0.5;
@@ -1482,6 +1617,7 @@ void gbv_ot_options_default(gbv_ot_options* o) {
   o->max_cg = 4000;
   o->precision = GBV_PRECISION_FP32_RECHECK;
   o->cg_rtol = 1e-3;
+  o->step_growth = 4.0;
 }
 
 gbv_status gbv_ot_solve_device(gbv_context* c, const double* d_xyz, const double* d_nu, uint32_t n,

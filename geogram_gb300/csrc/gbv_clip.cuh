@@ -94,7 +94,7 @@ struct GeomArgs {
 // formulas and summation order.
 void launch_geometry(const GeomArgs& a, cudaStream_t st);
 
-// Cells beyond the large shape: one thread per cell, polytope in global
+// Cells beyond the large shape: one single-thread block per cell, polytope in global
 // memory (kHugeT corners, kHugeV planes), clipping and geometry in one
 // kernel.  Their facets go to a separate area: nf[slot] carries
 // kHugeFacets and hp_nbr[slot] / hp_area[slot] point at the cell's
@@ -122,6 +122,7 @@ struct HugeArgs {
   ushort4* scr_t;
   ushort4* scr_adj;
   double4* scr_cor;
+  float* scr_eps;
   double4* scr_pl;
   uint32_t* scr_vg;
   uint16_t* scr_v2t;
@@ -140,7 +141,12 @@ struct HugeArgs {
   uint32_t* extra;
   uint32_t* extra_cnt;
   uint32_t max_extra;
+  // optional per-query counters (kHugeStats each): cycles of the clipping,
+  // geometry and certification phases, clips, conflict tests, triangles,
+  // planes, octree nodes and seeds visited by the certification
+  unsigned long long* stats;
 };
+constexpr int kHugeStats = 9;
 
 void launch_huge(const HugeArgs& a, cudaStream_t st);
 

@@ -168,9 +168,38 @@ __device__ __forceinline__ void certify_cell(const GeomArgs& a, const SortedSeed
       overflow = true;
       break;
     }
-    if (lane < 8) stk[sp + lane] = (((code << 3) | (uint32_t)lane) << 4) | (uint32_t)(lev + 1);
-    __syncwarp();
-    sp += 8;
+    // children nearest to the seed (power lower bound) popped first: the
+    // corners' bounds then shrink early and prune the rest
+    {
+      float key = INFINITY;
+      bool live = false;
+      if (lane < 8) {
+        const uint32_t cc = (code << 3) | (uint32_t)lane;
+        const int csh = shift - 1;
+        live = S.cell_start[cc << (3 * csh)] != S.cell_start[(cc + 1u) << (3 * csh)];
+        if (live) {
+          const float cs = 0.5f * side;
+          const float qx = bx + (float)(lane & 1) * cs, qy = by + (float)((lane >> 1) & 1) * cs,
+                      qz = bz + (float)((lane >> 2) & 1) * cs;
+          const float sx = (float)pi_d.x, sy = (float)pi_d.y, sz = (float)pi_d.z;
+          const float ex = fmaxf(fmaxf(qx - sx, sx - (qx + cs)), 0.f);
+          const float ey = fmaxf(fmaxf(qy - sy, sy - (qy + cs)), 0.f);
+          const float ez = fmaxf(fmaxf(qz - sz, sz - (qz + cs)), 0.f);
+          key = ex * ex + ey * ey + ez * ez - (float)a.node_wmax[node_offset(lev + 1) + cc];
+        }
+      }
+      const unsigned lm = __ballot_sync(FULL, live);
+      // rank among the live children, descending key (ties by child index)
+      int rank = 0;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const float kk = __shfl_sync(FULL, key, k);
+        if (((lm >> k) & 1u) && (kk > key || (kk == key && k < lane))) ++rank;
+      }
+      if (live) stk[sp + rank] = (((code << 3) | (uint32_t)lane) << 4) | (uint32_t)(lev + 1);
+      __syncwarp();
+      sp += __popc(lm);
+    }
   }
   // the distinct best seeds, in corner order
 #pragma unroll

@@ -1,5 +1,5 @@
 // Cells beyond the capacity of the clipping kernels (more than 128 corners
-// or 64 live planes): one thread per cell, the polytope in global memory
+// or 64 live planes): one single-thread block per cell, the polytope in global memory
 // with room for kHugeT corners and kHugeV planes, FP64 with exact conflict
 // signs, and the reference's own list discipline, so that the results are
 // those of the other paths (and of the reference) bit for bit.
@@ -29,6 +29,7 @@
 // and never uses it); slots keep clipping order, which is the order in
 // which facets are reported, so nothing observable changes.
 #include "gbv_clip.cuh"
+#include "gbv_corner.cuh"
 #include "gbv_exact.cuh"
 #include "gbv_refgeom.cuh"
 
@@ -38,18 +39,19 @@ namespace {
 
 constexpr uint16_t kEnd = 16383;     // END_OF_LIST of the 14-bit links
 constexpr uint16_t kConf = 32768;    // link flag: the triangle is in conflict
-constexpr double kDetFilter = 4e-14; // |det| above this times its permanent: sign is sure
 
 struct HugeCell {
   ushort4* t;     // plane slots i, j, k and the list link
   ushort4* adj;   // adjacent triangles across the edges opposite i, j, k
   double4* cor;   // corner (x, y, z) and its squared distance to the seed
+  float* eps;     // error bound of the corner (cramer_bound)
   double4* pl;    // plane equations
   uint32_t* vg;   // plane slot -> neighbour slot (kNone for the box)
   uint16_t* v2t;
   uint8_t* v2e;
   int nb_t, nb_v, first_free, first_valid;
   bool full;
+  unsigned long long tests, nodes, seeds;  // work counters
 };
 
 __device__ __forceinline__ int vtx(const ushort4& t, int lv) {
@@ -69,8 +71,11 @@ __device__ __forceinline__ int find_vtx(const ushort4& t, int v) {
 
 __device__ __forceinline__ void set_corner(HugeCell& C, int t, const double4& pi) {
   const ushort4 tv = C.t[t];
-  const double3 p = r_corner(C.pl[tv.x], C.pl[tv.y], C.pl[tv.z]);
-  C.cor[t] = make_double4(p.x, p.y, p.z, r_sqdist(pi.x, pi.y, pi.z, p));
+  double x, y, z;
+  float e;
+  corner_fp64(C.pl[tv.x], C.pl[tv.y], C.pl[tv.z], x, y, z, e);
+  C.cor[t] = make_double4(x, y, z, r_sqdist(pi.x, pi.y, pi.z, make_double3(x, y, z)));
+  C.eps[t] = e;
 }
 
 // new_triangle: the most recently freed slot first, pushed at the head of
@@ -117,32 +122,19 @@ __device__ void init_box(HugeCell& C, const double* box, const double4& pi) {
 }
 
 // Conflict of triangle t with plane P: det [P_i; P_j; P_k; P] >= 0, exact.
-__device__ bool in_conflict(const HugeCell& C, int t, const double4& P,
-                            unsigned long long& n_exact) {
+// Decided, as in the clipping kernels, from the cached corner c: the sign
+// of P . (c, 1) when it exceeds the corner's error bound, else exactly.
+__device__ __forceinline__ bool in_conflict(const HugeCell& C, int t, const double4& P,
+                                            double pa1, double bw, unsigned long long& n_exact) {
+  const double4 c = C.cor[t];
+  const double sv = fma(P.z, c.z, fma(P.y, c.y, fma(P.x, c.x, P.w)));
+  const double bound = fma(pa1, (double)C.eps[t], bw);
+  if (sv < -bound) return true;
+  if (sv > bound) return false;
   const ushort4 tv = C.t[t];
-  const double4 a = C.pl[tv.x], b = C.pl[tv.y], c = C.pl[tv.z];
+  const double4 a = C.pl[tv.x], b = C.pl[tv.y], d = C.pl[tv.z];
   const double r0[4] = {a.x, a.y, a.z, a.w}, r1[4] = {b.x, b.y, b.z, b.w},
-               r2[4] = {c.x, c.y, c.z, c.w}, r3[4] = {P.x, P.y, P.z, P.w};
-  // floating-point value and permanent of the same expansion (rows 0-1
-  // minors, then row 2, then row 3)
-  double m[4][4], pm[4][4];
-  for (int i = 0; i < 4; ++i)
-    for (int j = i + 1; j < 4; ++j) {
-      m[i][j] = r0[i] * r1[j] - r0[j] * r1[i];
-      pm[i][j] = fabs(r0[i] * r1[j]) + fabs(r0[j] * r1[i]);
-    }
-  auto d3 = [&](int i, int j, int k, double& perm) {
-    perm = fabs(r2[i]) * pm[j][k] + fabs(r2[j]) * pm[i][k] + fabs(r2[k]) * pm[i][j];
-    return r2[i] * m[j][k] - r2[j] * m[i][k] + r2[k] * m[i][j];
-  };
-  double p0, p1, p2, p3;
-  const double D0 = d3(1, 2, 3, p0), D1 = d3(0, 2, 3, p1), D2 = d3(0, 1, 3, p2),
-               D3 = d3(0, 1, 2, p3);
-  const double det = -r3[0] * D0 + r3[1] * D1 - r3[2] * D2 + r3[3] * D3;
-  const double perm = fabs(r3[0]) * p0 + fabs(r3[1]) * p1 + fabs(r3[2]) * p2 + fabs(r3[3]) * p3;
-  const double bound = kDetFilter * perm;
-  if (det > bound) return true;
-  if (det < -bound) return false;
+               r2[4] = {d.x, d.y, d.z, d.w}, r3[4] = {P.x, P.y, P.z, P.w};
   ++n_exact;
   return det4_sign_exact(r0, r1, r2, r3) >= 0;
 }
@@ -155,9 +147,12 @@ __device__ bool clip(HugeCell& C, const double4& P, uint32_t j, const double4& p
   int t = C.first_valid;
   C.first_valid = kEnd;
   double keep = 0.0;
+  const double pa1 = (fabs(P.x) + fabs(P.y) + fabs(P.z)) * 1.0001;
+  const double bw = Consts<double>::kDot * fabs(P.w) * 1.0001;
   while (t != kEnd) {
     const int next = C.t[t].w;
-    if (in_conflict(C, t, P, n_exact)) {
+    ++C.tests;
+    if (in_conflict(C, t, P, pa1, bw, n_exact)) {
       C.t[t].w = (uint16_t)(head | kConf);
       head = t;
       if (tail == kEnd) tail = t;
@@ -231,22 +226,25 @@ __device__ bool clip(HugeCell& C, const double4& P, uint32_t j, const double4& p
   return true;
 }
 
-// Certification as in the geometry kernel, in FP64 and one corner at a
-// time: for every corner, a best-bound octree search for the seed of least
-// power at the corner among those below the seed's own power there and not
-// in the candidate list; the distinct ones are the extra candidates.
-__device__ void certify(const HugeArgs& a, const HugeCell& C, uint32_t s, uint32_t row,
+// Certification as in the geometry kernel (FP32 with the same margins),
+// one corner at a time: for every corner, a best-bound octree search for
+// the seed of least power at the corner among those below the seed's own
+// power there and not in the candidate list; the distinct ones are the
+// extra candidates.
+__device__ void certify(const HugeArgs& a, HugeCell& C, uint32_t s, uint32_t row,
                         const double4& pi, double wi) {
   const SortedSeeds& S = a.S;
   const GridDesc& gd = *S.gd;
+  const float hf = gd.h_f;
   const uint32_t ncand = a.nbr_cnt[row] & kCntMask;
   uint32_t found = 0;
   bool more = false;
   uint32_t stk[96];
   for (int t = C.first_valid; t != kEnd; t = C.t[t].w) {
-    const double4 c = C.cor[t];
-    const double rho = c.w - wi;
-    double best = rho + 1e-12 * fabs(rho) + 1e-300;
+    const double4 cd = C.cor[t];
+    const float cx = (float)cd.x, cy = (float)cd.y, cz = (float)cd.z;
+    const float rho = (float)(cd.w - wi);
+    float best = rho + 1e-5f * fabsf(rho) + 1e-7f;
     uint32_t bj = kNone;
     int sp = 0;
     stk[sp++] = 0u;
@@ -258,25 +256,27 @@ __device__ void certify(const HugeArgs& a, const HugeCell& C, uint32_t s, uint32
       const uint32_t b = S.cell_start[code << (3 * shift)];
       const uint32_t en = S.cell_start[(code + 1u) << (3 * shift)];
       if (b == en) continue;
-      const double WB = a.node_wmax[node_offset(lev) + code];
-      const double side = gd.h * (double)(1u << shift);
-      const double bx = gd.lo[0] + (double)compact3(code) * side;
-      const double by = gd.lo[1] + (double)compact3(code >> 1) * side;
-      const double bz = gd.lo[2] + (double)compact3(code >> 2) * side;
-      const double pad = 1e-12 * (1.0 + fabs(bx) + fabs(by) + fabs(bz)) + 1e-9 * side;
-      const double dx = fmax(fmax(bx - pad - c.x, c.x - (bx + side + pad)), 0.0);
-      const double dy = fmax(fmax(by - pad - c.y, c.y - (by + side + pad)), 0.0);
-      const double dz = fmax(fmax(bz - pad - c.z, c.z - (bz + side + pad)), 0.0);
-      const double d2 = dx * dx + dy * dy + dz * dz;
-      if (d2 - WB >= best + 1e-10 * (fabs(best) + fabs(WB) + d2)) continue;
+      ++C.nodes;
+      const float WB = (float)a.node_wmax[node_offset(lev) + code];
+      const float side = hf * (float)(1u << shift);
+      const float bx = gd.lo_f[0] + (float)compact3(code) * side;
+      const float by = gd.lo_f[1] + (float)compact3(code >> 1) * side;
+      const float bz = gd.lo_f[2] + (float)compact3(code >> 2) * side;
+      const float pad = 1e-6f * (1.f + fabsf(bx) + fabsf(by) + fabsf(bz)) + 1e-5f * side;
+      const float dx = fmaxf(fmaxf(bx - pad - cx, cx - (bx + side + pad)), 0.f);
+      const float dy = fmaxf(fmaxf(by - pad - cy, cy - (by + side + pad)), 0.f);
+      const float dz = fmaxf(fmaxf(bz - pad - cz, cz - (bz + side + pad)), 0.f);
+      const float d2 = dx * dx + dy * dy + dz * dz;
+      if (d2 >= (best + WB) + 1e-5f * (fabsf(best) + fabsf(WB) + d2) + 1e-7f) continue;
       if (en - b <= 32u || lev == gd.L) {
+        C.seeds += en - b;
         for (uint32_t jn = b; jn < en; ++jn) {
           if (jn == s) continue;
           const double4 pj = S.xd[jn];
           if (pj.x == pi.x && pj.y == pi.y && pj.z == pi.z) continue;
-          const double wj = S.ws ? S.ws[jn] : 0.0;
-          const double ex = c.x - pj.x, ey = c.y - pj.y, ez = c.z - pj.z;
-          const double d = ex * ex + ey * ey + ez * ez - wj;
+          const float wj = S.ws ? (float)S.ws[jn] : 0.f;
+          const float ex = cx - (float)pj.x, ey = cy - (float)pj.y, ez = cz - (float)pj.z;
+          const float d = ex * ex + ey * ey + ez * ez - wj;
           if (!(d < best)) continue;
           bool member = false;
           for (uint32_t k = 0; k < ncand && !member; ++k)
@@ -291,8 +291,33 @@ __device__ void certify(const HugeArgs& a, const HugeCell& C, uint32_t s, uint32
         more = true;
         break;
       }
-      for (int ch = 7; ch >= 0; --ch)
-        stk[sp++] = (((code << 3) | (uint32_t)ch) << 4) | (uint32_t)(lev + 1);
+      // children by their lower bound on the power at c, the most promising
+      // popped first; children that cannot improve are not pushed
+      float lb[8];
+      int ord[8], nk = 0;
+      const float cs = 0.5f * side;
+      for (int ch = 0; ch < 8; ++ch) {
+        const uint32_t cc = (code << 3) | (uint32_t)ch;
+        const int csh = shift - 1;
+        if (S.cell_start[cc << (3 * csh)] == S.cell_start[(cc + 1u) << (3 * csh)]) continue;
+        const float qx = bx + (float)(ch & 1) * cs, qy = by + (float)((ch >> 1) & 1) * cs,
+                    qz = bz + (float)((ch >> 2) & 1) * cs;
+        const float ex = fmaxf(fmaxf(qx - pad - cx, cx - (qx + cs + pad)), 0.f);
+        const float ey = fmaxf(fmaxf(qy - pad - cy, cy - (qy + cs + pad)), 0.f);
+        const float ez = fmaxf(fmaxf(qz - pad - cz, cz - (qz + cs + pad)), 0.f);
+        const float v = ex * ex + ey * ey + ez * ez -
+                        (float)a.node_wmax[node_offset(lev + 1) + cc];
+        int q = nk++;
+        while (q > 0 && lb[q - 1] < v) {  // descending: the smallest is pushed last
+          lb[q] = lb[q - 1];
+          ord[q] = ord[q - 1];
+          --q;
+        }
+        lb[q] = v;
+        ord[q] = ch;
+      }
+      for (int k = 0; k < nk; ++k)
+        stk[sp++] = (((code << 3) | (uint32_t)ord[k]) << 4) | (uint32_t)(lev + 1);
     }
     if (bj == kNone) continue;
     bool dup = false;
@@ -306,8 +331,10 @@ __device__ void certify(const HugeArgs& a, const HugeCell& C, uint32_t s, uint32
   a.extra_cnt[row] = (found < a.max_extra ? found : a.max_extra) | (more ? 0x80000000u : 0u);
 }
 
-__global__ void __launch_bounds__(32) huge_kernel(HugeArgs a) {
-  const uint32_t qi = blockIdx.x * blockDim.x + threadIdx.x;
+// One cell per block of one thread: cells walk different lists, and the
+// threads of a warp would run their divergent walks one after the other.
+__global__ void __launch_bounds__(1) huge_kernel(HugeArgs a) {
+  const uint32_t qi = blockIdx.x;
   if (qi >= a.nq) return;
   const SortedSeeds& S = a.S;
   const uint32_t s = a.qlist[qi];
@@ -316,6 +343,7 @@ __global__ void __launch_bounds__(32) huge_kernel(HugeArgs a) {
   C.t = a.scr_t + (size_t)qi * kHugeT;
   C.adj = a.scr_adj + (size_t)qi * kHugeT;
   C.cor = a.scr_cor + (size_t)qi * kHugeT;
+  C.eps = a.scr_eps + (size_t)qi * kHugeT;
   C.pl = a.scr_pl + (size_t)qi * kHugeV;
   C.vg = a.scr_vg + (size_t)qi * kHugeV;
   C.v2t = a.scr_v2t + (size_t)qi * kHugeV;
@@ -323,6 +351,8 @@ __global__ void __launch_bounds__(32) huge_kernel(HugeArgs a) {
   const double4 pi = S.xd[s];
   const double qi_ = S.q[s];
   const double hi2 = __dmul_rn(pi.w, pi.w);
+  C.tests = C.nodes = C.seeds = 0;
+  const long long c0 = clock64();
   init_box(C, a.box, pi);
   double R2 = 0.0;
   for (int t = C.first_valid; t != kEnd; t = C.t[t].w) R2 = fmax(R2, C.cor[t].w);
@@ -369,6 +399,15 @@ __global__ void __launch_bounds__(32) huge_kernel(HugeArgs a) {
   }
   a.status[s] = st;
   a.nclip[s] = jj;
+  const long long c1 = clock64();
+  if (a.stats) {
+    unsigned long long* o = a.stats + (size_t)qi * kHugeStats;
+    o[0] = (unsigned long long)(c1 - c0);
+    o[3] = jj;
+    o[4] = C.tests;
+    o[5] = (unsigned long long)C.nb_t;
+    o[6] = (unsigned long long)C.nb_v;
+  }
   if (st == CELL_OVERFLOW || st == CELL_NEED_MORE_K) return;
 
   // ---- geometry: compute_geometry, compute_mg, facet_area
@@ -448,14 +487,22 @@ __global__ void __launch_bounds__(32) huge_kernel(HugeArgs a) {
   a.nf[s] = nfac | kHugeFacets;
   a.hp_nbr[s] = fn;
   a.hp_area[s] = fa;
+  const long long c2 = clock64();
   if (a.node_wmax) certify(a, C, s, row, pi, S.ws ? S.ws[s] : 0.0);
+  if (a.stats) {
+    unsigned long long* o = a.stats + (size_t)qi * kHugeStats;
+    o[1] = (unsigned long long)(c2 - c1);
+    o[2] = (unsigned long long)(clock64() - c2);
+    o[7] = C.nodes;
+    o[8] = C.seeds;
+  }
 }
 
 }  // namespace
 
 void launch_huge(const HugeArgs& a, cudaStream_t st) {
   if (a.nq == 0) return;
-  huge_kernel<<<(a.nq + 31) / 32, 32, 0, st>>>(a);
+  huge_kernel<<<a.nq, 1, 0, st>>>(a);
   count_launch();
   last_launch_error = cudaGetLastError();
 }

@@ -228,6 +228,9 @@ typedef struct {
     uint32_t reserved;
     /* CG stops at ||r|| <= cg_rtol ||b|| (default and 0: 1e-3) */
     double cg_rtol;
+    /* the line search of a Newton step starts at min(1, step_growth * the
+     * previous step) (default 4); 0: always at 1 */
+    double step_growth;
 } gbv_ot_options;
 
 typedef struct {

@@ -20,7 +20,8 @@ oracle's cells, which are pinned to the reference's ConvexCell:
   Newton      solve H x = nu - vol by Jacobi-preconditioned CG in FP64 to
               a relative residual of 1e-3, halve the step until every cell
               keeps at least eps0 and the residual norm drops by
-              (1 - alpha / 2)
+              (1 - alpha / 2), the first trial being min(1, 4 x the
+              previous step)
 
 Parity for optimal transport is unpinned: the reference's solver and its
 test data are absent.  What pins it here is structure: the Hessian against
@@ -103,7 +104,7 @@ def pcg(H, b: np.ndarray, rtol: float, max_iter: int):
 
 def newton(xyz: np.ndarray, nu: np.ndarray | None = None, w0: np.ndarray | None = None,
            tol: float = 1e-6, max_newton: int = 60, max_cg: int = 4000, nthreads: int = 4,
-           cg_rtol: float = 1e-3):
+           cg_rtol: float = 1e-3, step_growth: float = 4.0):
     """Damped Newton from w0 (zeros) to max_i |vol_i - nu_i| / nu_i < tol.
 
     Returns (w, info) with info = dict(iters, converged, mass_error_inf,
@@ -117,12 +118,13 @@ def newton(xyz: np.ndarray, nu: np.ndarray | None = None, w0: np.ndarray | None 
     err = np.max(np.abs(r) / nu)
     eps0 = 0.5 * min(nu.min(), c["vol"].min())
     it = 0
+    alpha_prev = 1.0
     while err >= tol and it < max_newton:
         it += 1
         H = hessian(xyz, c)
         b = -(r - r.mean())
         x, _ = pcg(H, b, cg_rtol, max_cg)
-        alpha = 1.0
+        alpha = min(1.0, step_growth * alpha_prev) if step_growth > 0 else 1.0
         for _ in range(30):
             wt = w + alpha * x
             ct = laguerre_cells(xyz, wt, nthreads)
@@ -131,6 +133,7 @@ def newton(xyz: np.ndarray, nu: np.ndarray | None = None, w0: np.ndarray | None 
             if ct["vol"].min() >= eps0 and \
                     np.linalg.norm(rt) <= (1.0 - 0.5 * alpha) * np.linalg.norm(r):
                 w, c, r = wt, ct, rt
+                alpha_prev = alpha
                 break
             alpha *= 0.5
         else:
