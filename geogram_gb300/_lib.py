@@ -76,6 +76,10 @@ class OtReport(ctypes.Structure):
         ("ms_total", ctypes.c_double),
         ("ms_cells", ctypes.c_double),
         ("ms_linear", ctypes.c_double),
+        ("start_scale", ctypes.c_double),
+        ("ms_start", ctypes.c_double),
+        ("start_cg_iters", ctypes.c_uint32),
+        ("reserved2", ctypes.c_uint32),
     ]
 
     def as_dict(self) -> dict:
@@ -138,8 +142,25 @@ SIGNATURES = {
     "gbv_ot_gradient_hessian": (ctypes.c_int, [_P, _P, _P, _P, _U32, ctypes.POINTER(OtOptions),
                                                _P, _P, _P, _P, _P, ctypes.c_uint64,
                                                ctypes.POINTER(ctypes.c_uint64)]),
+    "gbv_mlp_features": (ctypes.c_int, [_P, _P, _U32, _P, _P]),
+    "gbv_mlp_forward": (ctypes.c_int, [_P, _P, _P, _P, _U32, _P, _P]),
+    "gbv_mlp_loss_grad": (ctypes.c_int, [_P, _P, _P, _P, _P, _U32, _P,
+                                         ctypes.POINTER(ctypes.c_double), _P]),
+    "gbv_mlp_adam": (ctypes.c_int, [_P, _P, _P, _P, _P, _U32, ctypes.c_float, ctypes.c_float,
+                                    ctypes.c_float, ctypes.c_float, _P]),
+    "gbv_ot_warm_start": (ctypes.c_int, [_P, _P, _U32, ctypes.POINTER(OtOptions), _P, _P, _P,
+                                         _P]),
+    "gbv_ot_solve_learned_device": (ctypes.c_int, [_P, _P, _P, _U32, ctypes.POINTER(OtOptions),
+                                                   _P, _P, _P, _P, ctypes.POINTER(OtReport)]),
+    "gbv_mlp_gemm_nt": (ctypes.c_int, [_P, _P, ctypes.c_int, _P, ctypes.c_int, _P, ctypes.c_int,
+                                       ctypes.c_int, ctypes.c_int, ctypes.c_int, _P]),
     "gbv_knn_noalloc": (ctypes.c_int, [_P, _U32, _U32, _U32, _U32, _P, _P, _P]),
 }
+
+MLP_INPUTS = 19
+MLP_PARAMS = 37377
+MLP_NORM = 40
+MLP_MAX_BATCH = 65536
 
 _lib = None
 _lock = threading.Lock()

@@ -29,6 +29,7 @@
 
 #include "gbv_clip.cuh"
 #include "gbv_ot.cuh"
+#include "gbv_mlp.cuh"
 
 namespace {
 
@@ -1026,7 +1027,10 @@ static bool laguerre_device(gbv_context* c, const double* d_xyz, const double* d
     if (std::getenv("GBV_OT_LOG"))
       std::fprintf(stderr, "[ot]   round %d: %u cells with extra candidates (room %u)\n", round, m,
                    P.max_extra);
-    if (round >= 24) throw StatusError{GBV_ERR_NOT_CONVERGED, "certification did not settle"};
+    if (round >= 32)
+      throw StatusError{GBV_ERR_NOT_CONVERGED,
+                        "certification did not settle: " + std::to_string(m) +
+                            " cell(s) still found candidates after 32 rounds"};
     const std::string tag = std::to_string(round & 1);
     const uint32_t newk = cur.k + P.max_extra;
     uint32_t* q_s = c->buf<uint32_t>("lag_q" + tag, m);
@@ -1057,6 +1061,75 @@ static bool laguerre_device(gbv_context* c, const double* d_xyz, const double* d
   }
   GBV_CUDA(cudaGetLastError());
   return true;
+}
+
+// ---------------------------------------------------------------------
+// Learned warm start: buffers and features
+// ---------------------------------------------------------------------
+static MlpBuffers mlp_buffers(gbv_context* c, uint32_t rows) {
+  const size_t r = (size_t)(rows + 31) / 32 * 32;
+  const size_t e = r * kMlpHid;
+  MlpBuffers B;
+  B.xn = c->buf<bf16>("mlp_xn", r * kMlpInPad);
+  B.h1 = c->buf<bf16>("mlp_h1", e);
+  B.h2 = c->buf<bf16>("mlp_h2", e);
+  B.h3 = c->buf<bf16>("mlp_h3", e);
+  B.z1 = c->buf<float>("mlp_z1", e);
+  B.z2 = c->buf<float>("mlp_z2", e);
+  B.z3 = c->buf<float>("mlp_z3", e);
+  B.acc = c->buf<float>("mlp_acc", e);
+  B.y = c->buf<float>("mlp_y", r);
+  B.dy = c->buf<float>("mlp_dy", r);
+  B.dz = c->buf<float>("mlp_dz", e);
+  B.dzb = c->buf<bf16>("mlp_dzb", e);
+  B.dzt = c->buf<bf16>("mlp_dzt", e);
+  B.ht = c->buf<bf16>("mlp_ht", e);
+  B.part = c->buf<float>("mlp_part", mlp_part_floats());
+  B.w1b = c->buf<bf16>("mlp_w1b", kMlpHid * kMlpInPad);
+  B.w2b = c->buf<bf16>("mlp_w2b", kMlpHid * kMlpHid);
+  B.w3b = c->buf<bf16>("mlp_w3b", kMlpHid * kMlpHid);
+  B.w1t = c->buf<bf16>("mlp_w1t", kMlpHid * kMlpInPad);
+  B.w2t = c->buf<bf16>("mlp_w2t", kMlpHid * kMlpHid);
+  B.w3t = c->buf<bf16>("mlp_w3t", kMlpHid * kMlpHid);
+  B.lpart = c->buf<double>("mlp_lpart", kMlpLossParts);
+  return B;
+}
+
+// Raw features of n seeds (device, caller order); uses the context's grid.
+static void mlp_features_device(gbv_context* c, const double* d_xyz, uint32_t n, float* d_raw,
+                                cudaStream_t st) {
+  if (n < 17) throw StatusError{GBV_ERR_INVALID_ARGUMENT, "the features need n >= 17"};
+  setup_seeds(c, n, false);
+  c->nn_ready = false;
+  c->has_cells = false;
+  SortedSeeds& S = c->S;
+  build_grid(d_xyz, 3, 3, nullptr, n, S.L, S, c->scr, st);
+  uint32_t* oi = c->buf<uint32_t>("mlp_knn_i", (size_t)n * 17);
+  double* od = c->buf<double>("mlp_knn_d", (size_t)n * 17);
+  KnnArgs ka{};
+  ka.S = &S;
+  ka.nq = n;
+  ka.k = 17;
+  ka.mode = KNN_ALL;
+  ka.exp_idx = oi;
+  ka.exp_d2 = od;
+  ka.flag_count = c->buf<uint32_t>("knn_flag_count", 1);
+  ka.flag_list = c->buf<uint32_t>("nn_flag_list", n);
+  launch_knn(ka, st);
+  mlp_features(d_xyz, od, n, d_raw, st);
+  GBV_CUDA(cudaGetLastError());
+}
+
+static void mlp_forward_all(gbv_context* c, const float* params, const float* norm,
+                            const float* raw, uint32_t n, float* y, cudaStream_t st) {
+  const uint32_t cap = std::min<uint32_t>(n, kMlpChunk);
+  MlpBuffers B = mlp_buffers(c, cap);
+  for (uint32_t off = 0; off < n; off += kMlpChunk) {
+    const uint32_t rows = std::min<uint32_t>(kMlpChunk, n - off);
+    mlp_forward(params, norm, raw + (size_t)off * kMlpIn, rows, B, false, st);
+    GBV_CUDA(cudaMemcpyAsync(y + off, B.y, sizeof(float) * rows, cudaMemcpyDeviceToDevice, st));
+  }
+  GBV_CUDA(cudaGetLastError());
 }
 
 // ---------------------------------------------------------------------
@@ -1113,6 +1186,11 @@ struct OtWork {
     r2 = S + C;
   }
 };
+
+__global__ void mul_kernel(double* __restrict__ y, const double* __restrict__ x, uint32_t n) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] *= x[i];
+}
 
 __global__ void fill_kernel(double* __restrict__ y, double v, uint32_t n) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1173,8 +1251,16 @@ static Hessian current_hessian(gbv_context* c, const double* xyz, uint32_t n, cu
   return H;
 }
 
+// Learned start (params non-null): the network predicts t_i = (H0 w*)_i /
+// vol_i(0), the Hessian at zero weights applied to the optimal weights over
+// the zero-weight cell volume -- the cell-averaged Laplacian of the
+// potential, by the Monge-Ampere relation a function of the local density,
+// which its inputs see -- and the start solves H0 w = t vol(0).  An exact t
+// would give w* itself; errors in t come out smoothed by the inverse
+// Laplacian instead of as seed-to-seed noise, which would empty cells.
 static void ot_solve(gbv_context* c, const double* xyz, const double* nu_in, uint32_t n,
-                     const gbv_ot_options& o, double* w, cudaStream_t st, gbv_ot_report* rep) {
+                     const gbv_ot_options& o, double* w, cudaStream_t st, gbv_ot_report* rep,
+                     const float* params = nullptr, const float* norm = nullptr) {
   if (n < 2) throw StatusError{GBV_ERR_INVALID_ARGUMENT, "n must be >= 2"};
   const auto t0 = std::chrono::steady_clock::now();
   double ms_cells = 0.0, ms_lin = 0.0;
@@ -1200,6 +1286,36 @@ static void ot_solve(gbv_context* c, const double* xyz, const double* nu_in, uin
   double* wt = c->buf<double>("ot_wt", n);
   fill_kernel<<<nblocks(n, 256), 256, 0, st>>>(ones, 1.0, n); count_launch();
   const double nu_norm = std::sqrt(W.dot(nu, nu));
+  // x = H^+ b by Jacobi-preconditioned CG; b (overwritten: the residual) is
+  // first projected on mean zero (H has the constants as kernel), and so
+  // is x at the end.  Returns the iterations.
+  auto pcg = [&](const Hessian& H, double* b, double tol) -> uint32_t {
+    const double mean = W.dot(b, ones) / n;
+    add_scalar(b, -mean, n, st);
+    const double bnorm = std::sqrt(W.dot(b, b));
+    GBV_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, st));
+    cg_precond(b, H.diag, z, n, st);
+    GBV_CUDA(cudaMemcpyAsync(p, z, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+    double rz = W.dot(b, z);
+    uint32_t k = 0;
+    while (k < o.max_cg) {
+      spmv_dot(H, p, Ap, W.part, kOtParts, st);
+      const double pAp = W.fetch_sum();
+      if (!(pAp > 0.0)) break;
+      const double alpha = rz / pAp;
+      cg_update_xr(x, b, p, Ap, alpha, n, st);
+      ++k;
+      const double rnorm = std::sqrt(W.dot(b, b));
+      if (rnorm <= tol * bnorm) break;
+      cg_precond(b, H.diag, z, n, st);
+      const double rz_new = W.dot(b, z);
+      cg_update_p(p, z, rz_new / rz, n, st);
+      rz = rz_new;
+    }
+    const double xmean = W.dot(x, ones) / n;
+    add_scalar(x, -xmean, n, st);
+    return k;
+  };
 
   uint32_t *adj_rp = nullptr, *adj_ix = nullptr;
   uint32_t cell_calls = 0, cg_total = 0, halvings = 0, it = 0;
@@ -1211,9 +1327,6 @@ static void ot_solve(gbv_context* c, const double* xyz, const double* nu_in, uin
     ms_cells += now_ms(tc);
     return done;
   };
-  cells(w, false);
-  double r2, rel_inf, vmin;
-  W.residual_stats(c->vol, nu, r, r2, rel_inf, vmin);
   double nu_min = DBL_MAX;
   {
     // min nu through the residual of ones * nu: reuse the min-vol slot
@@ -1221,39 +1334,66 @@ static void ot_solve(gbv_context* c, const double* xyz, const double* nu_in, uin
     W.residual_stats(nu, ones, Ap, a, b2, m);
     nu_min = m;
   }
-  const double eps0 = 0.5 * std::min(nu_min, vmin);
+  double ms_start = 0.0;
+  uint32_t start_cg = 0;
+  if (params) {
+    const auto ts = std::chrono::steady_clock::now();
+    GBV_CUDA(cudaMemsetAsync(w, 0, sizeof(double) * n, st));
+    cells(w, false);
+    Hessian H0 = current_hessian(c, xyz, n, st);
+    float* raw = c->buf<float>("ws_raw", (size_t)n * kMlpIn);
+    float* y = c->buf<float>("ws_y", n);
+    // b_i = t_i vol_i(0): the network predicts the cell-averaged Laplacian
+    double* vol0 = c->buf<double>("ws_vol0", n);
+    GBV_CUDA(cudaMemcpyAsync(vol0, c->vol, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+    mlp_features_device(c, xyz, n, raw, st);
+    mlp_forward_all(c, params, norm, raw, n, y, st);
+    mlp_denorm(y, norm, n, rr, st);
+    mul_kernel<<<nblocks(n, 256), 256, 0, st>>>(rr, vol0, n); count_launch();
+    start_cg = pcg(H0, rr, 1e-6);
+    GBV_CUDA(cudaMemcpyAsync(w, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+    ms_start = now_ms(ts);
+    if (ot_log_enabled())
+      std::fprintf(stderr, "[ot] learned start: %.1f ms, %u CG iterations\n", ms_start, start_cg);
+  }
+  // The damped Newton method needs a start whose cells all have volume.
+  // A given start (a warm start) whose cells fall below start_min is
+  // scaled toward zero, halving, and replaced by zeros after 10 halvings.
+  const double start_min = 1e-4 * nu_min;
+  const bool nonzero_start = std::sqrt(W.dot(w, w)) > 0.0;
+  double start_scale = 1.0;
+  double r2, rel_inf, vmin;
+  if (nonzero_start) {
+    for (int k = 0;; ++k) {
+      if (cells(w, false, start_min)) {
+        W.residual_stats(c->vol, nu, r, r2, rel_inf, vmin);
+        if (vmin >= start_min) break;
+      }
+      if (k == 10) {
+        GBV_CUDA(cudaMemsetAsync(w, 0, sizeof(double) * n, st));
+        start_scale = 0.0;
+        break;
+      }
+      scale_copy(w, w, 0.5, n, st);
+      start_scale *= 0.5;
+    }
+    if (ot_log_enabled()) std::fprintf(stderr, "[ot] start scaled by %g\n", start_scale);
+  }
+  if (!nonzero_start || start_scale == 0.0) {
+    cells(w, false);
+    W.residual_stats(c->vol, nu, r, r2, rel_inf, vmin);
+  }
+  // a start with an empty cell (duplicated seeds) still gets a positive floor
+  const double eps0 = vmin > 0.0 ? 0.5 * std::min(nu_min, vmin) : 1e-6 * nu_min;
   bool converged = rel_inf < o.tol;
   double alpha_prev = 1.0;
   for (it = 0; it < o.max_newton && !converged; ++it) {
     save_adjacency(c, n, st, &adj_rp, &adj_ix);
     const auto tl = std::chrono::steady_clock::now();
     Hessian H = current_hessian(c, xyz, n, st);
-    // b = -(vol - nu), projected on mean zero (H has the constants as kernel)
+    // b = -(vol - nu)
     scale_copy(rr, r, -1.0, n, st);
-    const double mean = W.dot(rr, ones) / n;
-    add_scalar(rr, -mean, n, st);
-    const double bnorm = std::sqrt(W.dot(rr, rr));
-    const double eta = o.cg_rtol > 0.0 ? o.cg_rtol : 1e-3;
-    GBV_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, st));
-    cg_precond(rr, H.diag, z, n, st);
-    GBV_CUDA(cudaMemcpyAsync(p, z, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
-    double rz = W.dot(rr, z);
-    for (uint32_t k = 0; k < o.max_cg; ++k) {
-      spmv_dot(H, p, Ap, W.part, kOtParts, st);
-      const double pAp = W.fetch_sum();
-      if (!(pAp > 0.0)) break;
-      const double alpha = rz / pAp;
-      cg_update_xr(x, rr, p, Ap, alpha, n, st);
-      ++cg_total;
-      const double rnorm = std::sqrt(W.dot(rr, rr));
-      if (rnorm <= eta * bnorm) break;
-      cg_precond(rr, H.diag, z, n, st);
-      const double rz_new = W.dot(rr, z);
-      cg_update_p(p, z, rz_new / rz, n, st);
-      rz = rz_new;
-    }
-    const double xmean = W.dot(x, ones) / n;
-    add_scalar(x, -xmean, n, st);
+    cg_total += pcg(H, rr, o.cg_rtol > 0.0 ? o.cg_rtol : 1e-3);
     ms_lin += now_ms(tl);
     // damped step (Kitagawa-Merigot-Thibert): halve until every cell keeps
     // at least eps0 and the residual drops by (1 - alpha / 2); the first
@@ -1311,6 +1451,9 @@ static void ot_solve(gbv_context* c, const double* xyz, const double* nu_in, uin
     rep->ms_total = now_ms(t0);
     rep->ms_cells = ms_cells;
     rep->ms_linear = ms_lin;
+    rep->start_scale = start_scale;
+    rep->ms_start = ms_start;
+    rep->start_cg_iters = start_cg;
   }
 }
 
@@ -1600,6 +1743,114 @@ gbv_status gbv_nn_get_nearest_neighbors_all(gbv_context* c, uint32_t k, uint32_t
     launch_knn(ka, st);
     GBV_CUDA(cudaMemcpyAsync(idx, oi, 4 * (size_t)n * k, cudaMemcpyDeviceToHost, st));
     if (d2) GBV_CUDA(cudaMemcpyAsync(d2, od, 8 * (size_t)n * k, cudaMemcpyDeviceToHost, st));
+    GBV_CUDA(cudaStreamSynchronize(st));
+    GBV_CUDA(cudaGetLastError());
+  });
+}
+
+gbv_status gbv_mlp_features(gbv_context* c, const double* d_xyz, uint32_t n, float* d_raw,
+                            void* stream) {
+  if (!c || !d_xyz || !d_raw) return fail(GBV_ERR_INVALID_ARGUMENT, "NULL argument");
+  return guarded([&] {
+    GBV_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    mlp_features_device(c, d_xyz, n, d_raw, st);
+    GBV_CUDA(cudaStreamSynchronize(st));
+  });
+}
+
+gbv_status gbv_mlp_forward(gbv_context* c, const float* d_params, const float* d_norm,
+                           const float* d_raw, uint32_t n, float* d_y, void* stream) {
+  if (!c || !d_params || !d_norm || !d_raw || !d_y)
+    return fail(GBV_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (n == 0) return fail(GBV_ERR_INVALID_ARGUMENT, "n must be > 0");
+  return guarded([&] {
+    GBV_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    mlp_forward_all(c, d_params, d_norm, d_raw, n, d_y, st);
+    GBV_CUDA(cudaStreamSynchronize(st));
+  });
+}
+
+gbv_status gbv_mlp_loss_grad(gbv_context* c, const float* d_params, const float* d_norm,
+                             const float* d_raw, const float* d_target, uint32_t n,
+                             float* d_grad, double* loss, void* stream) {
+  if (!c || !d_params || !d_norm || !d_raw || !d_target || !d_grad)
+    return fail(GBV_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (n == 0 || n > kMlpChunk)
+    return fail(GBV_ERR_INVALID_ARGUMENT, "batch must hold 1 to GBV_MLP_MAX_BATCH rows");
+  return guarded([&] {
+    GBV_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    MlpBuffers B = mlp_buffers(c, n);
+    mlp_loss_grad(d_params, d_norm, d_raw, d_target, n, d_grad, B, st);
+    double hp[kMlpLossParts];
+    GBV_CUDA(cudaMemcpyAsync(hp, B.lpart, sizeof(hp), cudaMemcpyDeviceToHost, st));
+    GBV_CUDA(cudaStreamSynchronize(st));
+    double s = 0.0;
+    for (double v : hp) s += v;
+    if (loss) *loss = s;
+    GBV_CUDA(cudaGetLastError());
+  });
+}
+
+gbv_status gbv_mlp_adam(gbv_context* c, float* d_params, float* d_m, float* d_v,
+                        const float* d_grad, uint32_t step, float lr, float beta1, float beta2,
+                        float eps, void* stream) {
+  if (!c || !d_params || !d_m || !d_v || !d_grad)
+    return fail(GBV_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (step == 0) return fail(GBV_ERR_INVALID_ARGUMENT, "step counts from 1");
+  return guarded([&] {
+    GBV_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    mlp_adam(d_params, d_m, d_v, d_grad, step, lr, beta1, beta2, eps, st);
+    GBV_CUDA(cudaGetLastError());
+  });
+}
+
+gbv_status gbv_ot_warm_start(gbv_context* c, const double* d_xyz, uint32_t n,
+                             const gbv_ot_options* opt, const float* d_params,
+                             const float* d_norm, double* d_w, void* stream) {
+  if (!c || !d_xyz || !d_params || !d_norm || !d_w)
+    return fail(GBV_ERR_INVALID_ARGUMENT, "NULL argument");
+  gbv_status s = check_ot_opts(opt);
+  if (s != GBV_OK) return s;
+  return guarded([&] {
+    GBV_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    gbv_ot_options o = *opt;
+    o.max_newton = 0;
+    ot_solve(c, d_xyz, nullptr, n, o, d_w, st, nullptr, d_params, d_norm);
+  });
+}
+
+gbv_status gbv_ot_solve_learned_device(gbv_context* c, const double* d_xyz, const double* d_nu,
+                                       uint32_t n, const gbv_ot_options* opt,
+                                       const float* d_params, const float* d_norm, double* d_w,
+                                       void* stream, gbv_ot_report* report) {
+  if (!c || !d_xyz || !d_params || !d_norm || !d_w)
+    return fail(GBV_ERR_INVALID_ARGUMENT, "NULL argument");
+  gbv_status s = check_ot_opts(opt);
+  if (s != GBV_OK) return s;
+  return guarded([&] {
+    GBV_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    ot_solve(c, d_xyz, d_nu, n, *opt, d_w, st, report, d_params, d_norm);
+  });
+}
+
+gbv_status gbv_mlp_gemm_nt(gbv_context* c, const void* d_a, int lda, const void* d_bt, int ldb,
+                           float* d_c, int ldc, int M, int N, int K, void* stream) {
+  if (!c || !d_a || !d_bt || !d_c) return fail(GBV_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (M <= 0 || N <= 0 || K <= 0 || K % 32 || lda % 8 || ldb % 8 || lda < K || ldb < K ||
+      ldc < N)
+    return fail(GBV_ERR_INVALID_ARGUMENT, "bad GEMM shape");
+  if (((uintptr_t)d_a | (uintptr_t)d_bt) & 15)
+    return fail(GBV_ERR_INVALID_ARGUMENT, "operands must be 16-byte aligned");
+  return guarded([&] {
+    GBV_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    gemm_nt((const bf16*)d_a, lda, (const bf16*)d_bt, ldb, d_c, ldc, M, N, K, 1, 0, st);
     GBV_CUDA(cudaStreamSynchronize(st));
     GBV_CUDA(cudaGetLastError());
   });

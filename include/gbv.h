@@ -244,6 +244,12 @@ typedef struct {
     double mass_error_l2;     /* ||vol - nu|| / ||nu|| at the end */
     double min_volume;
     double ms_total, ms_cells, ms_linear;
+    /* the given start was multiplied by this so that every cell keeps at
+     * least 1e-4 min(nu) (1: used as given, 0: replaced by zeros) */
+    double start_scale;
+    double ms_start;          /* learned start: features, network and solve */
+    uint32_t start_cg_iters;  /* learned start: CG iterations of its solve */
+    uint32_t reserved2;
 } gbv_ot_report;
 
 void gbv_ot_options_default(gbv_ot_options* opt);
@@ -270,6 +276,63 @@ gbv_status gbv_ot_gradient_hessian(gbv_context* ctx, const double* xyz, const do
                                    double* g, uint32_t* h_rowptr, uint32_t* h_col,
                                    double* h_val, double* h_diag, uint64_t h_capacity,
                                    uint64_t* nnz);
+
+/* ---------------------------------------------------------------- */
+/* Learned warm start for gbv_ot_solve.  No counterpart in the        */
+/* reference: the reference's solver starts from zero weights (or     */
+/* from a coarser level).  A small MLP predicts each seed's weight    */
+/* from its position and the distances to its 16 nearest seeds; its   */
+/* forward and backward passes run on the tensor cores (BF16 in,      */
+/* FP32 accumulation).  All pointers are device pointers.             */
+/* ---------------------------------------------------------------- */
+
+#define GBV_MLP_INPUTS 19
+/* FP32 parameters: W1[128][32] (inputs padded to 32 columns, the padding
+ * kept at zero), b1[128], W2[128][128], b2[128], W3[128][128], b3[128],
+ * W4[128], b4 */
+#define GBV_MLP_PARAMS 37377
+/* normalisation: input mean[19], input std[19], output mean, output std */
+#define GBV_MLP_NORM 40
+/* rows per gbv_mlp_loss_grad call */
+#define GBV_MLP_MAX_BATCH 65536u
+
+/* Raw features [n][19] of the seeds d_xyz [n][3]: x, y, z, then the 16
+ * nearest distances to other seeds times n^(1/3), ascending.  n >= 17. */
+gbv_status gbv_mlp_features(gbv_context* ctx, const double* d_xyz, uint32_t n, float* d_raw,
+                            void* stream);
+/* Network output (standardised) for n rows of raw features. */
+gbv_status gbv_mlp_forward(gbv_context* ctx, const float* d_params, const float* d_norm,
+                           const float* d_raw, uint32_t n, float* d_y, void* stream);
+/* Gradient (FP32, layout of the parameters) of the mean squared error
+ * between the output and the standardised targets (d_target are weights;
+ * the normalisation maps them); *loss receives the error.  n <=
+ * GBV_MLP_MAX_BATCH. */
+gbv_status gbv_mlp_loss_grad(gbv_context* ctx, const float* d_params, const float* d_norm,
+                             const float* d_raw, const float* d_target, uint32_t n,
+                             float* d_grad, double* loss, void* stream);
+/* One Adam step (bias-corrected) on the parameters; step counts from 1. */
+gbv_status gbv_mlp_adam(gbv_context* ctx, float* d_params, float* d_m, float* d_v,
+                        const float* d_grad, uint32_t step, float lr, float beta1, float beta2,
+                        float eps, void* stream);
+/* The learned start: cells and Hessian H0 at zero weights, the network's
+ * prediction of t_i = (H0 w*)_i / vol_i(0) (the cell-averaged Laplacian of
+ * the optimal weights; by the Monge-Ampere relation a function of the local
+ * density its inputs see), then w = H0^+ (t vol(0)) by conjugate gradient,
+ * scaled toward zero if a cell would fall below 1e-4 min(nu).
+ * d_w [n] receives the weights. */
+gbv_status gbv_ot_warm_start(gbv_context* ctx, const double* d_xyz, uint32_t n,
+                             const gbv_ot_options* opt, const float* d_params,
+                             const float* d_norm, double* d_w, void* stream);
+/* gbv_ot_solve_device from the learned start (d_w: output only). */
+gbv_status gbv_ot_solve_learned_device(gbv_context* ctx, const double* d_xyz, const double* d_nu,
+                                       uint32_t n, const gbv_ot_options* opt,
+                                       const float* d_params, const float* d_norm, double* d_w,
+                                       void* stream, gbv_ot_report* report);
+/* The tensor-core product the network uses, exposed for testing:
+ * C[M][N] (FP32, ldc) = A[M][K] Bt[N][K]^T, A and Bt BF16 row-major, K a
+ * multiple of 32, lda and ldb multiples of 8. */
+gbv_status gbv_mlp_gemm_nt(gbv_context* ctx, const void* d_a, int lda, const void* d_bt,
+                           int ldb, float* d_c, int ldc, int M, int N, int K, void* stream);
 
 /* ---------------------------------------------------------------- */
 /* Allocation-free kNN                                               */
