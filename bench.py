@@ -9,6 +9,7 @@ geometry; the seeds then move to their centroids (CVT Lloyd step,
 voronoi/CVT.cpp:133-167).  Steps are consecutive Lloyd iterations.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--ot-n N]
 
 Prints one JSON line.  `value` is cells/s with the seeds resident on the
 GPU (CUDA events on the library's stream, L2 flushed between steps);
@@ -16,7 +17,9 @@ GPU (CUDA events on the library's stream, L2 flushed between steps);
 device->host copies inside the timed region); `cpu_baseline` times the
 CPU restatement of the reference (oracle/) on a bounded sample on this
 machine's cores.  --impl reference times that CPU implementation alone on
-the same workload.
+the same workload.  `ot` adds the optimal-transport half of the headline
+metric: solve time from zero weights and from the learned start (--ot-n
+seeds of a clustered mixture; 1,000,000 is the full configuration).
 """
 from __future__ import annotations
 
@@ -280,10 +283,61 @@ def run_ours(args) -> None:
                            "max_rel_vol_err_vs_fp64": rel_vol, "max_abs_mg_err_vs_fp64": abs_mg,
                            "neighbour_lists_identical": same_nbr},
         }
+        if args.ot_n > 0:
+            line["ot"] = run_ot(args.ot_n, ctx)
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.barrier()
         dist.destroy_process_group()
+
+
+def gaussian_mixture(n: int, k: int, sigma: float, rng: np.random.Generator) -> np.ndarray:
+    """n seeds from k isotropic Gaussians (means uniform in [0.2, 0.8]^3,
+    standard deviation sigma), rejected outside the unit cube."""
+    mu = rng.uniform(0.2, 0.8, (k, 3))
+    out, have = [], 0
+    while have < n:
+        c = rng.integers(0, k, n)
+        p = mu[c] + sigma * rng.standard_normal((n, 3))
+        p = p[((p > 0.0) & (p < 1.0)).all(1)]
+        out.append(p)
+        have += len(p)
+    return np.concatenate(out)[:n]
+
+
+def run_ot(n: int, ctx) -> dict:
+    """Semi-discrete OT to the uniform measure on the unit cube (nu_i = 1/n)
+    of n seeds from an 8-component Gaussian mixture (sigma 0.05, seed 0),
+    damped Newton + FP64 CG to a relative mass error of 1e-6: from zero
+    weights and from the learned start.  Wall time on the host around each
+    solve (everything runs on the GPU; the learned start includes its
+    features, network and solve)."""
+    import torch
+    import geogram_gb300 as g
+    from geogram_gb300.warmstart import WarmStartModel
+    x = torch.tensor(gaussian_mixture(n, 8, 0.05, np.random.default_rng(0)), device="cuda")
+    model = WarmStartModel.load()
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rep = fn()
+        torch.cuda.synchronize()
+        return rep, time.perf_counter() - t0
+
+    keys = ("newton_iters", "cell_calls", "cg_iters", "halvings", "converged", "mass_error_inf")
+    w = torch.zeros(n, dtype=torch.float64, device="cuda")
+    rp, tp = timed(lambda: g.ot_solve_device(x, w, tol=1e-6, ctx=ctx))
+    w2 = torch.empty(n, dtype=torch.float64, device="cuda")
+    rl, tl = timed(lambda: model.solve(x, w2, tol=1e-6, ctx=ctx))
+    plain = {k: rp[k] for k in keys}
+    plain["seconds"] = tp
+    learned = {k: rl[k] for k in keys}
+    learned.update(seconds=tl, start_ms=rl["ms_start"], start_scale=rl["start_scale"])
+    return {"workload": f"OT of {n} seeds, 8-component Gaussian mixture (means U[0.2,0.8]^3, "
+                        "sigma 0.05, seed 0) to the uniform measure on the unit cube, "
+                        "relative mass error 1e-6",
+            "n": n, "plain": plain, "learned_start": learned, "speedup": tp / tl}
 
 
 def main():
@@ -295,6 +349,8 @@ def main():
     ap.add_argument("--precision", default="fp32")
     ap.add_argument("--cpu-sample", type=int, default=100_000)
     ap.add_argument("--ref-sample", type=int, default=50_000)
+    ap.add_argument("--ot-n", type=int, default=100_000,
+                    help="seeds of the optimal-transport comparison (0: skip)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -229,12 +229,13 @@ def compute_cells(xyz: np.ndarray, weights: np.ndarray | None = None, *,
 
 def compute_cells_device(xyz, weights=None, *, box=((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)),
                          k0: int = 20, check_sr: bool = True, precision="fp64",
-                         stream=None, ctx: Context | None = None) -> dict:
+                         certification: str = "security_radius", stream=None,
+                         ctx: Context | None = None) -> dict:
     """Same on torch CUDA tensors (float64, n x 3 and n); results stay on
     the device (read them with device_results)."""
     ctx = ctx or default_context()
     n = xyz.shape[0]
-    o = cell_options(box, k0, check_sr, precision)
+    o = cell_options(box, k0, check_sr, precision, certification)
     rep = CellReport()
     st = ctypes.c_void_p(stream.cuda_stream) if stream is not None else None
     _lib.check(ctx._lib.gbv_cells_compute_device(ctx.handle, _lib.ptr(xyz), _lib.ptr(weights), n,

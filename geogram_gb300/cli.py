@@ -1,0 +1,88 @@
+"""Command-line driver: cells or optimal transport of synthetic seeds.
+
+    python -m geogram_gb300.cli cells --n 1000000 [--mixture 8 --sigma 0.05]
+                                      [--weights 1e-4] [--precision fp32|fp64]
+                                      [--certification security_radius|power_range]
+    python -m geogram_gb300.cli ot --n 1000000 [--mixture 8 --sigma 0.05]
+                                   [--learned] [--max-newton N] [--tol 1e-6]
+
+The counterpart of the reference's compute_RVD / compute_OTM drivers for
+meshless cells in the unit cube (src/examples/exploragram/compute_OTM/
+main.cpp:109-321): seeds are generated here (uniform, or a Gaussian
+mixture with means uniform in [0.2, 0.8]^3), everything else runs on the
+GPU.  Prints one JSON line with the report.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import time
+
+import numpy as np
+
+
+def seeds(n: int, mixture: int, sigma: float, seed: int) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    if mixture <= 0:
+        return rng.random((n, 3))
+    mu = rng.uniform(0.2, 0.8, (mixture, 3))
+    out, have = [], 0
+    while have < n:
+        c = rng.integers(0, mixture, n)
+        p = mu[c] + sigma * rng.standard_normal((n, 3))
+        p = p[((p > 0.0) & (p < 1.0)).all(1)]
+        out.append(p)
+        have += len(p)
+    return np.concatenate(out)[:n]
+
+
+def main(argv=None) -> None:
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    sub = ap.add_subparsers(dest="cmd", required=True)
+    for name in ("cells", "ot"):
+        p = sub.add_parser(name)
+        p.add_argument("--n", type=int, default=1_000_000)
+        p.add_argument("--mixture", type=int, default=0, help="components (0: uniform seeds)")
+        p.add_argument("--sigma", type=float, default=0.05)
+        p.add_argument("--seed", type=int, default=0)
+        p.add_argument("--precision", default="fp32")
+        p.add_argument("--repeat", type=int, default=1)
+    c = sub.choices["cells"]
+    c.add_argument("--weights", type=float, default=0.0, help="weights uniform in [0, w]")
+    c.add_argument("--certification", default="security_radius")
+    o = sub.choices["ot"]
+    o.add_argument("--learned", action="store_true", help="start from the learned warm start")
+    o.add_argument("--max-newton", type=int, default=100)
+    o.add_argument("--tol", type=float, default=1e-6)
+    args = ap.parse_args(argv)
+
+    import torch
+    import geogram_gb300 as g
+    x = torch.tensor(seeds(args.n, args.mixture, args.sigma, args.seed), device="cuda")
+    out = {}
+    for _ in range(args.repeat):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        if args.cmd == "cells":
+            w = None
+            if args.weights > 0:
+                w = torch.tensor(np.random.default_rng(args.seed + 1).random(args.n) * args.weights,
+                                 device="cuda")
+            rep = g.compute_cells_device(x, w, precision=args.precision,
+                                         certification=args.certification)
+        else:
+            w = torch.zeros(args.n, dtype=torch.float64, device="cuda")
+            if args.learned:
+                from geogram_gb300.warmstart import WarmStartModel
+                rep = WarmStartModel.load().solve(x, w, tol=args.tol, max_newton=args.max_newton,
+                                                  precision=args.precision)
+            else:
+                rep = g.ot_solve_device(x, w, tol=args.tol, max_newton=args.max_newton,
+                                        precision=args.precision)
+        torch.cuda.synchronize()
+        out = dict(rep, wall_s=time.perf_counter() - t0)
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

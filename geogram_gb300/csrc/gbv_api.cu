@@ -522,7 +522,28 @@ struct Pipeline {
     GBV_CUDA(cudaMemsetAsync(c->counters, 0, 2 * sizeof(unsigned long long), st));
   }
 
-  void enable_certification(const double* wmax) { node_wmax = wmax; }
+  // certification counters (GBV_CERT_STATS in the environment)
+  unsigned long long* cert_stats = nullptr;
+
+  void enable_certification(const double* wmax) {
+    node_wmax = wmax;
+    if (std::getenv("GBV_CERT_STATS")) {
+      cert_stats = c->buf<unsigned long long>("cert_stats", 5);
+      GBV_CUDA(cudaMemsetAsync(cert_stats, 0, 5 * sizeof(unsigned long long), st));
+    }
+  }
+
+  void print_cert_stats() {
+    if (!cert_stats) return;
+    unsigned long long h[5];
+    GBV_CUDA(cudaMemcpyAsync(h, cert_stats, sizeof(h), cudaMemcpyDeviceToHost, st));
+    GBV_CUDA(cudaStreamSynchronize(st));
+    std::fprintf(stderr,
+                 "[cert] %llu cells: nodes %.1f/cell (max %llu), seeds scanned %.1f/cell (max "
+                 "%llu)\n",
+                 h[4], (double)h[0] / std::max(1ull, h[4]), h[2],
+                 (double)h[1] / std::max(1ull, h[4]), h[3]);
+  }
 
   // Room for up to `per_row` extra candidates of each of `rows` list rows.
   void size_extras(uint32_t per_row, uint32_t rows) {
@@ -575,6 +596,7 @@ struct Pipeline {
       g.extra = extra;
       g.extra_cnt = extra_cnt;
       g.max_extra = max_extra;
+      g.cert_stats = cert_stats;
     }
     launch_geometry(g, st);
     GBV_CUDA(last_launch_error);
@@ -991,31 +1013,37 @@ static bool laguerre_device(gbv_context* c, const double* d_xyz, const double* d
   uint32_t* ex_s = c->buf<uint32_t>("lag_ex_s", n);
   uint32_t* ex_r = c->buf<uint32_t>("lag_ex_r", n);
   uint32_t* ex_count = c->buf<uint32_t>("lag_ex_count", 1);
+  // A call that may stop after the first pass runs that pass without the
+  // certification (its volumes bound the final ones all the same), and
+  // only certifies when it goes on.
+  if (abort_below > 0.0) {
+    P.node_wmax = nullptr;
+    P.size_extras(32u, cur.stride);
+    if (P.process(cur, ql, nullptr, nq) != 0)
+      throw StatusError{GBV_ERR_STATE, "unexpected list exhaustion in Laguerre mode"};
+    double* part = c->buf<double>("lag_min_part", 256);
+    min_partial_kernel<<<256, 256, 0, st>>>(P.vol_s, n, part); count_launch();
+    double hp[256];
+    GBV_CUDA(cudaMemcpyAsync(hp, part, sizeof(hp), cudaMemcpyDeviceToHost, st));
+    GBV_CUDA(cudaStreamSynchronize(st));
+    double mn = DBL_MAX;
+    for (double v : hp) mn = std::min(mn, v);
+    if (mn < abort_below) {
+      c->has_cells = false;
+      if (std::getenv("GBV_OT_LOG"))
+        std::fprintf(stderr, "[ot]   first-pass min volume %.3e < %.3e: stopped\n", mn,
+                     abort_below);
+      return false;
+    }
+    P.node_wmax = wmax;
+  }
   for (int round = 0;; ++round) {
     // cells far from their final shape (e.g. next to dense clusters) may
     // need hundreds of extra candidates: the room per cell doubles each round
     P.size_extras(std::min<uint32_t>(32u << std::min(round, 6), kHugeV), cur.stride);
     if (P.process(cur, ql, nullptr, nq) != 0)
       throw StatusError{GBV_ERR_STATE, "unexpected list exhaustion in Laguerre mode"};
-    if (round == 0) {
-      GBV_CUDA(cudaEventRecord(c->ev[5], st));
-      if (abort_below > 0.0) {
-        double* part = c->buf<double>("lag_min_part", 256);
-        min_partial_kernel<<<256, 256, 0, st>>>(P.vol_s, n, part); count_launch();
-        double hp[256];
-        GBV_CUDA(cudaMemcpyAsync(hp, part, sizeof(hp), cudaMemcpyDeviceToHost, st));
-        GBV_CUDA(cudaStreamSynchronize(st));
-        double mn = DBL_MAX;
-        for (double v : hp) mn = std::min(mn, v);
-        if (mn < abort_below) {
-          c->has_cells = false;
-          if (std::getenv("GBV_OT_LOG"))
-            std::fprintf(stderr, "[ot]   first-pass min volume %.3e < %.3e: stopped\n", mn,
-                         abort_below);
-          return false;
-        }
-      }
-    }
+    if (round == 0) GBV_CUDA(cudaEventRecord(c->ev[5], st));
     GBV_CUDA(cudaMemsetAsync(ex_count, 0, 4, st));
     collect_extra_kernel<<<nblocks(nq, 256), 256, 0, st>>>(ql, nq, P.extra_cnt, P.status_s,
                                                            ex_count, ex_s, ex_r); count_launch();
@@ -1059,6 +1087,7 @@ static bool laguerre_device(gbv_context* c, const double* d_xyz, const double* d
   } else {
     GBV_CUDA(cudaStreamSynchronize(st));
   }
+  P.print_cert_stats();
   GBV_CUDA(cudaGetLastError());
   return true;
 }

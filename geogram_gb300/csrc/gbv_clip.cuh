@@ -88,6 +88,9 @@ struct GeomArgs {
   uint32_t* extra;
   uint32_t* extra_cnt;
   uint32_t max_extra;
+  // optional certification counters: [0] nodes, [1] seeds scanned, [2] max
+  // nodes of one cell, [3] max seeds of one cell, [4] cells
+  unsigned long long* cert_stats;
 };
 
 // FP64 geometry of the final cells, one warp per cell, with the reference's

@@ -84,6 +84,7 @@ __device__ __forceinline__ void certify_cell(const GeomArgs& a, const SortedSeed
     }
   }
   bool overflow = false;
+  unsigned long long n_nodes = 0, n_seeds = 0;
   int sp = 0;
   if (lane == 0) stk[0] = 0u;
   sp = 1;
@@ -98,6 +99,7 @@ __device__ __forceinline__ void certify_cell(const GeomArgs& a, const SortedSeed
     const uint32_t b = S.cell_start[code << (3 * shift)];
     const uint32_t en = S.cell_start[(code + 1u) << (3 * shift)];
     if (b == en) continue;
+    ++n_nodes;
     const float WB = (float)a.node_wmax[node_offset(lev) + code];
     const float side = hf * (float)(1u << shift);
     const float bx = gd.lo_f[0] + (float)compact3(code) * side;
@@ -118,6 +120,7 @@ __device__ __forceinline__ void certify_cell(const GeomArgs& a, const SortedSeed
     }
     if (__all_sync(FULL, ok)) continue;
     if (en - b <= 32u || lev == gd.L) {
+      n_seeds += en - b;
       for (uint32_t base = b; base < en; base += 32) {
         const uint32_t j = base + lane;
         bool cut = false;
@@ -224,6 +227,13 @@ __device__ __forceinline__ void certify_cell(const GeomArgs& a, const SortedSeed
   if (lane == 0) {
     const bool more = overflow || found > a.max_extra;
     a.extra_cnt[row] = (found < a.max_extra ? found : a.max_extra) | (more ? 0x80000000u : 0u);
+    if (a.cert_stats) {
+      atomicAdd(&a.cert_stats[0], n_nodes);
+      atomicAdd(&a.cert_stats[1], n_seeds);
+      atomicMax(&a.cert_stats[2], n_nodes);
+      atomicMax(&a.cert_stats[3], n_seeds);
+      atomicAdd(&a.cert_stats[4], 1ull);
+    }
   }
   __syncwarp();
 }
