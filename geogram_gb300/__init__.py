@@ -54,6 +54,12 @@ class Context:
         self.handle = h
         self.device = device
 
+    def device_bytes(self) -> tuple[int, int]:
+        """(bytes held now, most bytes held at once) in device memory."""
+        peak = ctypes.c_uint64()
+        now = self._lib.gbv_device_bytes(self.handle, ctypes.byref(peak))
+        return int(now), int(peak.value)
+
     def close(self) -> None:
         if getattr(self, "handle", None):
             self._lib.gbv_destroy(self.handle)

@@ -118,6 +118,7 @@ _U32 = ctypes.c_uint32
 SIGNATURES = {
     "gbv_last_error": (ctypes.c_char_p, []),
     "gbv_kernel_launches": (ctypes.c_uint64, []),
+    "gbv_device_bytes": (ctypes.c_uint64, [_P, ctypes.POINTER(ctypes.c_uint64)]),
     "gbv_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(_P)]),
     "gbv_destroy": (ctypes.c_int, [_P]),
     "gbv_cell_options_default": (None, [ctypes.POINTER(CellOptions)]),

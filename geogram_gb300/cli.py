@@ -21,15 +21,20 @@ import time
 import numpy as np
 
 
-def seeds(n: int, mixture: int, sigma: float, seed: int) -> np.ndarray:
+def seeds(n: int, mixture: int, sigma: float, seed: int,
+          sigma_range: tuple[float, float] | None = None) -> np.ndarray:
+    """Uniform seeds, or a Gaussian mixture: one standard deviation sigma,
+    or per component log-uniform in sigma_range."""
     rng = np.random.default_rng(seed)
     if mixture <= 0:
         return rng.random((n, 3))
     mu = rng.uniform(0.2, 0.8, (mixture, 3))
+    sig = (np.exp(rng.uniform(np.log(sigma_range[0]), np.log(sigma_range[1]), mixture))
+           if sigma_range else np.full(mixture, sigma))
     out, have = [], 0
     while have < n:
         c = rng.integers(0, mixture, n)
-        p = mu[c] + sigma * rng.standard_normal((n, 3))
+        p = mu[c] + sig[c, None] * rng.standard_normal((n, 3))
         p = p[((p > 0.0) & (p < 1.0)).all(1)]
         out.append(p)
         have += len(p)
@@ -44,6 +49,8 @@ def main(argv=None) -> None:
         p.add_argument("--n", type=int, default=1_000_000)
         p.add_argument("--mixture", type=int, default=0, help="components (0: uniform seeds)")
         p.add_argument("--sigma", type=float, default=0.05)
+        p.add_argument("--sigma-range", default=None,
+                       help="lo,hi: per-component sigma log-uniform in [lo, hi]")
         p.add_argument("--seed", type=int, default=0)
         p.add_argument("--precision", default="fp32")
         p.add_argument("--repeat", type=int, default=1)
@@ -58,7 +65,9 @@ def main(argv=None) -> None:
 
     import torch
     import geogram_gb300 as g
-    x = torch.tensor(seeds(args.n, args.mixture, args.sigma, args.seed), device="cuda")
+    sr = tuple(float(v) for v in args.sigma_range.split(",")) if args.sigma_range else None
+    x = torch.tensor(seeds(args.n, args.mixture, args.sigma, args.seed, sr), device="cuda")
+    ctx = g.default_context()
     out = {}
     for _ in range(args.repeat):
         torch.cuda.synchronize()
@@ -81,6 +90,9 @@ def main(argv=None) -> None:
                                         precision=args.precision)
         torch.cuda.synchronize()
         out = dict(rep, wall_s=time.perf_counter() - t0)
+    now, peak = ctx.device_bytes()
+    out["device_bytes_peak"] = peak
+    out["device_bytes_inputs"] = int(x.numel() * 8 * 2)
     print(json.dumps(out))
 
 

@@ -97,8 +97,12 @@ struct gbv_context {
     void* p = nullptr;
     GBV_CUDA(cudaMalloc(&p, bytes));
     bufs[name] = {p, bytes};
+    size_t total = 0;
+    for (const auto& kv : bufs) total += kv.second.second;
+    peak_bytes = std::max(peak_bytes, total);
     return (T*)p;
   }
+  size_t peak_bytes = 0;  // most device memory the arena held at once
 };
 
 namespace gbv {
@@ -1532,6 +1536,14 @@ extern "C" {
 const char* gbv_last_error(void) { return g_last_error.c_str(); }
 
 uint64_t gbv_kernel_launches(void) { return g_launches.load(); }
+
+uint64_t gbv_device_bytes(const gbv_context* c, uint64_t* peak) {
+  if (!c) return 0;
+  uint64_t total = 0;
+  for (const auto& kv : c->bufs) total += kv.second.second;
+  if (peak) *peak = c->peak_bytes;
+  return total;
+}
 
 void gbv_cell_options_default(gbv_cell_options* o) {
   if (!o) return;

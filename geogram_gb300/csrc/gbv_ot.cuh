@@ -29,7 +29,9 @@ void spmv_dot(const Hessian& H, const double* x, double* y, double* part, int np
               cudaStream_t st);
 
 // Deterministic FP64 reductions to part[0..nparts) (Neumaier sums per block).
-constexpr int kOtParts = 256;
+// Also the grid of the SpMV and the reductions: 8 blocks of 256 threads per
+// SM of the GB300's 152, enough resident warps to cover HBM latency.
+constexpr int kOtParts = 8 * 152;
 void dot_parts(const double* a, const double* b, uint32_t n, double* part, cudaStream_t st);
 
 // r = vol - nu; parts: [0] sum r^2 terms, [1] max |r_i| / nu_i, [2] min vol.

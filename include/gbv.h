@@ -115,6 +115,11 @@ const char* gbv_last_error(void);
  * the GPU work of a call. */
 uint64_t gbv_kernel_launches(void);
 
+/* Device memory the context holds now (its buffers are kept between calls
+ * and grown on demand); *peak (optional) receives the most it held at
+ * once.  No reference counterpart (a footprint report). */
+uint64_t gbv_device_bytes(const gbv_context* ctx, uint64_t* peak);
+
 /* Creates a context on CUDA device `device`.  Replaces nothing in the
  * reference (its engines are plain C++ objects); the context owns one
  * CUDA stream and the device buffers. */
