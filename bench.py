@@ -18,8 +18,9 @@ device->host copies inside the timed region); `cpu_baseline` times the
 CPU restatement of the reference (oracle/) on a bounded sample on this
 machine's cores.  --impl reference times that CPU implementation alone on
 the same workload.  `ot` adds the optimal-transport half of the headline
-metric: solve time from zero weights and from the learned start (--ot-n
-seeds of a clustered mixture; 1,000,000 is the full configuration).
+metric: solve time from zero weights, from the learned start and with the
+multilevel solve (--ot-n seeds of a clustered mixture; 1,000,000 is the
+full configuration).
 """
 from __future__ import annotations
 
@@ -330,14 +331,20 @@ def run_ot(n: int, ctx) -> dict:
     rp, tp = timed(lambda: g.ot_solve_device(x, w, tol=1e-6, ctx=ctx))
     w2 = torch.empty(n, dtype=torch.float64, device="cuda")
     rl, tl = timed(lambda: model.solve(x, w2, tol=1e-6, ctx=ctx))
+    w3 = torch.empty(n, dtype=torch.float64, device="cuda")
+    rv, tv = timed(lambda: g.ot_solve_levels_device(x, w3, ratio=8, min_level=20000, tol=1e-6,
+                                                    ctx=ctx))
     plain = {k: rp[k] for k in keys}
     plain["seconds"] = tp
     learned = {k: rl[k] for k in keys}
     learned.update(seconds=tl, start_ms=rl["ms_start"], start_scale=rl["start_scale"])
+    levels = {k: rv[k] for k in keys}
+    levels.update(seconds=tv, levels=rv["levels"], start_scale=rv["start_scale"])
     return {"workload": f"OT of {n} seeds, 8-component Gaussian mixture (means U[0.2,0.8]^3, "
                         "sigma 0.05, seed 0) to the uniform measure on the unit cube, "
                         "relative mass error 1e-6",
-            "n": n, "plain": plain, "learned_start": learned, "speedup": tp / tl}
+            "n": n, "plain": plain, "learned_start": learned, "speedup": tp / tl,
+            "multilevel": levels, "multilevel_speedup": tp / tv}
 
 
 def main():

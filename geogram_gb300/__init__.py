@@ -41,6 +41,7 @@ __all__ = [
     "CELL_STALLED",
     "PRECISION_FP64", "PRECISION_FP32_RECHECK", "cell_options", "CERTIFY_SECURITY_RADIUS",
     "CERTIFY_POWER_RANGE", "ot_options", "ot_solve", "ot_solve_device", "ot_gradient_hessian",
+    "ot_solve_levels", "ot_solve_levels_device",
 ]
 
 
@@ -354,3 +355,39 @@ def ot_gradient_hessian(xyz: np.ndarray, w: np.ndarray, nu: np.ndarray | None = 
                                          _lib.ptr(col), _lib.ptr(val), _lib.ptr(diag), k,
                                          ctypes.byref(nnz)))
     return g, (rp, col[:nnz.value], val[:nnz.value], diag)
+
+
+def ot_solve_levels(xyz: np.ndarray, nu: np.ndarray | None = None, *, ratio: int = 8,
+                    min_level: int = 20000, box=((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)),
+                    tol: float = 1e-6, max_newton: int = 100, precision="fp32",
+                    ctx: Context | None = None) -> tuple[np.ndarray, dict]:
+    """Multilevel solve (the reference driver's optimize_levels): nested
+    random subsets of n / ratio^l seeds, coarse to fine, each starting from
+    the coarser weights interpolated at its seeds."""
+    ctx = ctx or default_context()
+    x = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+    n = len(x)
+    w = np.zeros(n)
+    m = None if nu is None else np.ascontiguousarray(nu, dtype=np.float64).reshape(n)
+    o = ot_options(box, tol, max_newton, precision=precision)
+    rep = OtReport()
+    _lib.check(ctx._lib.gbv_ot_solve_levels(ctx.handle, _lib.ptr(x), _lib.ptr(m), n,
+                                            ctypes.byref(o), int(ratio), int(min_level),
+                                            _lib.ptr(w), ctypes.byref(rep)))
+    return w, rep.as_dict()
+
+
+def ot_solve_levels_device(xyz_dev, w_dev, nu_dev=None, *, ratio: int = 8,
+                           min_level: int = 20000, box=((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)),
+                           tol: float = 1e-6, max_newton: int = 100, precision="fp32",
+                           stream=None, ctx: Context | None = None) -> dict:
+    """ot_solve_levels on torch CUDA tensors; w_dev (float64, n) receives the weights."""
+    ctx = ctx or default_context()
+    o = ot_options(box, tol, max_newton, precision=precision)
+    rep = OtReport()
+    st = ctypes.c_void_p(stream.cuda_stream) if stream is not None else None
+    _lib.check(ctx._lib.gbv_ot_solve_levels_device(ctx.handle, _lib.ptr(xyz_dev),
+                                                   _lib.ptr(nu_dev), xyz_dev.shape[0],
+                                                   ctypes.byref(o), int(ratio), int(min_level),
+                                                   _lib.ptr(w_dev), st, ctypes.byref(rep)))
+    return rep.as_dict()

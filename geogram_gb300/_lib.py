@@ -69,7 +69,7 @@ class OtReport(ctypes.Structure):
         ("cg_iters", ctypes.c_uint32),
         ("halvings", ctypes.c_uint32),
         ("cell_calls", ctypes.c_uint32),
-        ("reserved", ctypes.c_uint32),
+        ("levels", ctypes.c_uint32),
         ("mass_error_inf", ctypes.c_double),
         ("mass_error_l2", ctypes.c_double),
         ("min_volume", ctypes.c_double),
@@ -140,6 +140,11 @@ SIGNATURES = {
                                     ctypes.POINTER(OtReport)]),
     "gbv_ot_solve_device": (ctypes.c_int, [_P, _P, _P, _U32, ctypes.POINTER(OtOptions), _P, _P,
                                            ctypes.POINTER(OtReport)]),
+    "gbv_ot_solve_levels": (ctypes.c_int, [_P, _P, _P, _U32, ctypes.POINTER(OtOptions), _U32,
+                                           _U32, _P, ctypes.POINTER(OtReport)]),
+    "gbv_ot_solve_levels_device": (ctypes.c_int, [_P, _P, _P, _U32, ctypes.POINTER(OtOptions),
+                                                  _U32, _U32, _P, _P,
+                                                  ctypes.POINTER(OtReport)]),
     "gbv_ot_gradient_hessian": (ctypes.c_int, [_P, _P, _P, _P, _U32, ctypes.POINTER(OtOptions),
                                                _P, _P, _P, _P, _P, ctypes.c_uint64,
                                                ctypes.POINTER(ctypes.c_uint64)]),

@@ -4,7 +4,7 @@
                                       [--weights 1e-4] [--precision fp32|fp64]
                                       [--certification security_radius|power_range]
     python -m geogram_gb300.cli ot --n 1000000 [--mixture 8 --sigma 0.05]
-                                   [--learned] [--max-newton N] [--tol 1e-6]
+                                   [--learned | --levels] [--max-newton N] [--tol 1e-6]
 
 The counterpart of the reference's compute_RVD / compute_OTM drivers for
 meshless cells in the unit cube (src/examples/exploragram/compute_OTM/
@@ -59,6 +59,10 @@ def main(argv=None) -> None:
     c.add_argument("--certification", default="security_radius")
     o = sub.choices["ot"]
     o.add_argument("--learned", action="store_true", help="start from the learned warm start")
+    o.add_argument("--levels", action="store_true",
+                   help="multilevel solve (optimize_levels): coarse-to-fine subsets")
+    o.add_argument("--ratio", type=int, default=8)
+    o.add_argument("--min-level", type=int, default=20000)
     o.add_argument("--max-newton", type=int, default=100)
     o.add_argument("--tol", type=float, default=1e-6)
     args = ap.parse_args(argv)
@@ -81,7 +85,11 @@ def main(argv=None) -> None:
                                          certification=args.certification)
         else:
             w = torch.zeros(args.n, dtype=torch.float64, device="cuda")
-            if args.learned:
+            if args.levels:
+                rep = g.ot_solve_levels_device(x, w, ratio=args.ratio, min_level=args.min_level,
+                                               tol=args.tol, max_newton=args.max_newton,
+                                               precision=args.precision)
+            elif args.learned:
                 from geogram_gb300.warmstart import WarmStartModel
                 rep = WarmStartModel.load().solve(x, w, tol=args.tol, max_newton=args.max_newton,
                                                   precision=args.precision)

@@ -1389,10 +1389,11 @@ static void ot_solve(gbv_context* c, const double* xyz, const double* nu_in, uin
     if (ot_log_enabled())
       std::fprintf(stderr, "[ot] learned start: %.1f ms, %u CG iterations\n", ms_start, start_cg);
   }
-  // The damped Newton method needs a start whose cells all have volume.
-  // A given start (a warm start) whose cells fall below start_min is
-  // scaled toward zero, halving, and replaced by zeros after 10 halvings.
-  const double start_min = 1e-4 * nu_min;
+  // The damped Newton method needs a start whose cells all have volume
+  // (its floor eps0 comes from the start's smallest cell).  A given start
+  // (a warm start) with a cell below start_min is scaled toward zero,
+  // halving, and replaced by zeros after 10 halvings.
+  const double start_min = 1e-8 * nu_min;
   const bool nonzero_start = std::sqrt(W.dot(w, w)) > 0.0;
   double start_scale = 1.0;
   double r2, rel_inf, vmin;
@@ -1410,7 +1411,9 @@ static void ot_solve(gbv_context* c, const double* xyz, const double* nu_in, uin
       scale_copy(w, w, 0.5, n, st);
       start_scale *= 0.5;
     }
-    if (ot_log_enabled()) std::fprintf(stderr, "[ot] start scaled by %g\n", start_scale);
+    if (ot_log_enabled())
+      std::fprintf(stderr, "[ot] start scaled by %g (min volume %.3e, min nu %.3e)\n",
+                   start_scale, vmin, nu_min);
   }
   if (!nonzero_start || start_scale == 0.0) {
     cells(w, false);
@@ -1487,6 +1490,229 @@ static void ot_solve(gbv_context* c, const double* xyz, const double* nu_in, uin
     rep->start_scale = start_scale;
     rep->ms_start = ms_start;
     rep->start_cg_iters = start_cg;
+    rep->levels = 1;
+  }
+}
+
+// ---------------------------------------------------------------------
+// Multilevel optimal transport (the reference driver's optimize_levels,
+// compute_OTM/main.cpp:292-294): solve on nested random subsets of the
+// seeds, coarse to fine, each level starting from the coarser one's weights
+// interpolated at its seeds.
+// ---------------------------------------------------------------------
+// Integer hash (the "lowbias32" finaliser published by C. Wellons): the
+// level of seed i is set by where hash(i) falls, so levels are nested.
+__device__ __forceinline__ uint32_t level_hash(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x7feb352du;
+  x ^= x >> 15;
+  x *= 0x846ca68bu;
+  x ^= x >> 16;
+  return x;
+}
+
+__global__ void level_flag_kernel(uint32_t n, uint32_t thr, uint32_t* __restrict__ flag) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i <= n) flag[i] = (i < n && level_hash(i) < thr) ? 1u : 0u;
+}
+
+__global__ void level_gather_kernel(const double* __restrict__ xyz, const double* __restrict__ nu,
+                                    const uint32_t* __restrict__ flag,
+                                    const uint32_t* __restrict__ pos, uint32_t n,
+                                    double* __restrict__ xo, double* __restrict__ nuo) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || !flag[i]) return;
+  const uint32_t k = pos[i];
+  xo[3 * (size_t)k] = xyz[3 * (size_t)i];
+  xo[3 * (size_t)k + 1] = xyz[3 * (size_t)i + 1];
+  xo[3 * (size_t)k + 2] = xyz[3 * (size_t)i + 2];
+  if (nu) nuo[k] = nu[i];
+}
+
+// Weighted local linear fit of the coarse weights around each fine seed:
+// minimise sum_m g_m (w_m - a - b . (q_m - p))^2 over the kk nearest coarse
+// seeds, g_m = exp(-d_m^2 / h^2) with h the distance to the 8th nearest;
+// w(p) = a.  Smooth across seeds (no seed-to-seed noise) and exact for
+// linear potentials.
+__global__ void mls_kernel(const double* __restrict__ xf, const double* __restrict__ xc,
+                           const double* __restrict__ wc, const uint32_t* __restrict__ nidx,
+                           const double* __restrict__ nd2, uint32_t nf, uint32_t kk,
+                           double* __restrict__ wf) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nf) return;
+  const double px = xf[3 * (size_t)i], py = xf[3 * (size_t)i + 1], pz = xf[3 * (size_t)i + 2];
+  const double h2 = fmax(nd2[(size_t)i * kk + min(kk - 1, 7u)], 1e-300);
+  double A[4][4] = {}, r[4] = {};
+  double gsum = 0.0, gw = 0.0;
+  for (uint32_t m = 0; m < kk; ++m) {
+    const uint32_t j = nidx[(size_t)i * kk + m];
+    const double g = exp(-nd2[(size_t)i * kk + m] / h2);
+    const double v[4] = {1.0, xc[3 * (size_t)j] - px, xc[3 * (size_t)j + 1] - py,
+                         xc[3 * (size_t)j + 2] - pz};
+    for (int a = 0; a < 4; ++a) {
+      r[a] += g * wc[j] * v[a];
+      for (int b = 0; b < 4; ++b) A[a][b] += g * v[a] * v[b];
+    }
+    gsum += g;
+    gw += g * wc[j];
+  }
+  // a little ridge on the slope terms keeps flat neighbourhoods solvable
+  for (int a = 1; a < 4; ++a) A[a][a] += 1e-6 * h2 * gsum;
+  // Gaussian elimination with partial pivoting (4 x 4)
+  bool ok = true;
+  for (int c = 0; c < 4 && ok; ++c) {
+    int piv = c;
+    for (int q = c + 1; q < 4; ++q)
+      if (fabs(A[q][c]) > fabs(A[piv][c])) piv = q;
+    if (!(fabs(A[piv][c]) > 1e-300)) {
+      ok = false;
+      break;
+    }
+    if (piv != c) {
+      for (int b = 0; b < 4; ++b) {
+        const double t = A[c][b];
+        A[c][b] = A[piv][b];
+        A[piv][b] = t;
+      }
+      const double t = r[c];
+      r[c] = r[piv];
+      r[piv] = t;
+    }
+    for (int q = c + 1; q < 4; ++q) {
+      const double f = A[q][c] / A[c][c];
+      for (int b = c; b < 4; ++b) A[q][b] -= f * A[c][b];
+      r[q] -= f * r[c];
+    }
+  }
+  double x[4] = {};
+  if (ok) {
+    for (int c = 3; c >= 0; --c) {
+      double t = r[c];
+      for (int b = c + 1; b < 4; ++b) t -= A[c][b] * x[b];
+      x[c] = t / A[c][c];
+    }
+  }
+  wf[i] = (ok && isfinite(x[0])) ? x[0] : gw / gsum;
+}
+
+// Weights at the fine seeds xf (device, nf x 3) from the coarse seeds xc
+// and their weights wc.
+static void interpolate_weights(gbv_context* c, const double* xc, const double* wc, uint32_t nc,
+                                const double* xf, uint32_t nf, double* wf, cudaStream_t st) {
+  const uint32_t kk = std::min<uint32_t>(16, nc);
+  setup_seeds(c, nc, false);
+  c->nn_ready = false;
+  c->has_cells = false;
+  SortedSeeds& S = c->S;
+  build_grid(xc, 3, 3, nullptr, nc, S.L, S, c->scr, st);
+  double4* q4 = c->buf<double4>("lvl_q4", nf);
+  to_query4_kernel<<<nblocks(nf, 256), 256, 0, st>>>(xf, nf, 3, q4); count_launch();
+  uint32_t* oi = c->buf<uint32_t>("lvl_oi", (size_t)nf * kk);
+  double* od = c->buf<double>("lvl_od", (size_t)nf * kk);
+  KnnArgs ka{};
+  ka.S = &S;
+  ka.nq = nf;
+  ka.qpts = q4;
+  ka.k = kk;
+  ka.mode = KNN_QUERY;
+  ka.exp_idx = oi;
+  ka.exp_d2 = od;
+  ka.flag_count = c->buf<uint32_t>("knn_flag_count", 1);
+  ka.flag_list = c->buf<uint32_t>("lvl_flag_list", nf);
+  launch_knn(ka, st);
+  mls_kernel<<<nblocks(nf, 128), 128, 0, st>>>(xf, xc, wc, oi, od, nf, kk, wf); count_launch();
+  GBV_CUDA(cudaGetLastError());
+}
+
+static void ot_solve_levels(gbv_context* c, const double* xyz, const double* nu, uint32_t n,
+                            const gbv_ot_options& o, uint32_t ratio, uint32_t min_level,
+                            double* w, cudaStream_t st, gbv_ot_report* rep) {
+  if (ratio < 2) throw StatusError{GBV_ERR_INVALID_ARGUMENT, "ratio must be >= 2"};
+  min_level = std::max<uint32_t>(min_level, 64);
+  // level sizes, finest first: n, n / ratio, ... down to >= min_level
+  std::vector<uint32_t> target{n};
+  while (target.back() / ratio >= min_level) target.push_back(target.back() / ratio);
+  std::reverse(target.begin(), target.end());
+  const int nl = (int)target.size();
+  const auto t0 = std::chrono::steady_clock::now();
+  gbv_ot_report total{};
+  uint32_t* flag = c->buf<uint32_t>("lvl_flag", (size_t)n + 1);
+  uint32_t* pos = c->buf<uint32_t>("lvl_pos", (size_t)n + 1);
+  uint32_t* stmp = c->buf<uint32_t>("lvl_scan_tmp", scan_tmp_elems((size_t)n + 1));
+  const double* xprev = nullptr;
+  double* wprev = nullptr;
+  uint32_t mprev = 0;
+  for (int l = 0; l < nl; ++l) {
+    const bool finest = l == nl - 1;
+    const double* xl = xyz;
+    const double* nul = nu;
+    uint32_t m = n;
+    const std::string tag = std::to_string(l & 1);
+    if (!finest) {
+      // hash threshold for about target[l] seeds
+      const uint32_t thr = (uint32_t)std::min<double>(4294967295.0,
+                                                      4294967296.0 * target[l] / (double)n);
+      level_flag_kernel<<<nblocks((size_t)n + 1, 256), 256, 0, st>>>(n, thr, flag); count_launch();
+      GBV_CUDA(cudaMemcpyAsync(pos, flag, sizeof(uint32_t) * ((size_t)n + 1),
+                               cudaMemcpyDeviceToDevice, st));
+      exclusive_scan_u32(pos, (size_t)n + 1, stmp, st);
+      GBV_CUDA(cudaMemcpyAsync(&c->h_counts[0], pos + n, 4, cudaMemcpyDeviceToHost, st));
+      GBV_CUDA(cudaStreamSynchronize(st));
+      m = c->h_counts[0];
+      if (m < 2) continue;
+      double* xo = c->buf<double>("lvl_x" + tag, 3 * (size_t)m);
+      double* nuo = nu ? c->buf<double>("lvl_nu" + tag, m) : nullptr;
+      level_gather_kernel<<<nblocks(n, 256), 256, 0, st>>>(xyz, nu, flag, pos, n, xo, nuo);
+      count_launch();
+      if (nuo) {
+        // the level's masses sum to the box volume
+        double* part = c->buf<double>("sum_part", 2 * 256);
+        double* outs = c->buf<double>("sum_out", 1);
+        sum_partial_kernel<<<256, kSumThreads, 0, st>>>(nuo, m, part); count_launch();
+        sum_final_kernel<<<1, 32, 0, st>>>(part, 256, outs); count_launch();
+        double sum = 0.0;
+        GBV_CUDA(cudaMemcpyAsync(&sum, outs, 8, cudaMemcpyDeviceToHost, st));
+        GBV_CUDA(cudaStreamSynchronize(st));
+        const double bv = (o.box_max[0] - o.box_min[0]) * (o.box_max[1] - o.box_min[1]) *
+                          (o.box_max[2] - o.box_min[2]);
+        scale_copy(nuo, nuo, bv / sum, m, st);
+      }
+      xl = xo;
+      nul = nuo;
+    }
+    double* wl = finest ? w : c->buf<double>("lvl_w" + tag, m);
+    if (wprev) interpolate_weights(c, xprev, wprev, mprev, xl, m, wl, st);
+    else GBV_CUDA(cudaMemsetAsync(wl, 0, sizeof(double) * m, st));
+    gbv_ot_options ol = o;
+    if (!finest) ol.tol = std::max(o.tol, 1e-3);
+    gbv_ot_report r{};
+    ot_solve(c, xl, nul, m, ol, wl, st, &r);
+    if (ot_log_enabled())
+      std::fprintf(stderr, "[ot] level %d/%d: %u seeds, %u Newton, %u cell passes, %.0f ms, "
+                   "start scale %g, mass error %.2e\n", l + 1, nl, m, r.newton_iters,
+                   r.cell_calls, r.ms_total, r.start_scale, r.mass_error_inf);
+    total.cg_iters += r.cg_iters;
+    total.halvings += r.halvings;
+    total.cell_calls += r.cell_calls;
+    total.ms_cells += r.ms_cells;
+    total.ms_linear += r.ms_linear;
+    if (finest) {
+      total.converged = r.converged;
+      total.newton_iters = r.newton_iters;
+      total.mass_error_inf = r.mass_error_inf;
+      total.mass_error_l2 = r.mass_error_l2;
+      total.min_volume = r.min_volume;
+      total.start_scale = r.start_scale;
+    }
+    xprev = xl;
+    wprev = wl;
+    mprev = m;
+  }
+  if (rep) {
+    *rep = total;
+    rep->levels = (uint32_t)nl;
+    rep->ms_total =
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   }
 }
 
@@ -1862,6 +2088,40 @@ gbv_status gbv_ot_warm_start(gbv_context* c, const double* d_xyz, uint32_t n,
     gbv_ot_options o = *opt;
     o.max_newton = 0;
     ot_solve(c, d_xyz, nullptr, n, o, d_w, st, nullptr, d_params, d_norm);
+  });
+}
+
+gbv_status gbv_ot_solve_levels_device(gbv_context* c, const double* d_xyz, const double* d_nu,
+                                      uint32_t n, const gbv_ot_options* opt, uint32_t ratio,
+                                      uint32_t min_level, double* d_w, void* stream,
+                                      gbv_ot_report* report) {
+  if (!c || !d_xyz || !d_w) return fail(GBV_ERR_INVALID_ARGUMENT, "NULL argument");
+  gbv_status s = check_ot_opts(opt);
+  if (s != GBV_OK) return s;
+  return guarded([&] {
+    GBV_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    ot_solve_levels(c, d_xyz, d_nu, n, *opt, ratio, min_level, d_w, st, report);
+  });
+}
+
+gbv_status gbv_ot_solve_levels(gbv_context* c, const double* xyz, const double* nu, uint32_t n,
+                               const gbv_ot_options* opt, uint32_t ratio, uint32_t min_level,
+                               double* w, gbv_ot_report* report) {
+  if (!c || !xyz || !w) return fail(GBV_ERR_INVALID_ARGUMENT, "NULL argument");
+  gbv_status s = check_ot_opts(opt);
+  if (s != GBV_OK) return s;
+  return guarded([&] {
+    GBV_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = c->stream;
+    double* dx = c->buf<double>("ot_in_xyz", 3 * (size_t)n);
+    double* dw = c->buf<double>("ot_in_w", n);
+    double* dnu = nu ? c->buf<double>("ot_in_nu", n) : nullptr;
+    GBV_CUDA(cudaMemcpyAsync(dx, xyz, 24 * (size_t)n, cudaMemcpyHostToDevice, st));
+    if (nu) GBV_CUDA(cudaMemcpyAsync(dnu, nu, 8 * (size_t)n, cudaMemcpyHostToDevice, st));
+    ot_solve_levels(c, dx, dnu, n, *opt, ratio, min_level, dw, st, report);
+    GBV_CUDA(cudaMemcpyAsync(w, dw, 8 * (size_t)n, cudaMemcpyDeviceToHost, st));
+    GBV_CUDA(cudaStreamSynchronize(st));
   });
 }
 

@@ -244,13 +244,13 @@ typedef struct {
     uint32_t cg_iters;        /* total */
     uint32_t halvings;        /* damping steps of the line search */
     uint32_t cell_calls;      /* Laguerre diagrams computed */
-    uint32_t reserved;
+    uint32_t levels;          /* 1, or the levels of gbv_ot_solve_levels */
     double mass_error_inf;    /* max_i |vol_i - nu_i| / nu_i at the end */
     double mass_error_l2;     /* ||vol - nu|| / ||nu|| at the end */
     double min_volume;
     double ms_total, ms_cells, ms_linear;
     /* the given start was multiplied by this so that every cell keeps at
-     * least 1e-4 min(nu) (1: used as given, 0: replaced by zeros) */
+     * least 1e-8 min(nu) (1: used as given, 0: replaced by zeros) */
     double start_scale;
     double ms_start;          /* learned start: features, network and solve */
     uint32_t start_cg_iters;  /* learned start: CG iterations of its solve */
@@ -265,6 +265,21 @@ void gbv_ot_options_default(gbv_ot_options* opt);
  * receives the solution.  Host arrays; the report may be NULL. */
 gbv_status gbv_ot_solve(gbv_context* ctx, const double* xyz, const double* nu, uint32_t n,
                         const gbv_ot_options* opt, double* w_inout, gbv_ot_report* report);
+
+/* Multilevel solve, as the reference driver's optimize_levels
+ * (compute_OTM/main.cpp:292-294): nested random subsets of n / ratio^l
+ * seeds (the coarsest at least min_level), each solved to a relative mass
+ * error of max(tol, 1e-3) and the finest to tol; every level starts from
+ * the coarser weights interpolated at its seeds (a Gaussian-weighted local
+ * linear fit over the 16 nearest coarser seeds).  w_out: output only.
+ * Totals in the report (newton_iters and the errors are the finest level's). */
+gbv_status gbv_ot_solve_levels(gbv_context* ctx, const double* xyz, const double* nu, uint32_t n,
+                               const gbv_ot_options* opt, uint32_t ratio, uint32_t min_level,
+                               double* w_out, gbv_ot_report* report);
+gbv_status gbv_ot_solve_levels_device(gbv_context* ctx, const double* d_xyz, const double* d_nu,
+                                      uint32_t n, const gbv_ot_options* opt, uint32_t ratio,
+                                      uint32_t min_level, double* d_w, void* stream,
+                                      gbv_ot_report* report);
 
 /* Same on device arrays, ordered on `stream` (NULL: the context's). */
 gbv_status gbv_ot_solve_device(gbv_context* ctx, const double* d_xyz, const double* d_nu,
@@ -323,7 +338,7 @@ gbv_status gbv_mlp_adam(gbv_context* ctx, float* d_params, float* d_m, float* d_
  * prediction of t_i = (H0 w*)_i / vol_i(0) (the cell-averaged Laplacian of
  * the optimal weights; by the Monge-Ampere relation a function of the local
  * density its inputs see), then w = H0^+ (t vol(0)) by conjugate gradient,
- * scaled toward zero if a cell would fall below 1e-4 min(nu).
+ * scaled toward zero if a cell would fall below 1e-8 min(nu).
  * d_w [n] receives the weights. */
 gbv_status gbv_ot_warm_start(gbv_context* ctx, const double* d_xyz, uint32_t n,
                              const gbv_ot_options* opt, const float* d_params,

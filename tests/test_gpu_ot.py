@@ -156,3 +156,20 @@ def test_warm_start_from_solution_needs_no_step(g):
     w2, rep2 = g.ot_solve(x, w0=w, tol=1e-6)
     assert rep2["newton_iters"] == 0 and rep2["converged"] == 1
     assert np.array_equal(w2, w)
+
+
+@pytest.mark.parametrize("nu_kind", ["uniform", "random"])
+def test_multilevel_solve(g, ot, nu_kind):
+    """optimize_levels: coarse-to-fine; the finest level must reach the
+    tolerance, checked with the oracle's volumes."""
+    rng = np.random.default_rng(8)
+    x = gaussian_mixture(6000, 6, 0.06, rng)
+    nu = None
+    if nu_kind == "random":
+        nu = rng.uniform(0.5, 1.5, len(x))
+        nu /= nu.sum()
+    w, rep = g.ot_solve_levels(x, nu, ratio=4, min_level=400, tol=1e-6)
+    assert rep["levels"] == 2 and rep["converged"] == 1, rep  # 6000 -> 1500 (-> 375 < 400)
+    v = ot.laguerre_cells(x, w)["vol"]
+    target = np.full(len(x), 1.0 / len(x)) if nu is None else nu
+    assert np.max(np.abs(v - target) / target) < 1e-6
