@@ -39,6 +39,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 N_SEEDS = 1_000_000
+# DRAM bytes of one knn_fast_kernel launch (k = 64) on this workload, from an
+# ncu capture (67.10 MB read + 229.45 MB written)
+KNN_TRAFFIC_BYTES = 296.55e6
 W_MAX = 1e-4
 METRIC = "Laguerre cells/s (power diagram, 1M seeds, FP32 clip + FP64 re-clip, one Lloyd step)"
 WORKLOAD = ("power diagram of 1M seeds uniform in [0,1]^3, weights U[0,1e-4], seed 0; "
@@ -270,7 +273,10 @@ def run_ours(args) -> None:
             "roofline": {"kernel": "knn_fast_kernel (first kNN pass)", "bound": "hbm",
                          "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,
-                         "bytes_per_seed": bytes_per_seed, "traffic": None},
+                         "bytes_per_seed": bytes_per_seed,
+                         # ncu dram__bytes_read.sum + dram__bytes_write.sum of this kernel's
+                         # first pass on this workload (one capture, bytes per launch)
+                         "traffic": KNN_TRAFFIC_BYTES},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "cells/s",
                     "h2d_bytes_per_step": 32 * N_SEEDS, "d2h_bytes_per_step": 24 * N_SEEDS},
