@@ -466,6 +466,8 @@ struct Pipeline {
   uint32_t n_recheck = 0, n_over = 0, n_morek = 0;
   // certification (Laguerre mode)
   const double* node_wmax = nullptr;
+  const double4* node_lin = nullptr;
+  const double* node_ex = nullptr;
   uint32_t* extra = nullptr;
   uint32_t* extra_cnt = nullptr;
   uint32_t max_extra = 32;
@@ -529,8 +531,10 @@ struct Pipeline {
   // certification counters (GBV_CERT_STATS in the environment)
   unsigned long long* cert_stats = nullptr;
 
-  void enable_certification(const double* wmax) {
+  void enable_certification(const double* wmax, const double4* lin, const double* ex) {
     node_wmax = wmax;
+    node_lin = lin;
+    node_ex = ex;
     if (std::getenv("GBV_CERT_STATS")) {
       cert_stats = c->buf<unsigned long long>("cert_stats", 5);
       GBV_CUDA(cudaMemsetAsync(cert_stats, 0, 5 * sizeof(unsigned long long), st));
@@ -596,6 +600,8 @@ struct Pipeline {
     g.shape = kind == 2 ? CLIP_LARGE : CLIP_SMALL;
     if (node_wmax) {
       g.node_wmax = node_wmax;
+      g.node_lin = node_lin;
+      g.node_ex = node_ex;
       g.cand_cnt = L.cnt;
       g.extra = extra;
       g.extra_cnt = extra_cnt;
@@ -651,6 +657,8 @@ struct Pipeline {
       h.hp_area = hp_area;
       if (node_wmax) {
         h.node_wmax = node_wmax;
+        h.node_lin = node_lin;
+        h.node_ex = node_ex;
         h.extra = extra;
         h.extra_cnt = extra_cnt;
         h.max_extra = max_extra;
@@ -973,10 +981,19 @@ static bool laguerre_device(gbv_context* c, const double* d_xyz, const double* d
   build_grid(d_xyz, 3, 3, d_w, n, S.L, S, c->scr, st);
   double* wmax = c->buf<double>("node_wmax", node_count(S.L));
   build_node_wmax(S, wmax, st);
+  // linear weight bounds per node (they prune where the weights have a
+  // large smooth gradient, as optimal-transport weights do)
+  double4* nlin = nullptr;
+  double* nex = nullptr;
+  if (d_w) {
+    nlin = c->buf<double4>("node_lin", node_count(S.L));
+    nex = c->buf<double>("node_ex", node_count(S.L));
+    build_node_linear(S, nlin, nex, c->buf<double>("node_mom", 14 * node_count(S.L)), st);
+  }
   GBV_CUDA(cudaEventRecord(c->ev[1], st));
   // no list cap for seeds with copies (the security-radius loop is not used)
   Pipeline P(c, n, box_min, box_max, fp32, false, n, st);
-  P.enable_certification(wmax);
+  P.enable_certification(wmax, nlin, nex);
   uint32_t K;
   uint32_t* lists;
   uint32_t* cnt = c->buf<uint32_t>("lag_cnt", n);

@@ -84,6 +84,8 @@ struct GeomArgs {
   // list row), and counted in extra_cnt[row] (bit 31: more were found than
   // fit).
   const double* node_wmax;
+  const double4* node_lin;    // per-node linear weight bound (a, g) and its excess
+  const double* node_ex;      //   (build_node_linear); may be null
   const uint32_t* cand_cnt;   // candidate list lengths, per list row
   uint32_t* extra;
   uint32_t* extra_cnt;
@@ -141,6 +143,8 @@ struct HugeArgs {
   double** hp_area;
   // certification (as GeomArgs; off when node_wmax is null)
   const double* node_wmax;
+  const double4* node_lin;
+  const double* node_ex;
   uint32_t* extra;
   uint32_t* extra_cnt;
   uint32_t max_extra;

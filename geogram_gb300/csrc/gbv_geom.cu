@@ -106,6 +106,13 @@ __device__ __forceinline__ void certify_cell(const GeomArgs& a, const SortedSeed
     const float by = gd.lo_f[1] + (float)compact3(code >> 1) * side;
     const float bz = gd.lo_f[2] + (float)compact3(code >> 2) * side;
     const float pad = 1e-6f * (1.f + fabsf(bx) + fabsf(by) + fabsf(bz)) + 1e-5f * side;
+    const bool have_lin = a.node_lin != nullptr;
+    double4 fl = make_double4(0.0, 0.0, 0.0, 0.0);
+    double fe = 0.0;
+    if (have_lin) {
+      fl = a.node_lin[node_offset(lev) + code];
+      fe = a.node_ex[node_offset(lev) + code];
+    }
     bool ok = true;
 #pragma unroll
     for (int q = 0; q < NCL; ++q) {
@@ -116,7 +123,10 @@ __device__ __forceinline__ void certify_cell(const GeomArgs& a, const SortedSeed
       const float dz = fmaxf(fmaxf(bz - pad - c.z, c.z - (bz + side + pad)), 0.f);
       const float d2 = dx * dx + dy * dy + dz * dz;
       const float need = (c.w + WB) + 1e-5f * (fabsf(c.w) + fabsf(WB) + d2) + 1e-7f;
-      ok = ok && (d2 >= need);
+      const bool clear = (d2 >= need) ||
+                         (have_lin && linear_bound_clears(c.x, c.y, c.z, c.w, bx, by, bz, side,
+                                                          pad, fl, fe));
+      ok = ok && clear;
     }
     if (__all_sync(FULL, ok)) continue;
     if (en - b <= 32u || lev == gd.L) {

@@ -241,6 +241,197 @@ __global__ void wmax_up_kernel(const double* __restrict__ child, size_t nparent,
   parent[p] = m;
 }
 
+// ---------------------------------------------------------------------
+// Linear weight bound per octree node
+// ---------------------------------------------------------------------
+constexpr int kMom = 14;  // S0, S1 (3), S2 (xx xy xz yy yz zz), Sw, Swd (3)
+
+__device__ __forceinline__ double3 node_centre(const GridDesc& gd, int lev, uint32_t code) {
+  const double side = gd.h * (double)(1u << (gd.L - lev));
+  return make_double3(gd.lo[0] + ((double)compact3(code) + 0.5) * side,
+                      gd.lo[1] + ((double)compact3(code >> 1) + 0.5) * side,
+                      gd.lo[2] + ((double)compact3(code >> 2) + 0.5) * side);
+}
+
+__global__ void leaf_moments_kernel(SortedSeeds S, size_t ncells, double* __restrict__ mom) {
+  const size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncells) return;
+  const GridDesc& gd = *S.gd;
+  const double3 m = node_centre(gd, gd.L, (uint32_t)c);
+  double v[kMom] = {};
+  for (uint32_t s = S.cell_start[c]; s < S.cell_start[c + 1]; ++s) {
+    const double4 p = S.xd[s];
+    const double w = S.ws ? S.ws[s] : 0.0;
+    const double dx = p.x - m.x, dy = p.y - m.y, dz = p.z - m.z;
+    v[0] += 1.0;
+    v[1] += dx; v[2] += dy; v[3] += dz;
+    v[4] += dx * dx; v[5] += dx * dy; v[6] += dx * dz;
+    v[7] += dy * dy; v[8] += dy * dz; v[9] += dz * dz;
+    v[10] += w;
+    v[11] += w * dx; v[12] += w * dy; v[13] += w * dz;
+  }
+  double* o = mom + (node_offset(gd.L) + c) * kMom;
+  for (int k = 0; k < kMom; ++k) o[k] = v[k];
+}
+
+// parent moments from the 8 children's, shifted to the parent's centre
+__global__ void combine_moments_kernel(const GridDesc* __restrict__ gdp, int lev, size_t nparent,
+                                       double* __restrict__ mom) {
+  const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= nparent) return;
+  const GridDesc& gd = *gdp;
+  const double3 mp = node_centre(gd, lev, (uint32_t)p);
+  double v[kMom] = {};
+  for (int k = 0; k < 8; ++k) {
+    const uint32_t cc = ((uint32_t)p << 3) | (uint32_t)k;
+    const double* c = mom + (node_offset(lev + 1) + cc) * kMom;
+    if (c[0] == 0.0) continue;
+    const double3 mc = node_centre(gd, lev + 1, cc);
+    const double ex = mc.x - mp.x, ey = mc.y - mp.y, ez = mc.z - mp.z;
+    const double n0 = c[0];
+    v[0] += n0;
+    v[1] += c[1] + n0 * ex; v[2] += c[2] + n0 * ey; v[3] += c[3] + n0 * ez;
+    v[4] += c[4] + 2.0 * c[1] * ex + n0 * ex * ex;
+    v[5] += c[5] + c[1] * ey + c[2] * ex + n0 * ex * ey;
+    v[6] += c[6] + c[1] * ez + c[3] * ex + n0 * ex * ez;
+    v[7] += c[7] + 2.0 * c[2] * ey + n0 * ey * ey;
+    v[8] += c[8] + c[2] * ez + c[3] * ey + n0 * ey * ez;
+    v[9] += c[9] + 2.0 * c[3] * ez + n0 * ez * ez;
+    v[10] += c[10];
+    v[11] += c[11] + c[10] * ex; v[12] += c[12] + c[10] * ey; v[13] += c[13] + c[10] * ez;
+  }
+  double* o = mom + (node_offset(lev) + p) * kMom;
+  for (int k = 0; k < kMom; ++k) o[k] = v[k];
+}
+
+// least-squares (a, g) per node; empty nodes get zeros
+__global__ void fit_nodes_kernel(const double* __restrict__ mom, size_t nn,
+                                 double4* __restrict__ lin, unsigned long long* __restrict__ ex) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nn) return;
+  const double* v = mom + i * kMom;
+  ex[i] = 0ull;  // the ordered key of -inf (below every double key)
+  double4 r = make_double4(0.0, 0.0, 0.0, 0.0);
+  if (v[0] > 0.0) {
+    r.x = v[10] / v[0];
+    if (v[0] >= 4.0) {
+      double A[4][4] = {{v[0], v[1], v[2], v[3]},
+                        {v[1], v[4], v[5], v[6]},
+                        {v[2], v[5], v[7], v[8]},
+                        {v[3], v[6], v[8], v[9]}};
+      double b[4] = {v[10], v[11], v[12], v[13]};
+      const double ridge = 1e-9 * (v[4] + v[7] + v[9]) + 1e-300;
+      for (int k = 1; k < 4; ++k) A[k][k] += ridge;
+      bool ok = true;
+      for (int c = 0; c < 4 && ok; ++c) {
+        int piv = c;
+        for (int q = c + 1; q < 4; ++q)
+          if (fabs(A[q][c]) > fabs(A[piv][c])) piv = q;
+        if (!(fabs(A[piv][c]) > 0.0)) { ok = false; break; }
+        if (piv != c) {
+          for (int k = 0; k < 4; ++k) { const double t = A[c][k]; A[c][k] = A[piv][k]; A[piv][k] = t; }
+          const double t = b[c]; b[c] = b[piv]; b[piv] = t;
+        }
+        for (int q = c + 1; q < 4; ++q) {
+          const double f = A[q][c] / A[c][c];
+          for (int k = c; k < 4; ++k) A[q][k] -= f * A[c][k];
+          b[q] -= f * b[c];
+        }
+      }
+      if (ok) {
+        double x[4];
+        for (int c = 3; c >= 0; --c) {
+          double t = b[c];
+          for (int k = c + 1; k < 4; ++k) t -= A[c][k] * x[k];
+          x[c] = t / A[c][c];
+        }
+        if (isfinite(x[0]) && isfinite(x[1]) && isfinite(x[2]) && isfinite(x[3]))
+          r = make_double4(x[0], x[1], x[2], x[3]);
+      }
+    }
+  }
+  lin[i] = r;
+}
+
+// monotone map of doubles to unsigned keys (atomicMax on doubles)
+__device__ __forceinline__ unsigned long long dkey(double v) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double dval(unsigned long long k) {
+  const unsigned long long b = (k >> 63) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k;
+  return __longlong_as_double((long long)b);
+}
+
+// e[node] = max over the node's seeds of w - a - g . (p - m), at level lev
+__global__ void node_excess_kernel(SortedSeeds S, int lev, const double4* __restrict__ lin,
+                                   unsigned long long* __restrict__ ex) {
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned FULL = 0xFFFFFFFFu;
+  const GridDesc& gd = *S.gd;
+  bool live = s < S.n;
+  uint32_t node = 0;
+  double r = -INFINITY;
+  if (live) {
+    const double4 p = S.xd[s];
+    // the fine cell holding slot s: cell_start[c] <= s < cell_start[c + 1]
+    uint32_t lo = 0, hi = 1u << (3 * gd.L);
+    while (hi - lo > 1) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (S.cell_start[mid] <= s) lo = mid;
+      else hi = mid;
+    }
+    node = lo >> (3 * (gd.L - lev));
+    const double3 m = node_centre(gd, lev, node);
+    const double4 f = lin[node_offset(lev) + node];
+    const double w = S.ws ? S.ws[s] : 0.0;
+    r = w - f.x - (f.y * (p.x - m.x) + f.z * (p.y - m.y) + f.w * (p.z - m.z));
+  }
+  // one atomic per warp when the whole warp is in one node
+  const uint32_t n0 = __shfl_sync(FULL, node, 0);
+  const bool same = __all_sync(FULL, !live || node == n0);
+  if (same) {
+    double mx = r;
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(FULL, mx, o));
+    if ((threadIdx.x & 31) == 0 && mx > -INFINITY)
+      atomicMax(&ex[node_offset(lev) + n0], dkey(mx));
+  } else if (live) {
+    atomicMax(&ex[node_offset(lev) + node], dkey(r));
+  }
+}
+
+// in place: ex holds keys, each thread turns its own entry into a double
+__global__ void excess_decode_kernel(double* __restrict__ ex, size_t nn) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nn) return;
+  const unsigned long long k = reinterpret_cast<unsigned long long*>(ex)[i];
+  ex[i] = k ? dval(k) : 0.0;
+}
+
+void build_node_linear(const SortedSeeds& S, double4* lin, double* ex, double* moments,
+                       cudaStream_t st) {
+  const int L = S.L;
+  const size_t nf = (size_t)1 << (3 * L);
+  const size_t nn = node_count(L);
+  leaf_moments_kernel<<<(unsigned)((nf + 255) / 256), 256, 0, st>>>(S, nf, moments);
+  count_launch();
+  for (int l = L - 1; l >= 0; --l) {
+    const size_t np = (size_t)1 << (3 * l);
+    combine_moments_kernel<<<(unsigned)((np + 255) / 256), 256, 0, st>>>(S.gd, l, np, moments);
+    count_launch();
+  }
+  // the excess maxima are kept as ordered keys in ex itself, decoded at the end
+  unsigned long long* keys = reinterpret_cast<unsigned long long*>(ex);
+  fit_nodes_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(moments, nn, lin, keys);
+  count_launch();
+  for (int l = 0; l <= L; ++l) {
+    node_excess_kernel<<<(S.n + 255) / 256, 256, 0, st>>>(S, l, lin, keys);
+    count_launch();
+  }
+  excess_decode_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(ex, nn);
+  count_launch();
+}
+
 void build_node_wmax(const SortedSeeds& S, double* wmax, cudaStream_t st) {
   const int L = S.L;
   const size_t nf = (size_t)1 << (3 * L);

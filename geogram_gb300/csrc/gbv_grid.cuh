@@ -55,6 +55,42 @@ __host__ __device__ inline size_t node_offset(int l) {
 inline size_t node_count(int L) { return node_offset(L + 1); }
 void build_node_wmax(const SortedSeeds& S, double* wmax, cudaStream_t st);
 
+// Linear upper bound of the weights per octree node: for every seed j of
+// node B (centre m), w_j <= a + g . (p_j - m) + e, with (a, g) the
+// least-squares fit of the node's weights and e the largest excess.  For
+// any point c it bounds the power of the node's seeds from below:
+//   |c - p_j|^2 - w_j >= dist(c + g/2, box)^2 - (c - m) . g - |g|^2 / 4 - a - e.
+// lin[node] = (a, gx, gy, gz), ex[node] = e; moments: 14 doubles per node of
+// scratch.  Deterministic (fixed combination order; the maxima are
+// order-independent).
+void build_node_linear(const SortedSeeds& S, double4* lin, double* ex, double* moments,
+                       cudaStream_t st);
+
+// True when no seed of the node (box [b, b + side]^3, padded by pad) can
+// have power below `best` at corner c by the linear bound (FP32, with a
+// margin that only keeps more nodes).
+__device__ __forceinline__ bool linear_bound_clears(float cx, float cy, float cz, float best,
+                                                    float bx, float by, float bz, float side,
+                                                    float pad, const double4& fl, double fe) {
+  const float ga = (float)fl.x, gx = (float)fl.y, gy = (float)fl.z, gz = (float)fl.w;
+  const float ge = (float)fe;
+  const float px = cx + 0.5f * gx, py = cy + 0.5f * gy, pz = cz + 0.5f * gz;
+  const float dx = fmaxf(fmaxf(bx - pad - px, px - (bx + side + pad)), 0.f);
+  const float dy = fmaxf(fmaxf(by - pad - py, py - (by + side + pad)), 0.f);
+  const float dz = fmaxf(fmaxf(bz - pad - pz, pz - (bz + side + pad)), 0.f);
+  const float d2 = dx * dx + dy * dy + dz * dz;
+  const float h = 0.5f * side;
+  const float lin = (cx - (bx + h)) * gx + (cy - (by + h)) * gy + (cz - (bz + h)) * gz;
+  const float g2 = 0.25f * (gx * gx + gy * gy + gz * gz);
+  const float lb = d2 - lin - g2 - ga - ge;
+  // rounding of the FP32 copies of a, g, e (g times |p - m| <= side) and of
+  // this evaluation
+  const float margin = 1e-5f * (fabsf(best) + fabsf(ga) + fabsf(ge) + fabsf(lin) + g2 + d2 +
+                                (fabsf(gx) + fabsf(gy) + fabsf(gz)) * side) +
+                       1e-7f;
+  return lb >= best + margin;
+}
+
 enum KnnMode : int {
   KNN_CELLS = 0,  // exclude self and zero-distance seeds (delaunay_nn rule)
   KNN_ALL = 1,    // all stored points, self included (get_nearest_neighbors)
