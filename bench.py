@@ -19,8 +19,8 @@ CPU restatement of the reference (oracle/) on a bounded sample on this
 machine's cores.  --impl reference times that CPU implementation alone on
 the same workload.  `ot` adds the optimal-transport half of the headline
 metric: solve time from zero weights, from the learned start and with the
-multilevel solve (--ot-n seeds of a clustered mixture; 1,000,000 is the
-full configuration).
+multilevel solve (--ot-n seeds of the clustered mixture, 1,000,000 by
+default: about 50 s per solve).
 """
 from __future__ import annotations
 
@@ -362,7 +362,7 @@ def main():
     ap.add_argument("--precision", default="fp32")
     ap.add_argument("--cpu-sample", type=int, default=100_000)
     ap.add_argument("--ref-sample", type=int, default=50_000)
-    ap.add_argument("--ot-n", type=int, default=100_000,
+    ap.add_argument("--ot-n", type=int, default=1_000_000,
                     help="seeds of the optimal-transport comparison (0: skip)")
     args = ap.parse_args()
     if args.warmup < 3:
