@@ -361,7 +361,7 @@ def ot_solve_levels(xyz: np.ndarray, nu: np.ndarray | None = None, *, ratio: int
                     min_level: int = 20000, box=((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)),
                     tol: float = 1e-6, max_newton: int = 100, precision="fp32",
                     ctx: Context | None = None) -> tuple[np.ndarray, dict]:
-    """Multilevel solve (the reference driver's optimize_levels): nested
+    """Multilevel solve (optimize_levels of the reference's compute_OTM): nested
     random subsets of n / ratio^l seeds, coarse to fine, each starting from
     the coarser weights interpolated at its seeds."""
     ctx = ctx or default_context()

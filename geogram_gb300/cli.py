@@ -1,4 +1,4 @@
-"""Command-line driver: cells or optimal transport of synthetic seeds.
+"""Command-line program: cells or optimal transport of synthetic seeds.
 
     python -m geogram_gb300.cli cells --n 1000000 [--mixture 8 --sigma 0.05]
                                       [--weights 1e-4] [--precision fp32|fp64]
@@ -6,7 +6,7 @@
     python -m geogram_gb300.cli ot --n 1000000 [--mixture 8 --sigma 0.05]
                                    [--learned | --levels] [--max-newton N] [--tol 1e-6]
 
-The counterpart of the reference's compute_RVD / compute_OTM drivers for
+The counterpart of the reference's compute_RVD / compute_OTM programs for
 meshless cells in the unit cube (src/examples/exploragram/compute_OTM/
 main.cpp:109-321): seeds are generated here (uniform, or a Gaussian
 mixture with means uniform in [0.2, 0.8]^3), everything else runs on the

@@ -1512,7 +1512,7 @@ static void ot_solve(gbv_context* c, const double* xyz, const double* nu_in, uin
 }
 
 // ---------------------------------------------------------------------
-// Multilevel optimal transport (the reference driver's optimize_levels,
+// Multilevel optimal transport (optimize_levels of the reference's compute_OTM,
 // compute_OTM/main.cpp:292-294): solve on nested random subsets of the
 // seeds, coarse to fine, each level starting from the coarser one's weights
 // interpolated at its seeds.

@@ -217,7 +217,7 @@ gbv_status gbv_lloyd_device(gbv_context* ctx, double* d_xyz, const double* d_w,
 
 /* ---------------------------------------------------------------- */
 /* Semi-discrete optimal transport (OptimalTransportMap3d, exploragram;
- * driver compute_OTM/main.cpp:280-296).  The exploragram sources are not in
+ * program compute_OTM/main.cpp:280-296).  The exploragram sources are not in
  * the reference checkout; the solver follows the published method it
  * implements: damped Newton on the Kantorovich dual with FP64 conjugate
  * gradient on the Laguerre Hessian.                                  */
@@ -266,7 +266,7 @@ void gbv_ot_options_default(gbv_ot_options* opt);
 gbv_status gbv_ot_solve(gbv_context* ctx, const double* xyz, const double* nu, uint32_t n,
                         const gbv_ot_options* opt, double* w_inout, gbv_ot_report* report);
 
-/* Multilevel solve, as the reference driver's optimize_levels
+/* Multilevel solve, as optimize_levels in the reference's compute_OTM
  * (compute_OTM/main.cpp:292-294): nested random subsets of n / ratio^l
  * seeds (the coarsest at least min_level), each solved to a relative mass
  * error of max(tol, 1e-3) and the finest to tol; every level starts from

@@ -1,7 +1,7 @@
 /*
  * gbv_oracle.c -- CPU restatement of geogram's meshless Laguerre cell path.
  *
- * TEST INFRASTRUCTURE ONLY: the checker for the GPU kernels and the timed
+ * TEST INFRASTRUCTURE ONLY: the oracle of the GPU kernels' tests and the timed
  * CPU baseline ("port") of bench.py.  Nothing in the product (the
  * geogram_gb300 package and its CUDA library) links, imports or calls it.
  *

@@ -7,7 +7,7 @@ ctypes access to
     VBW::ConvexCell compiled from the reference sources (built only where
     the reference checkout is present).
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use
-this module, as the checker.  The product never imports it.
+this module, to check results.  The product never imports it.
 """
 from __future__ import annotations
 

@@ -3,7 +3,7 @@
 Test infrastructure only: the product never imports this module.
 
 The reference's solver (exploragram's OptimalTransportMap3d) is not in the
-reference checkout; its only trace is the driver
+reference checkout; its only trace is the compute_OTM program
 src/examples/exploragram/compute_OTM/main.cpp:280-296 (set_points,
 set_epsilon, optimize).  This module restates the published method it
 implements (B. Levy, "A numerical algorithm for L2 semi-discrete optimal

@@ -2,8 +2,8 @@
 
 The fixtures hold geogram's own outputs (BalancedKdTree + VBW::ConvexCell,
 tests/golden/make_golden.py).  Both precision modes must reproduce them bit
-for bit: neighbour lists, facet areas, volumes and centroids (the north
-star's bar is 1e-12 relative for volumes and centroids; the engine matches
+for bit: neighbour lists, facet areas, volumes and centroids (1e-12
+relative would be the bar for volumes and centroids; the engine matches
 exactly).  Degenerate inputs (a lattice) are compared on the quantities
 that do not depend on how equidistant neighbours are ordered."""
 import numpy as np

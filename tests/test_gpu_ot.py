@@ -6,7 +6,7 @@ Laguerre cells, in which every seed clips every cell.  Clipping order
 differs (candidates by distance, then the seeds the range query finds), so
 volumes agree to rounding (1e-11 relative), neighbour sets exactly.
 
-The solver is judged by the pinned oracle volumes at the weights it returns
+The solver is checked with the pinned oracle volumes at the weights it returns
 (max_i |vol_i - nu_i| / nu_i < 1e-6) and by the oracle's own Newton
 solution (weights equal up to the constant the dual leaves free)."""
 import numpy as np

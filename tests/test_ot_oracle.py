@@ -4,7 +4,7 @@ The reference's solver is absent from its checkout, so OT parity is
 unpinned; these tests pin what can be pinned: the Hessian against finite
 differences of the cell volumes (which are pinned to the reference's
 ConvexCell), the known answer of a lattice, and convergence of the plain
-Newton solver to the mass tolerance the benchmark spec fixes (1e-6)."""
+Newton solver to the mass tolerance of the OT workload (1e-6)."""
 import numpy as np
 import pytest
 
