@@ -1,0 +1,40 @@
+"""Host-side Python pieces that need no GPU: the warm-start network's
+parameter layout and stored model, and the command-line seed generator."""
+import numpy as np
+
+
+def test_warmstart_parameter_layout(tmp_path):
+    from geogram_gb300 import _lib, warmstart as ws
+    p = ws.init_params(seed=3)
+    assert p.shape == (_lib.MLP_PARAMS,) and p.dtype == np.float32
+    u = ws.unpack(p)
+    assert u["W1"].shape == (ws.H, ws.IN) and u["W2"].shape == (ws.H, ws.H)
+    assert u["W4"].shape == (ws.H,) and u["b4"].shape == (1,)
+    # the padded input columns start (and must stay) at zero
+    assert np.all(p[ws.OFF_W1:ws.OFF_B1].reshape(ws.H, 32)[:, ws.IN:] == 0.0)
+    m = ws.WarmStartModel(p)
+    path = tmp_path / "m.npz"
+    m.save(str(path), note="x")
+    m2 = ws.WarmStartModel.load(str(path))
+    assert np.array_equal(m2.params, m.params) and np.array_equal(m2.norm, m.norm)
+
+
+def test_shipped_model_loads():
+    import json
+    from geogram_gb300 import _lib, warmstart as ws
+    m = ws.WarmStartModel.load()
+    assert m.params.shape == (_lib.MLP_PARAMS,) and m.norm.shape == (_lib.MLP_NORM,)
+    assert np.all(np.isfinite(m.params)) and np.all(m.norm[ws.IN:2 * ws.IN] > 0)
+    rep = json.loads(str(np.load(ws.DEFAULT_MODEL)["report"]))
+    assert rep["loss_last"] < rep["loss_first"]
+
+
+def test_cli_seed_generator():
+    from geogram_gb300.cli import seeds
+    u = seeds(1000, 0, 0.05, 1)
+    assert u.shape == (1000, 3) and np.all((u >= 0) & (u < 1))
+    g = seeds(5000, 8, 0.05, 1)
+    assert g.shape == (5000, 3) and np.all((g > 0) & (g < 1))
+    h = seeds(5000, 32, 0.05, 1, (0.01, 0.1))
+    assert h.shape == (5000, 3) and np.all((h > 0) & (h < 1))
+    assert np.array_equal(seeds(100, 4, 0.05, 7), seeds(100, 4, 0.05, 7))
