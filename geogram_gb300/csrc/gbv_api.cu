@@ -883,7 +883,11 @@ static void cells_device(gbv_context* c, const double* d_xyz, const double* d_w,
   while (morek > 0) {
     P.n_morek += morek;
     if (cur.k >= nm1) throw StatusError{GBV_ERR_STATE, "list growth did not terminate"};
-    const uint32_t batch = std::min<uint32_t>(kKnnSmemK, nm1 - cur.k);
+    // geometric growth: every round at least doubles the lists, so a cell
+    // that needs k neighbours (outer seeds of clustered inputs need
+    // thousands) takes O(log k) rounds and O(k) clips in all, instead of
+    // being re-clipped every 64 more
+    const uint32_t batch = std::min<uint32_t>(std::max<uint32_t>(kKnnSmemK, cur.k), nm1 - cur.k);
     const uint32_t newk = cur.k + batch;
     const std::string tag = std::to_string(round & 1);
     uint32_t* q_s = c->buf<uint32_t>("ext_s" + tag, morek);
@@ -914,6 +918,10 @@ static void cells_device(gbv_context* c, const double* d_xyz, const double* d_w,
     ka.last_idx = last_i;
     ka.flag_count = flag_count;
     ka.flag_list = flag_list;
+    if (batch > kKnnSmemK) {  // lists beyond the shared-memory heap
+      ka.gl_d2 = c->buf<double>("ext_gd2", (size_t)batch * morek);
+      ka.gl_slot = c->buf<uint32_t>("ext_gslot", (size_t)batch * morek);
+    }
     launch_knn(ka, st);
     add_count_kernel<<<nblocks(morek, 128), 128, 0, st>>>(cnt, morek, cur.k, q_r, cur.cnt); count_launch();
     GBV_CUDA(cudaGetLastError());
