@@ -610,6 +610,44 @@ __device__ __forceinline__ void write_outputs(const KnnArgs& a, const SortedSeed
   }
 }
 
+// (da, pa) > (db, pb) in the list order: distance, then original index
+__device__ __forceinline__ bool pair_greater(double da, uint32_t pa, double db, uint32_t pb) {
+  return da > db || (da == db && pa > pb);
+}
+
+// Puts (d, slot) (original index p) at position pos of the max-heap of size
+// `size` held in ld/ls (with stride) and sifts it down.
+__device__ __forceinline__ void heap_sift_down(double* ld, uint32_t* ls, uint32_t stride,
+                                               const uint32_t* __restrict__ perm, uint32_t pos,
+                                               uint32_t size, double d, uint32_t slot,
+                                               uint32_t p) {
+  for (;;) {
+    const uint32_t l = 2 * pos + 1;
+    if (l >= size) break;
+    uint32_t ch = l;
+    double dc = ld[(size_t)l * stride];
+    uint32_t sc = ls[(size_t)l * stride];
+    uint32_t pc = perm[sc];
+    if (l + 1 < size) {
+      const double dr = ld[(size_t)(l + 1) * stride];
+      const uint32_t sr = ls[(size_t)(l + 1) * stride];
+      const uint32_t pr = perm[sr];
+      if (pair_greater(dr, pr, dc, pc)) {
+        ch = l + 1;
+        dc = dr;
+        sc = sr;
+        pc = pr;
+      }
+    }
+    if (!pair_greater(dc, pc, d, p)) break;
+    ld[(size_t)pos * stride] = dc;
+    ls[(size_t)pos * stride] = sc;
+    pos = ch;
+  }
+  ld[(size_t)pos * stride] = d;
+  ls[(size_t)pos * stride] = slot;
+}
+
 // ---- exact search: FP64 distances of every candidate, FP64 list ---------
 // qsel: when non-null, the kernel runs only the queries qsel[0..*qcount).
 template <bool SMEM>
@@ -663,29 +701,63 @@ knn_exact_kernel(KnnArgs a, SortedSeeds S, const GridDesc* __restrict__ gdp,
         continue;
       }
       if (!after_lo(c, d, pj)) continue;
-      if (cnt == K) {
-        if (d > worst) continue;
-        if (d == worst && pj > S.perm[LS(K - 1)]) continue;
+      if constexpr (SMEM) {
+        // short lists (k <= 64): insertion into the sorted list
+        if (cnt == K) {
+          if (d > worst) continue;
+          if (d == worst && pj > S.perm[LS(K - 1)]) continue;
+        }
+        uint32_t pos = (cnt < K) ? cnt : K - 1;
+        while (pos > 0) {
+          const double dp = L(pos - 1);
+          if (dp < d) break;
+          if (dp == d && S.perm[LS(pos - 1)] < pj) break;
+          L(pos) = dp;
+          LS(pos) = LS(pos - 1);
+          --pos;
+        }
+        L(pos) = d;
+        LS(pos) = s2;
+        if (cnt < K) ++cnt;
+        if (cnt == K) worst = L(K - 1);
+      } else {
+        // long lists (up to every seed): a bounded max-heap on (d, index),
+        // O(log k) per candidate, sorted once at the end
+        if (cnt < K) {
+          uint32_t pos = cnt++;
+          while (pos > 0) {
+            const uint32_t par = (pos - 1) >> 1;
+            const double dp = L(par);
+            const uint32_t sp = LS(par);
+            if (!pair_greater(d, pj, dp, S.perm[sp])) break;
+            L(pos) = dp;
+            LS(pos) = sp;
+            pos = par;
+          }
+          L(pos) = d;
+          LS(pos) = s2;
+        } else {
+          if (!pair_greater(L(0), S.perm[LS(0)], d, pj)) continue;
+          heap_sift_down(ld, ls, stride, S.perm, 0, K, d, s2, pj);
+        }
+        if (cnt == K) worst = L(0);
       }
-      uint32_t pos = (cnt < K) ? cnt : K - 1;
-      while (pos > 0) {
-        const double dp = L(pos - 1);
-        if (dp < d) break;
-        if (dp == d && S.perm[LS(pos - 1)] < pj) break;
-        L(pos) = dp;
-        LS(pos) = LS(pos - 1);
-        --pos;
-      }
-      L(pos) = d;
-      LS(pos) = s2;
-      if (cnt < K) ++cnt;
       if (cnt == K) {
-        worst = L(K - 1);
         const float r = sqrtf(__double2float_ru(worst)) * 1.0000076f + delta;
         thr = r * r * 1.0000076f;
       }
     }
   });
+  if constexpr (!SMEM) {
+    // heapsort: the max-heap becomes the ascending list
+    for (uint32_t end = cnt; end > 1; --end) {
+      const double dl = L(end - 1);
+      const uint32_t sl = LS(end - 1);
+      L(end - 1) = L(0);
+      LS(end - 1) = LS(0);
+      heap_sift_down(ld, ls, stride, S.perm, 0, end - 1, dl, sl, S.perm[sl]);
+    }
+  }
   write_outputs(a, S, c, qi, cnt, copies, dup_lower, ld, ls, stride);
 }
 
