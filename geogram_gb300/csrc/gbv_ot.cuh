@@ -28,10 +28,11 @@ void assemble_hessian(const double* xyz, const uint32_t* rowptr, const uint32_t*
 void spmv_dot(const Hessian& H, const double* x, double* y, double* part, int nparts,
               cudaStream_t st);
 
-// Deterministic FP64 reductions to part[0..nparts) (Neumaier sums per block).
-// Also the grid of the SpMV and the reductions: 8 blocks of 256 threads per
-// SM of the GB300's 152, enough resident warps to cover HBM latency.
-constexpr int kOtParts = 8 * 152;
+// Deterministic FP64 reductions to part[0..nparts) (Neumaier sums per block);
+// also the grid of the SpMV.  256 blocks: a grid of 8 blocks per SM made the
+// dot products twice as slow (their per-block FP64 reduction is serial) and
+// did not speed up the SpMV.
+constexpr int kOtParts = 256;
 void dot_parts(const double* a, const double* b, uint32_t n, double* part, cudaStream_t st);
 
 // r = vol - nu; parts: [0] sum r^2 terms, [1] max |r_i| / nu_i, [2] min vol.
