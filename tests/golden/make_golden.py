@@ -66,9 +66,32 @@ def shell(m, n_background, seed):
     return np.concatenate([[[0.5, 0.5, 0.5]], 0.5 + d * r[:, None], bg])
 
 
+def laguerre_cases():
+    """Laguerre cells without the security radius: every other seed is a
+    candidate (k0 = n - 1), so weights of any spread give the exact cells --
+    the cells of the optimal-transport solver.  The weights are the optimal
+    transport weights of the seeds (uniform measure on the cube), from the
+    oracle's Newton solver: every cell has volume 1/n, the weights spread
+    far beyond the squared spacing."""
+    from oracle import ot
+    x = gmm(np.random.default_rng(5), 1200, 6, 0.04, 0.08)
+    w, _ = ot.newton(x, tol=1e-9, nthreads=8)
+    yield "laguerre_ot_1200", x, w
+
+
 def main(only=None):
     """Writes every fixture, or only those whose names are listed."""
     oracle.build_ref()
+    for name, x, w in laguerre_cases():
+        if only and name not in only:
+            continue
+        x = np.ascontiguousarray(x)
+        r = oracle.cells(x, w, k0=len(x) - 1, check_sr=False, nthreads=8, which="ref",
+                         max_nbr=400)
+        np.savez_compressed(os.path.join(HERE, f"cells_{name}.npz"), x=x, w=w, vol=r["vol"],
+                            mg=r["mg"], rowptr=r["rowptr"], nbr=r["nbr"], area=r["area"],
+                            status=r["status"], n_clip=r["n_clip"], k_list=r["k_list"])
+        print(name, len(x), "cells (every seed a candidate), nnz", len(r["nbr"]))
     for name, x, w in cases():
         if only and name not in only:
             continue

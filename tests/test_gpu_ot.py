@@ -79,6 +79,17 @@ def test_power_range_cells_vs_oracle(g, ot, case, prec):
     assert abs(c.volume.sum() - 1.0) < 1e-12
 
 
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_power_range_cells_vs_reference_fixture(g, prec):
+    """At optimal-transport weights, against geogram's own cells (every seed
+    a candidate; tests/golden/cells_laguerre_ot_1200.npz)."""
+    from conftest import load_golden
+    r = load_golden("cells_laguerre_ot_1200.npz")
+    c = g.compute_cells(r["x"], r["w"], precision=prec, certification="power_range")
+    assert_laguerre_equal(c, r, len(r["x"]))
+    assert np.max(np.abs(c.volume * len(r["x"]) - 1.0)) < 1e-8
+
+
 def test_power_range_equals_security_radius_on_voronoi(g):
     """Zero weights: both certifications give the same cells."""
     x = np.random.default_rng(5).random((3000, 3))

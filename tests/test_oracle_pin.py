@@ -87,3 +87,23 @@ def test_port_matches_reference_live(oracle_mod):
         b = oracle_mod.cells(x, ww, nthreads=8, which="port")
         for key in ("vol", "mg", "rowptr", "nbr", "area", "status", "n_clip", "k_list"):
             assert np.array_equal(a[key], b[key]), key
+
+
+def test_port_matches_reference_laguerre_fixture(oracle_mod):
+    """Laguerre cells with every seed as candidate (the cells of the OT
+    solver), at optimal-transport weights: bit for bit against geogram."""
+    g = load_golden("cells_laguerre_ot_1200.npz")
+    n = len(g["x"])
+    r = oracle_mod.cells(g["x"], g["w"], k0=n - 1, check_sr=False, nthreads=4)
+    for key in ("vol", "mg", "rowptr", "nbr", "area", "status", "n_clip", "k_list"):
+        assert np.array_equal(r[key], g[key]), key
+
+
+def test_reference_confirms_ot_weights():
+    """The fixture's weights come from the OT restatement; the reference's
+    own cells at those weights have volume 1/n: the solution satisfies the
+    mass condition by geogram's ConvexCell, not only by the oracle's."""
+    g = load_golden("cells_laguerre_ot_1200.npz")
+    n = len(g["x"])
+    assert np.max(np.abs(g["vol"] * n - 1.0)) < 1e-8
+    assert abs(g["vol"].sum() - 1.0) < 1e-12
