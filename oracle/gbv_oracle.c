@@ -834,7 +834,7 @@ static void cells_range(void* vctx, unsigned b, unsigned e) {
 
 /* Cells of seeds [i0, i1) of the n seeds (all n take part as neighbours);
  * outputs are indexed i - i0.  Same per-seed contract as ref_cells in
- * oracle/ref/ref_driver.cpp.  *n_exact receives the number of exact
+ * oracle/ref/ref_harness.cpp.  *n_exact receives the number of exact
  * (expansion) predicate evaluations. */
 int orc_cells_range(const double* xyz, const double* w, unsigned n, unsigned i0, unsigned i1,
                     unsigned k0, int check_sr, int exact, int nthreads, double* vol, double* mg,
@@ -865,7 +865,7 @@ int orc_cells_range(const double* xyz, const double* w, unsigned n, unsigned i0,
     return 0;
 }
 
-/* All n cells; same contract as ref_cells in oracle/ref/ref_driver.cpp. */
+/* All n cells; same contract as ref_cells in oracle/ref/ref_harness.cpp. */
 int orc_cells(const double* xyz, const double* w, unsigned n, unsigned k0, int check_sr,
               int exact, int nthreads, double* vol, double* mg, uint32_t* nbr_count,
               uint32_t* nbr_idx, double* nbr_area, unsigned max_nbr, uint32_t* k_list,

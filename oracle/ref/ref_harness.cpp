@@ -1,9 +1,9 @@
 /*
- * Oracle reference driver -- TEST INFRASTRUCTURE ONLY.
+ * Oracle reference harness -- TEST INFRASTRUCTURE ONLY.
  *
  * This file is compiled together with geogram's own sources, straight from
  * the reference checkout, into oracle/_ref/libgbv_ref.so (recipe:
- * oracle/ref/Makefile).  It is the checker for the CPU restatement in
+ * oracle/ref/Makefile).  It validates the CPU restatement in
  * oracle/gbv_oracle.c and for the GPU path; nothing in the product links or
  * calls it.
  *
