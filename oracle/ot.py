@@ -102,6 +102,34 @@ def pcg(H, b: np.ndarray, rtol: float, max_iter: int):
     return x - x.mean(), it
 
 
+def separable_start(xyz: np.ndarray, box_min=(0.0, 0.0, 0.0), box_max=(1.0, 1.0, 1.0)) -> np.ndarray:
+    """Starting weights from the seeds' marginal distributions (no reference
+    counterpart: the reference's solver starts from zero).
+
+    w = |p|^2 - 2 phi(p) with phi(p) = sum_a Phi_a(p_a), where Phi_a' = F_a
+    is the piecewise-linear interpolation of the empirical CDF of axis a
+    (rank k of n -> (k + 1/2) / n, mapped onto the box's extent).  For
+    product measures grad phi is the Brenier map onto the uniform box.
+
+    No cell of distinct seeds is empty.  Seed i's cell is the set of x where
+    x.p_i - phi(p_i) is largest over the seeds (the power distance
+    |x - p|^2 - w rearranged), and at x = grad phi(p_i) convexity gives
+    x.p_j - phi(p_j) < x.p_i - phi(p_i) for every j != i, strictly because
+    each Phi_a is strictly convex between distinct coordinates.  That x lies
+    strictly inside the box since 0 < F_a < 1, so the cell keeps a
+    neighbourhood of it.  Returned with mean zero."""
+    x = np.asarray(xyz, np.float64)
+    n = len(x)
+    w = (x * x).sum(1)
+    for a in range(3):
+        order = np.argsort(x[:, a], kind="stable")
+        s = x[order, a]
+        F = box_min[a] + (np.arange(n) + 0.5) / n * (box_max[a] - box_min[a])
+        Phi = np.concatenate([[0.0], np.cumsum(np.diff(s) * 0.5 * (F[1:] + F[:-1]))])
+        w[order] -= 2.0 * Phi
+    return w - w.mean()
+
+
 def newton(xyz: np.ndarray, nu: np.ndarray | None = None, w0: np.ndarray | None = None,
            tol: float = 1e-6, max_newton: int = 60, max_cg: int = 4000, nthreads: int = 4,
            cg_rtol: float = 1e-3, step_growth: float = 4.0):

@@ -56,3 +56,38 @@ def test_newton_converges_on_a_mixture(ot):
     v = ot.laguerre_cells(x, w)["vol"]
     assert np.max(np.abs(v * len(x) - 1.0)) < 1e-6
     assert abs(v.sum() - 1.0) < 1e-12
+
+
+@pytest.mark.parametrize("sigma,snap", [(0.005, 0), (0.02, 0), (0.05, 64)])
+def test_separable_start_empties_no_cell(ot, sigma, snap):
+    """No empty cell from the separable start, for tight clusters and for seeds
+    sharing coordinates (snapped to a 64-grid: many ties on every axis)."""
+    rng = np.random.default_rng(11)
+    x = gaussian_mixture(500, 8, sigma, rng)
+    if snap:
+        x = (np.floor(x * snap) + 0.5) / snap
+        x[:, 0] += rng.random(len(x)) * 1e-3   # keep the seeds distinct
+    w = ot.separable_start(x)
+    c = ot.laguerre_cells(x, w)
+    assert (c["vol"] > 0).all()
+    assert abs(c["vol"].sum() - 1.0) < 1e-12
+    # the certificate point grad phi(p_i) = (F_a(p_ia)) lies in cell i
+    n = len(x)
+    g = np.empty_like(x)
+    for a in range(3):
+        o = np.argsort(x[:, a], kind="stable")
+        g[o, a] = (np.arange(n) + 0.5) / n
+    pw = ((g[:, None, :] - x[None, :, :]) ** 2).sum(2) - w[None, :]
+    assert (pw.argmin(1) == np.arange(n)).all()
+
+
+def test_newton_from_separable_start(ot):
+    """Same solution as from zero (unique up to a constant), fewer cell passes."""
+    rng = np.random.default_rng(0)
+    x = gaussian_mixture(400, 8, 0.02, rng)
+    w0, i0 = ot.newton(x, tol=1e-8)
+    w1, i1 = ot.newton(x, w0=ot.separable_start(x), tol=1e-8)
+    assert i0["converged"] and i1["converged"]
+    d = (w1 - w1.mean()) - (w0 - w0.mean())
+    assert np.max(np.abs(d)) < 1e-6 * np.ptp(w0)
+    assert i1["cell_calls"] <= i0["cell_calls"]
