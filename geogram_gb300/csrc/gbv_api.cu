@@ -178,6 +178,18 @@ __global__ void facet_count_kernel(const uint32_t* __restrict__ slot_of,
   if (i == n) rowptr[n] = 0;
 }
 
+// Sum of the n per-cell facet counts in 64 bits (the CSR offsets are 32-bit);
+// *total must be zero on entry.
+__global__ void facet_total_kernel(const uint32_t* __restrict__ counts, uint32_t n,
+                                   unsigned long long* __restrict__ total) {
+  unsigned long long s = 0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    s += counts[i];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0 && s != 0) atomicAdd(total, s);
+}
+
 // Unsorts the per-cell results into the caller's order and writes the CSR.
 __global__ void unsort_kernel(const uint32_t* __restrict__ slot_of, uint32_t n,
                               const double* __restrict__ vol_s, const double* __restrict__ mg_s,
@@ -765,6 +777,19 @@ struct Pipeline {
     c->status = c->buf<int32_t>("status", n);
     c->rowptr = c->buf<uint32_t>("rowptr", (size_t)n + 1);
     facet_count_kernel<<<nblocks((size_t)n + 1, 256), 256, 0, st>>>(S.slot_of, nf, n, c->rowptr); count_launch();
+    // A cell has at most kHugeV facets, so below 2^32 / kHugeV cells the
+    // 32-bit offsets cannot wrap; above, the total is checked exactly.
+    if ((uint64_t)n * kHugeV > 0xffffffffull) {
+      unsigned long long* tot = c->buf<unsigned long long>("facet_total", 1);
+      GBV_CUDA(cudaMemsetAsync(tot, 0, sizeof(unsigned long long), st));
+      facet_total_kernel<<<4 * 152, 256, 0, st>>>(c->rowptr, n, tot); count_launch();
+      unsigned long long h_tot = 0;
+      GBV_CUDA(cudaMemcpyAsync(&h_tot, tot, sizeof h_tot, cudaMemcpyDeviceToHost, st));
+      GBV_CUDA(cudaStreamSynchronize(st));
+      if (h_tot > 0xffffffffull)
+        throw StatusError{GBV_ERR_CAPACITY, std::to_string(h_tot) +
+                                                " facets exceed the 32-bit CSR offsets"};
+    }
     uint32_t* stmp = c->buf<uint32_t>("csr_scan_tmp", scan_tmp_elems((size_t)n + 1));
     exclusive_scan_u32(c->rowptr, (size_t)n + 1, stmp, st);
     GBV_CUDA(cudaMemcpyAsync(&c->h_counts[0], c->rowptr + n, 4, cudaMemcpyDeviceToHost, st));
@@ -1827,7 +1852,7 @@ gbv_status gbv_create(int device, gbv_context** out) {
     GBV_CUDA(cudaMallocHost(&c->h_counts, 4 * sizeof(uint32_t)));
   });
   if (st != GBV_OK) {
-    delete c;
+    gbv_destroy(c);  // releases whatever was created before the failure
     return st;
   }
   *out = c;
