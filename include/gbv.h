@@ -165,7 +165,8 @@ gbv_status gbv_nn_get_nearest_neighbors_all(gbv_context* ctx, uint32_t k,
  * 3722-3726) until the security radius certifies the cell
  * (generic_RVD.h:2278-2352).  xyz: 3n doubles; w: n weights or NULL
  * (Voronoi).  Inputs are host pointers; results stay on the device until
- * gbv_cells_fetch().  The report may be NULL. */
+ * gbv_cells_fetch().  The report may be NULL.  GBV_ERR_CAPACITY when the
+ * cells' facets total 2^32 or more (the CSR offsets are 32-bit). */
 gbv_status gbv_cells_compute(gbv_context* ctx, const double* xyz,
                              const double* w, uint32_t n,
                              const gbv_cell_options* opt,
