@@ -329,6 +329,25 @@ def ot_solve_device(xyz_dev, w_dev, nu_dev=None, *, box=((0.0, 0.0, 0.0), (1.0, 
     return rep.as_dict()
 
 
+def ot_separable_start_device(xyz_dev, *, box=((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)), stream=None,
+                              ctx: Context | None = None):
+    """Starting weights for ot_solve_device from the seeds' marginal
+    distributions (float64 tensor, n; not centred): w = |p|^2 - 2 sum_a
+    Phi_a(p_a), Phi_a' the piecewise-linear CDF of axis a.  No cell of these
+    weights is empty for distinct seeds.  xyz_dev: float64 CUDA tensor, n x 3."""
+    import torch
+    ctx = ctx or default_context()
+    x = xyz_dev.contiguous()
+    if x.dtype != torch.float64 or x.dim() != 2 or x.shape[1] != 3:
+        raise ValueError("xyz_dev must be a float64 tensor of shape (n, 3)")
+    w = torch.empty(x.shape[0], dtype=torch.float64, device=x.device)
+    o = ot_options(box)
+    st = ctypes.c_void_p(stream.cuda_stream) if stream is not None else None
+    _lib.check(ctx._lib.gbv_ot_separable_start(ctx.handle, _lib.ptr(x), x.shape[0],
+                                               ctypes.byref(o), _lib.ptr(w), st))
+    return w
+
+
 def ot_gradient_hessian(xyz: np.ndarray, w: np.ndarray, nu: np.ndarray | None = None, *,
                         box=((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)), precision="fp32",
                         ctx: Context | None = None):

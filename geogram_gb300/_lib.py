@@ -158,6 +158,7 @@ SIGNATURES = {
                                          _P]),
     "gbv_ot_solve_learned_device": (ctypes.c_int, [_P, _P, _P, _U32, ctypes.POINTER(OtOptions),
                                                    _P, _P, _P, _P, ctypes.POINTER(OtReport)]),
+    "gbv_ot_separable_start": (ctypes.c_int, [_P, _P, _U32, ctypes.POINTER(OtOptions), _P, _P]),
     "gbv_mlp_gemm_nt": (ctypes.c_int, [_P, _P, ctypes.c_int, _P, ctypes.c_int, _P, ctypes.c_int,
                                        ctypes.c_int, ctypes.c_int, ctypes.c_int, _P]),
     "gbv_knn_noalloc": (ctypes.c_int, [_P, _U32, _U32, _U32, _U32, _P, _P, _P]),

@@ -4,7 +4,8 @@
                                       [--weights 1e-4] [--precision fp32|fp64]
                                       [--certification security_radius|power_range]
     python -m geogram_gb300.cli ot --n 1000000 [--mixture 8 --sigma 0.05]
-                                   [--learned | --levels] [--max-newton N] [--tol 1e-6]
+                                   [--learned | --levels | --start separable]
+                                   [--max-newton N] [--tol 1e-6]
 
 The counterpart of the reference's compute_RVD / compute_OTM programs for
 meshless cells in the unit cube (src/examples/exploragram/compute_OTM/
@@ -61,6 +62,8 @@ def main(argv=None) -> None:
     o.add_argument("--learned", action="store_true", help="start from the learned warm start")
     o.add_argument("--levels", action="store_true",
                    help="multilevel solve (optimize_levels): coarse-to-fine subsets")
+    o.add_argument("--start", default="zero", choices=("zero", "separable"),
+                   help="plain solve from zero weights or from the separable marginal-CDF start")
     o.add_argument("--ratio", type=int, default=8)
     o.add_argument("--min-level", type=int, default=20000)
     o.add_argument("--max-newton", type=int, default=100)
@@ -94,8 +97,13 @@ def main(argv=None) -> None:
                 rep = WarmStartModel.load().solve(x, w, tol=args.tol, max_newton=args.max_newton,
                                                   precision=args.precision)
             else:
+                ts = time.perf_counter()
+                if args.start == "separable":
+                    w = g.ot_separable_start_device(x)
+                t_start = time.perf_counter() - ts
                 rep = g.ot_solve_device(x, w, tol=args.tol, max_newton=args.max_newton,
                                         precision=args.precision)
+                rep = dict(rep, start=args.start, start_s=t_start)
         torch.cuda.synchronize()
         out = dict(rep, wall_s=time.perf_counter() - t0)
     now, peak = ctx.device_bytes()

@@ -30,6 +30,7 @@
 #include "gbv_clip.cuh"
 #include "gbv_ot.cuh"
 #include "gbv_mlp.cuh"
+#include "gbv_start.cuh"
 
 namespace {
 
@@ -2138,6 +2139,25 @@ gbv_status gbv_ot_warm_start(gbv_context* c, const double* d_xyz, uint32_t n,
     gbv_ot_options o = *opt;
     o.max_newton = 0;
     ot_solve(c, d_xyz, nullptr, n, o, d_w, st, nullptr, d_params, d_norm);
+  });
+}
+
+gbv_status gbv_ot_separable_start(gbv_context* c, const double* d_xyz, uint32_t n,
+                                  const gbv_ot_options* opt, double* d_w, void* stream) {
+  if (!c || !d_xyz || !d_w) return fail(GBV_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (n == 0 || n > 0x80000000u) return fail(GBV_ERR_INVALID_ARGUMENT, "n must be in [1, 2^31]");
+  gbv_status s = check_ot_opts(opt);
+  if (s != GBV_OK) return s;
+  return guarded([&] {
+    GBV_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    const size_t m = start_sort_len(n);
+    double* key = c->buf<double>("start_key", m);
+    uint32_t* val = c->buf<uint32_t>("start_val", m);
+    double* chunk = c->buf<double>("start_chunk", start_chunks(n));
+    separable_start(d_xyz, n, opt->box_min, opt->box_max, key, val, chunk, d_w, st);
+    GBV_CUDA(cudaGetLastError());
+    GBV_CUDA(cudaStreamSynchronize(st));
   });
 }
 

@@ -349,6 +349,14 @@ gbv_status gbv_ot_solve_learned_device(gbv_context* ctx, const double* d_xyz, co
                                        uint32_t n, const gbv_ot_options* opt,
                                        const float* d_params, const float* d_norm, double* d_w,
                                        void* stream, gbv_ot_report* report);
+/* Separable start (no reference counterpart: the reference's solver starts
+ * from zero): w_i = |p_i|^2 - 2 sum_a Phi_a(p_ia), Phi_a' the piecewise-
+ * linear empirical CDF of axis a mapped onto the box of opt (the seed of
+ * rank k to box_min + (k + 1/2)/n (box_max - box_min)).  For distinct seeds
+ * no cell of these weights is empty.  d_xyz [3n] device seeds, d_w [n]
+ * receives the weights (not centred), 1 <= n <= 2^31. */
+gbv_status gbv_ot_separable_start(gbv_context* ctx, const double* d_xyz, uint32_t n,
+                                  const gbv_ot_options* opt, double* d_w, void* stream);
 /* The tensor-core product the network uses, exposed for testing:
  * C[M][N] (FP32, ldc) = A[M][K] Bt[N][K]^T, A and Bt BF16 row-major, K a
  * multiple of 32, lda and ldb multiples of 8. */
