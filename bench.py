@@ -9,7 +9,7 @@ geometry; the seeds then move to their centroids (CVT Lloyd step,
 voronoi/CVT.cpp:133-167).  Steps are consecutive Lloyd iterations.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--ot-n N]
+                    [--ot-n N] [--ot-cpu-n N]
 
 Prints one JSON line.  `value` is cells/s with the seeds resident on the
 GPU (CUDA events on the library's stream, L2 flushed between steps);
@@ -20,7 +20,9 @@ machine's cores.  --impl reference times that CPU implementation alone on
 the same workload.  `ot` adds the optimal-transport half of the headline
 metric: solve time from zero weights, from the learned start and with the
 multilevel solve (--ot-n seeds of the clustered mixture, 1,000,000 by
-default: about 50 s per solve).
+default: about 50 s per solve); its `cpu_baseline` times the CPU restatement
+of the solver (oracle/ot.py) on --ot-cpu-n seeds of the same mixture with the
+GPU solver on the same seeds beside it.
 """
 from __future__ import annotations
 
@@ -292,6 +294,11 @@ def run_ours(args) -> None:
         }
         if args.ot_n > 0:
             line["ot"] = run_ot(args.ot_n, ctx)
+            if args.ot_cpu_n > 0:
+                try:
+                    line["ot"]["cpu_baseline"] = ot_cpu_baseline(args.ot_cpu_n, ctx)
+                except Exception as e:  # a reported baseline: never lose the line for it
+                    line["ot"]["cpu_baseline"] = {"error": f"{type(e).__name__}: {e}"}
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.barrier()
@@ -353,6 +360,32 @@ def run_ot(n: int, ctx) -> dict:
             "multilevel": levels, "multilevel_speedup": tp / tv}
 
 
+def ot_cpu_baseline(n: int, ctx) -> dict:
+    """The OT restatement (oracle/ot.py: exact Laguerre cells, damped Newton,
+    Jacobi PCG) on the host with every core, on a bounded sample: n seeds of
+    the same mixture; the GPU solver on the same seeds beside it."""
+    import torch
+    import geogram_gb300 as g
+    from oracle import ot
+    cores = os.cpu_count() or 1
+    x = gaussian_mixture(n, 8, 0.05, np.random.default_rng(0))
+    t0 = time.perf_counter()
+    _, info = ot.newton(x, tol=1e-6, nthreads=cores)
+    t_cpu = time.perf_counter() - t0
+    xd = torch.tensor(x, device="cuda")
+    wd = torch.zeros(n, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    rep = g.ot_solve_device(xd, wd, tol=1e-6, ctx=ctx)
+    torch.cuda.synchronize()
+    t_gpu = time.perf_counter() - t0
+    return {"kind": "restatement", "cores": cores, "n": n, "seconds": t_cpu,
+            "newton_iters": info["iters"], "converged": info["converged"],
+            "gpu_seconds_same_seeds": t_gpu, "gpu_newton_iters": rep["newton_iters"],
+            "sample": f"OT of {n} seeds of the same mixture (seed 0) to mass error 1e-6, "
+                      f"oracle/ot.py on oracle/gbv_oracle.c with {cores} threads"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -364,6 +397,8 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=50_000)
     ap.add_argument("--ot-n", type=int, default=1_000_000,
                     help="seeds of the optimal-transport comparison (0: skip)")
+    ap.add_argument("--ot-cpu-n", type=int, default=2000,
+                    help="seeds of the CPU optimal-transport baseline sample (0: skip)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
