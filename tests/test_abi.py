@@ -59,3 +59,26 @@ def test_no_device_is_an_error_not_a_fallback():
     with pytest.raises(g.GbvError) as e:
         g.Context(0)
     assert e.value.status == 3  # GBV_ERR_NO_DEVICE
+
+
+# entry points that take no context first (or report through another channel)
+NO_CONTEXT = {"gbv_last_error", "gbv_kernel_launches", "gbv_device_bytes", "gbv_create",
+              "gbv_destroy", "gbv_cell_options_default", "gbv_ot_options_default",
+              "gbv_knn_noalloc"}
+
+
+def test_null_context_is_an_argument_error(lib):
+    """Every entry point that takes a context rejects NULL with
+    GBV_ERR_INVALID_ARGUMENT and a message, before touching a device."""
+    from geogram_gb300 import _lib
+    L = _lib.load()
+    checked = 0
+    for name, (_, argtypes) in _lib.SIGNATURES.items():
+        if name in NO_CONTEXT:
+            continue
+        args = [None if (t in (ctypes.c_void_p, ctypes.c_char_p) or issubclass(t, ctypes._Pointer))
+                else t(0) for t in argtypes]
+        assert getattr(L, name)(*args) == 1, name
+        assert L.gbv_last_error(), name
+        checked += 1
+    assert checked >= 20

@@ -1,5 +1,6 @@
 """Host-side Python pieces that need no GPU: the warm-start network's
-parameter layout and stored model, and the command-line seed generator."""
+parameter layout and stored model, the command-line seed generator and the
+bench's clock record."""
 import numpy as np
 
 
@@ -38,3 +39,18 @@ def test_cli_seed_generator():
     h = seeds(5000, 32, 0.05, 1, (0.01, 0.1))
     assert h.shape == (5000, 3) and np.all((h > 0) & (h < 1))
     assert np.array_equal(seeds(100, 4, 0.05, 7), seeds(100, 4, 0.05, 7))
+
+
+def test_bench_clock_summary_reports_throttle_reasons():
+    """The bench's clock record: median SM clock under load, and every
+    throttle reason seen active in any sample."""
+    import bench
+    cs = bench.ClockSampler(0)
+    assert cs.summary()["reasons"] == ["no nvidia-smi samples"]
+    off = ["Not Active"] * 4
+    cs.samples = [["0", "2070", "2070", "900.5", "0x0", *off],
+                  ["0", "1980", "2070", "1400.0", "0x4", *off[:3], "Active"],
+                  ["0", "2070", "2070", "1000.0", "0x8", "Active", *off[:3]]]
+    s = cs.summary()
+    assert s["sm_mhz"] == 2070 and s["sm_max_mhz"] == 2070 and s["samples"] == 3
+    assert s["reasons"] == ["hw_slowdown", "sw_power_cap"]
