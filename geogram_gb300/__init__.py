@@ -19,6 +19,9 @@ reference's C++ one:
                           driven by compute_OTM/main.cpp:280-296): damped
                           Newton on the weights, the dual's gradient and
                           Laguerre Hessian
+  ot_separable_start_device
+                          an analytic start for it from the seeds' marginal
+                          distributions (no reference counterpart)
 
 Everything runs on the GPU through libgbv.so (C ABI in include/gbv.h).
 Host arrays are numpy; device arrays are torch CUDA tensors.
@@ -41,7 +44,7 @@ __all__ = [
     "CELL_STALLED",
     "PRECISION_FP64", "PRECISION_FP32_RECHECK", "cell_options", "CERTIFY_SECURITY_RADIUS",
     "CERTIFY_POWER_RANGE", "ot_options", "ot_solve", "ot_solve_device", "ot_gradient_hessian",
-    "ot_solve_levels", "ot_solve_levels_device",
+    "ot_solve_levels", "ot_solve_levels_device", "ot_separable_start_device",
 ]
 
 
@@ -234,6 +237,24 @@ def compute_cells(xyz: np.ndarray, weights: np.ndarray | None = None, *,
     return Cells(vol, mg, rowptr, nbr[:rep.nnz], area[:rep.nnz], status, rep.as_dict())
 
 
+def _dev_arg(t, name: str, n: int | None = None, cols: int | None = None):
+    """A device argument as the C ABI reads it: a contiguous float64 CUDA
+    tensor, n x cols (cols given) or n (cols None); None passes through.
+    The entry points get raw pointers, so anything else would be misread."""
+    if t is None:
+        return None
+    if not (getattr(t, "is_cuda", False) and str(t.dtype) == "torch.float64"
+            and t.is_contiguous()):
+        raise ValueError(f"{name} must be a contiguous float64 CUDA tensor")
+    shape = tuple(t.shape)
+    want_dim = 1 if cols is None else 2
+    if len(shape) != want_dim or (cols is not None and shape[1] != cols) or \
+            (n is not None and shape[0] != n):
+        raise ValueError(f"{name} has shape {shape}, expected "
+                         f"{(n if n is not None else 'n',) + (() if cols is None else (cols,))}")
+    return t
+
+
 def compute_cells_device(xyz, weights=None, *, box=((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)),
                          k0: int = 20, check_sr: bool = True, precision="fp64",
                          certification: str = "security_radius", stream=None,
@@ -241,7 +262,8 @@ def compute_cells_device(xyz, weights=None, *, box=((0.0, 0.0, 0.0), (1.0, 1.0, 
     """Same on torch CUDA tensors (float64, n x 3 and n); results stay on
     the device (read them with device_results)."""
     ctx = ctx or default_context()
-    n = xyz.shape[0]
+    n = _dev_arg(xyz, "xyz", cols=3).shape[0]
+    _dev_arg(weights, "weights", n)
     o = cell_options(box, k0, check_sr, precision, certification)
     rep = CellReport()
     st = ctypes.c_void_p(stream.cuda_stream) if stream is not None else None
@@ -286,6 +308,8 @@ def lloyd_iterations(xyz_dev, iters: int, weights_dev=None, *,
                      ctx: Context | None = None) -> dict:
     """`iters` Lloyd iterations in place on a torch CUDA tensor (n x 3)."""
     ctx = ctx or default_context()
+    n = _dev_arg(xyz_dev, "xyz_dev", cols=3).shape[0]
+    _dev_arg(weights_dev, "weights_dev", n)
     o = cell_options(box, 20, True, precision)
     rep = CellReport()
     st = ctypes.c_void_p(stream.cuda_stream) if stream is not None else None
@@ -320,6 +344,9 @@ def ot_solve_device(xyz_dev, w_dev, nu_dev=None, *, box=((0.0, 0.0, 0.0), (1.0, 
                     stream=None, ctx: Context | None = None) -> dict:
     """ot_solve on torch CUDA tensors; w_dev (float64, n) is updated in place."""
     ctx = ctx or default_context()
+    n = _dev_arg(xyz_dev, "xyz_dev", cols=3).shape[0]
+    _dev_arg(w_dev, "w_dev", n)
+    _dev_arg(nu_dev, "nu_dev", n)
     o = ot_options(box, tol, max_newton, max_cg, precision, cg_rtol, step_growth)
     rep = OtReport()
     st = ctypes.c_void_p(stream.cuda_stream) if stream is not None else None
@@ -337,9 +364,7 @@ def ot_separable_start_device(xyz_dev, *, box=((0.0, 0.0, 0.0), (1.0, 1.0, 1.0))
     weights is empty for distinct seeds.  xyz_dev: float64 CUDA tensor, n x 3."""
     import torch
     ctx = ctx or default_context()
-    x = xyz_dev.contiguous()
-    if x.dtype != torch.float64 or x.dim() != 2 or x.shape[1] != 3:
-        raise ValueError("xyz_dev must be a float64 tensor of shape (n, 3)")
+    x = _dev_arg(xyz_dev, "xyz_dev", cols=3)
     w = torch.empty(x.shape[0], dtype=torch.float64, device=x.device)
     o = ot_options(box)
     st = ctypes.c_void_p(stream.cuda_stream) if stream is not None else None
@@ -402,6 +427,9 @@ def ot_solve_levels_device(xyz_dev, w_dev, nu_dev=None, *, ratio: int = 8,
                            stream=None, ctx: Context | None = None) -> dict:
     """ot_solve_levels on torch CUDA tensors; w_dev (float64, n) receives the weights."""
     ctx = ctx or default_context()
+    n = _dev_arg(xyz_dev, "xyz_dev", cols=3).shape[0]
+    _dev_arg(w_dev, "w_dev", n)
+    _dev_arg(nu_dev, "nu_dev", n)
     o = ot_options(box, tol, max_newton, precision=precision)
     rep = OtReport()
     st = ctypes.c_void_p(stream.cuda_stream) if stream is not None else None
