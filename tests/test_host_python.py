@@ -54,3 +54,19 @@ def test_bench_clock_summary_reports_throttle_reasons():
     s = cs.summary()
     assert s["sm_mhz"] == 2070 and s["sm_max_mhz"] == 2070 and s["samples"] == 3
     assert s["reasons"] == ["hw_slowdown", "sw_power_cap"]
+
+
+def test_device_argument_check():
+    """Device entry points get raw pointers: the wrappers refuse host tensors,
+    other dtypes, wrong shapes and non-contiguous views before any call."""
+    import pytest
+    import torch
+    import geogram_gb300 as g
+    assert g._dev_arg(None, "w", 5) is None
+    x = torch.zeros((5, 3), dtype=torch.float64)
+    for bad, kw in ((x, dict(cols=3)),                                  # host memory
+                    (x.float(), dict(cols=3)),
+                    (x.t(), dict(cols=3)),
+                    (x[:, 0], dict(n=5))):
+        with pytest.raises(ValueError):
+            g._dev_arg(bad, "t", **kw)
