@@ -420,6 +420,16 @@ static void clip_by_plane(cell_t* C, v4 eqn, uint32_t j, int exact) {
         }
         t = next;
     }
+    if (head == END_OF_LIST) {
+        /* The plane cuts nothing.  The reference keeps it as an unused
+         * vertex (convex_cell.cpp:467-476); no triangle refers to it and the
+         * facets are read in insertion order, so dropping it changes no
+         * output, and it keeps the 16-bit plane indices of the triangles
+         * (convex_cell.h:309-321) from wrapping in cells clipped by more
+         * than 65535 neighbours. */
+        --C->nb_v;
+        return;
+    }
     triangulate_conflict_zone(C, lv, head, tail);
     C->vglobal[lv] = j;
 }
@@ -773,6 +783,10 @@ static void cells_range(void* vctx, unsigned b, unsigned e) {
             if (list == 0) { st = 2; break; }
             if (prev == list) { st = 3; break; }
             for (; jj < list; ++jj) {
+                /* Beyond the 16-bit indices (65535 planes; triangle links
+                 * below END_OF_LIST, and one clip at most doubles the
+                 * triangles): status 5, the cell as clipped so far. */
+                if (C.nb_v >= 65534 || C.nb_t >= END_OF_LIST / 2) { st = 5; done = 1; break; }
                 uint32_t j = nb[jj];
                 double R2 = squared_radius(&C, (v3){xi[0], xi[1], xi[2]});
                 if (c->dim == 4) R2 += c->hl[i] * c->hl[i];
@@ -835,7 +849,10 @@ static void cells_range(void* vctx, unsigned b, unsigned e) {
 /* Cells of seeds [i0, i1) of the n seeds (all n take part as neighbours);
  * outputs are indexed i - i0.  Same per-seed contract as ref_cells in
  * oracle/ref/ref_harness.cpp.  *n_exact receives the number of exact
- * (expansion) predicate evaluations. */
+ * (expansion) predicate evaluations.  status: 0 certified, 1 every seed
+ * used, 2 duplicate, 3 list growth stalled, 4 more facets than max_nbr,
+ * 5 beyond the 16-bit plane / triangle indices of the reference's cell
+ * (the cell as clipped until then). */
 int orc_cells_range(const double* xyz, const double* w, unsigned n, unsigned i0, unsigned i1,
                     unsigned k0, int check_sr, int exact, int nthreads, double* vol, double* mg,
                     uint32_t* nbr_count, uint32_t* nbr_idx, double* nbr_area, unsigned max_nbr,
