@@ -3,26 +3,30 @@
 
 Workload (one step = one pass of the cell engine plus the Lloyd update):
 power diagram of 1,000,000 seeds uniform in the unit cube, weights uniform
-in [0, 1e-4], clipped to the unit box with the security-radius loop, FP32
-clipping with FP64 re-clip of every cell FP32 cannot certify, FP64
-geometry; the seeds then move to their centroids (CVT Lloyd step,
-voronoi/CVT.cpp:133-167).  Steps are consecutive Lloyd iterations.
+in [0, 1e-4] (seed 0), clipped to the unit box with the security-radius
+loop, FP32 clipping with FP64 re-clip of every cell FP32 cannot certify,
+FP64 geometry; the seeds then move to their centroids (CVT Lloyd step,
+voronoi/CVT.cpp:133-167).  Every step starts from the seeded positions,
+so each step computes the same diagram (the first of the ten Lloyd
+iterations of the workload) in both arms.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--ot-n N] [--ot-cpu-n N]
+                    [--ot-n N] [--ot-cpu-n N] [--extras 0|1]
 
 Prints one JSON line.  `value` is cells/s with the seeds resident on the
 GPU (CUDA events on the library's stream, L2 flushed between steps);
 `e2e` is the same through the C ABI with host arrays (host->device and
 device->host copies inside the timed region); `cpu_baseline` times the
-CPU restatement of the reference (oracle/) on a bounded sample on this
-machine's cores.  --impl reference times that CPU implementation alone on
-the same workload.  `ot` adds the optimal-transport half of the headline
-metric: solve time from zero weights, from the learned start and with the
-multilevel solve (--ot-n seeds of the clustered mixture, 1,000,000 by
-default: about 50 s per solve); its `cpu_baseline` times the CPU restatement
-of the solver (oracle/ot.py) on --ot-cpu-n seeds of the same mixture with the
-GPU solver on the same seeds beside it.
+CPU restatement of the reference (oracle/) on a bounded sample of the
+same diagram on this machine's cores, its grid build amortised over all
+the seeds.  --impl reference times that CPU implementation alone on the
+same workload.  `c2_lloyd10` runs the workload's ten Lloyd iterations;
+`c1` the 100k-seed Voronoi diagram in FP64 with one Lloyd step.  `ot` adds
+the optimal-transport half of the headline metric: solve time from zero
+weights and from the starts (--ot-n seeds of the clustered mixture,
+1,000,000 by default); its `cpu_baseline` times the CPU restatement of the
+solver (oracle/ot.py) on --ot-cpu-n seeds of the same mixture with the GPU
+solver on the same seeds beside it.
 """
 from __future__ import annotations
 
@@ -45,10 +49,15 @@ N_SEEDS = 1_000_000
 # ncu capture (67.10 MB read + 229.45 MB written)
 KNN_TRAFFIC_BYTES = 296.55e6
 W_MAX = 1e-4
-METRIC = "Laguerre cells/s (power diagram, 1M seeds, FP32 clip + FP64 re-clip, one Lloyd step)"
+METRIC = ("Laguerre cells/s (power diagram, 1M seeds, FP32 clip + FP64 re-clip, "
+          "Lloyd step from the seeded start)")
 WORKLOAD = ("power diagram of 1M seeds uniform in [0,1]^3, weights U[0,1e-4], seed 0; "
-            "certified cells clipped to the unit box, FP32 clipping + FP64 re-clip, "
-            "one Lloyd iteration per step")
+            "certified cells (k0 = 20, security radius) clipped to the unit box, "
+            "one Lloyd update; every step from the seeded positions")
+# identical in both arms: the same diagram, the same per-cell work
+CONFIG = {"workload": WORKLOAD, "n_seeds": N_SEEDS, "weights": "U[0,1e-4]", "seed": 0,
+          "diagram": "seeded start (first of the workload's 10 Lloyd iterations)",
+          "k0": 20, "certification": "security radius 4.1 R^2"}
 
 
 def make_inputs(n: int, seed: int = 0):
@@ -115,15 +124,30 @@ def load_peaks() -> tuple[float, str]:
         return 6800.0, "fallback"
 
 
+def cpu_sample(pc, i0: int, m: int, cores: int) -> tuple[float, float]:
+    """Seconds for cells [i0, i0 + m) of the prepared diagram plus their
+    share of the grid build, and the sample's mean clips per cell."""
+    r = pc.range(i0, i0 + m, cores)
+    # the Lloyd update of the sample (CVT.cpp:133-167: seeds of empty cells stay)
+    m_ = r["vol"][:, None]
+    xs = np.where(m_ > 1e-30, r["mg"].reshape(-1, 3) / np.where(m_ > 1e-30, m_, 1.0), 0.0)
+    del xs
+    return r["seconds"] + pc.build_seconds * m / pc.n, r["mean_clips"]
+
+
 def cpu_baseline(x: np.ndarray, w: np.ndarray, sample: int) -> dict:
     """The oracle (CPU restatement of the reference path) on cells [0, sample)
-    of the same seeds, with every host core."""
+    of the same diagram, with every host core."""
     from oracle import oracle
     cores = os.cpu_count() or 1
-    dt = oracle.cells_range_time(x, w, 0, sample, cores)
+    pc = oracle.PreparedCells(x, w)
+    dt, clips = cpu_sample(pc, 0, sample, cores)
+    pc.close()
     return {"value": sample / dt, "unit": "cells/s", "cores": cores, "kind": "port",
-            "sample": f"cells 0..{sample} of the {len(x)}-seed power diagram (all seeds as "
-                      f"neighbours), oracle/gbv_oracle.c with {cores} threads, {dt:.2f} s"}
+            "mean_clips": clips,
+            "sample": f"cells 0..{sample} of the {len(x)}-seed power diagram at the seeded "
+                      f"start (all seeds as neighbours), oracle/gbv_oracle.c with {cores} "
+                      f"threads, {dt:.2f} s incl. the grid build's share"}
 
 
 def max_over_ranks(x: float) -> float:
@@ -147,12 +171,16 @@ def run_reference(args) -> None:
     from oracle import oracle
     cores = os.cpu_count() or 1
     m = args.ref_sample
+    pc = oracle.PreparedCells(x, w)
     for s in range(args.warmup):
-        oracle.cells_range_time(x, w, 0, m, cores)
-    times = []
+        cpu_sample(pc, (s * m) % (N_SEEDS - m), m, cores)
+    times, clips = [], []
     for s in range(args.steps):
-        i0 = (s * m) % (N_SEEDS - m)
-        times.append(oracle.cells_range_time(x, w, i0, i0 + m, cores))
+        i0 = ((s + args.warmup) * m) % (N_SEEDS - m)
+        dt, cl = cpu_sample(pc, i0, m, cores)
+        times.append(dt)
+        clips.append(cl)
+    pc.close()
     total = sum(times)
     value = m * args.steps / total
     line = {
@@ -160,10 +188,14 @@ def run_reference(args) -> None:
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded numpy)",
-        "config": {"workload": WORKLOAD, "n_seeds": N_SEEDS, "sample_cells_per_step": m},
+        "config": dict(CONFIG),
+        "mean_clips": statistics.mean(clips),
+        "timing": {"sample_cells_per_step": m, "grid_build_s": pc.build_seconds,
+                   "grid_build": "once, amortised: each step adds build_s * m / n"},
         "cpu_baseline": {"value": value, "unit": "cells/s", "cores": cores, "kind": "port",
-                         "sample": f"{m} cells per step of the {N_SEEDS}-seed power diagram, "
-                                   f"oracle/gbv_oracle.c with {cores} threads"},
+                         "sample": f"{m} cells per step of the {N_SEEDS}-seed power diagram at "
+                                   f"the seeded start, oracle/gbv_oracle.c with {cores} "
+                                   f"threads"},
         "e2e": {"value": value, "unit": "cells/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -187,7 +219,8 @@ def run_ours(args) -> None:
     ctx = g.Context(local)
     lib = _lib.load()
     x_h, w_h = make_inputs(N_SEEDS, seed=rank)
-    x = torch.from_numpy(x_h).to(dev)
+    x0 = torch.from_numpy(x_h).to(dev)
+    x = x0.clone()
     w = torch.from_numpy(w_h).to(dev)
     stream = torch.cuda.current_stream(dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
@@ -196,6 +229,7 @@ def run_ours(args) -> None:
         return g.lloyd_iterations(x, 1, w, precision=args.precision, stream=stream, ctx=ctx)
 
     for _ in range(args.warmup):
+        x.copy_(x0)
         step()
     torch.cuda.synchronize()
     if world > 1:
@@ -207,6 +241,7 @@ def run_ours(args) -> None:
     ev_e = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     with ClockSampler(local) as clk:
         for s in range(args.steps):
+            x.copy_(x0)           # the seeded positions again, outside the events
             flush.fill_(float(s))  # L2 flush (256 MB > 126 MB L2), outside the events
             ev_s[s].record(stream)
             reports.append(step())
@@ -219,15 +254,15 @@ def run_ours(args) -> None:
     total_ms = max_over_ranks(sum(step_ms))
     value = world * N_SEEDS * args.steps / (total_ms / 1e3)
 
-    # ---- e2e through the C ABI with host arrays (H2D + compute + D2H)
-    xe = x_h.copy()
+    # ---- e2e through the C ABI with host arrays (H2D + compute + D2H),
+    # every step from the seeded positions
     e2e_t = []
-    for s in range(max(2, args.steps // 2)):
+    for s in range(max(3, args.steps // 2)):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        xe, _ = g.lloyd_step(xe, w_h, precision=args.precision, ctx=ctx)
+        g.lloyd_step(x_h, w_h, precision=args.precision, ctx=ctx)
         e2e_t.append(time.perf_counter() - t0)
-    e2e_value = world * N_SEEDS / statistics.mean(e2e_t[1:] if len(e2e_t) > 1 else e2e_t)
+    e2e_value = world * N_SEEDS / statistics.mean(e2e_t[1:])
 
     if rank == 0:
         # ---- the dominant kernel's roofline (kNN, HBM): algorithmic bytes per
@@ -241,22 +276,23 @@ def run_ours(args) -> None:
         peak, peak_kind = load_peaks()
         # ---- plain FP64 path on the same seeds, and the error of this mode
         # against it (both modes reproduce the reference's FP64 results)
-        xs = x.clone()
         torch.cuda.synchronize()
-        rep32 = g.compute_cells_device(xs, w, precision=args.precision, stream=stream, ctx=ctx)
+        g.compute_cells_device(x0, w, precision=args.precision, stream=stream, ctx=ctx)
         c32 = g.device_results(ctx)
-        rep64 = g.compute_cells_device(xs, w, precision="fp64", stream=stream, ctx=ctx)
+        g.compute_cells_device(x0, w, precision="fp64", stream=stream, ctx=ctx)
         c64 = g.device_results(ctx)
         t64 = []
-        for _ in range(2):
+        for _ in range(3):
+            flush.fill_(1.0)
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            g.compute_cells_device(xs, w, precision="fp64", stream=stream, ctx=ctx)
+            g.compute_cells_device(x0, w, precision="fp64", stream=stream, ctx=ctx)
             e1.record(stream)
             torch.cuda.synchronize()
             t64.append(e0.elapsed_time(e1))
-        fp64_cps = N_SEEDS / (min(t64) / 1e3)
+        fp64_cps = N_SEEDS / (statistics.median(t64) / 1e3)
+        t32 = statistics.median(r["ms_total"] for r in reports)
         rel_vol = float(np.max(np.abs(c32["volume"] - c64["volume"]) /
                                np.maximum(np.abs(c64["volume"]), 1e-300)))
         abs_mg = float(np.max(np.abs(c32["mg"] - c64["mg"])))
@@ -269,8 +305,11 @@ def run_ours(args) -> None:
             "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64",
             "data": "synthetic (seeded numpy, uniform seeds and weights)",
-            "config": {"workload": WORKLOAD, "n_seeds": N_SEEDS, "precision": args.precision,
-                       "l2": "flushed between steps (256 MB write)",
+            "config": dict(CONFIG),
+            "mean_clips": rep["mean_clips"],
+            "timing": {"precision": args.precision, "l2": "flushed between steps (256 MB write)",
+                       "seeds": "reset to the seeded positions before each step, outside "
+                                "the timed region",
                        "parallelism": "replicas only" if world > 1 else "1 GPU"},
             "roofline": {"kernel": "knn_fast_kernel (first kNN pass)", "bound": "hbm",
                          "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -286,12 +325,16 @@ def run_ours(args) -> None:
             "clocks": clk.summary(),
             "phases_ms": {kk: round(statistics.median(r[kk] for r in reports), 3)
                           for kk in ("ms_grid", "ms_knn", "ms_clip", "ms_retry", "ms_total")},
-            "cells": {kk: reports[-1][kk] for kk in ("n_recheck_fp64", "n_more_k", "n_overflow",
-                                                     "mean_clips", "max_clips", "nnz")},
-            "fp64_plain": {"cells_per_s": fp64_cps, "speedup_of_this_mode": value / fp64_cps,
+            "cells": {kk: rep[kk] for kk in ("n_recheck_fp64", "n_more_k", "n_overflow",
+                                             "mean_clips", "max_clips", "nnz", "knn_k")},
+            "fp64_plain": {"cells_per_s": fp64_cps, "ms": statistics.median(t64),
+                           "speedup_of_this_mode": statistics.median(t64) / t32,
                            "max_rel_vol_err_vs_fp64": rel_vol, "max_abs_mg_err_vs_fp64": abs_mg,
                            "neighbour_lists_identical": same_nbr},
         }
+        if args.extras:
+            line["c2_lloyd10"] = run_lloyd10(x0, w, args.precision, stream, ctx, flush)
+            line["c1"] = run_c1(ctx, stream)
         if args.ot_n > 0:
             line["ot"] = run_ot(args.ot_n, ctx)
             if args.ot_cpu_n > 0:
@@ -303,6 +346,65 @@ def run_ours(args) -> None:
     if world > 1:
         dist.barrier()
         dist.destroy_process_group()
+
+
+def run_lloyd10(x0, w, precision: str, stream, ctx, flush) -> dict:
+    """The workload as written: ten Lloyd iterations from the seeded start,
+    each timed with CUDA events (L2 flushed before each)."""
+    import torch
+    import geogram_gb300 as g
+    x = x0.clone()
+    ms, clips = [], []
+    for _ in range(10):
+        flush.fill_(2.0)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        r = g.lloyd_iterations(x, 1, w, precision=precision, stream=stream, ctx=ctx)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+        clips.append(round(r["mean_clips"], 3))
+    return {"iterations": 10, "total_ms": sum(ms), "ms_per_iteration": [round(v, 3) for v in ms],
+            "mean_clips_per_iteration": clips,
+            "cells_per_s": 10 * len(x0) / (sum(ms) / 1e3)}
+
+
+def run_c1(ctx, stream) -> dict:
+    """100k seeds uniform in the unit cube (seed 0), Voronoi (zero weights),
+    FP64, k0 = 20 with security-radius growth, one Lloyd step: GPU time, and
+    the CPU restatement on all its cells with every host core."""
+    import torch
+    import geogram_gb300 as g
+    from oracle import oracle
+    n = 100_000
+    xh = np.random.default_rng(0).random((n, 3))
+    x0 = torch.from_numpy(xh).cuda()
+    x = x0.clone()
+    ms = []
+    for s in range(8):
+        x.copy_(x0)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        r = g.lloyd_iterations(x, 1, None, precision="fp64", stream=stream, ctx=ctx)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if s >= 3:
+            ms.append(e0.elapsed_time(e1))
+    cores = os.cpu_count() or 1
+    pc = oracle.PreparedCells(xh, None)
+    out = pc.range(0, n, cores)
+    cpu_s = out["seconds"] + pc.build_seconds
+    pc.close()
+    gpu_ms = statistics.median(ms)
+    return {"workload": "Voronoi of 100k seeds U[0,1]^3 (seed 0), FP64, k0 = 20 + security "
+                        "radius, one Lloyd step",
+            "gpu_ms": gpu_ms, "gpu_cells_per_s": n / (gpu_ms / 1e3),
+            "mean_clips": r["mean_clips"],
+            "cpu_baseline": {"kind": "port", "cores": cores, "seconds": cpu_s,
+                             "cells_per_s": n / cpu_s, "mean_clips": out["mean_clips"],
+                             "sample": "all 100k cells, grid build included"}}
 
 
 def gaussian_mixture(n: int, k: int, sigma: float, rng: np.random.Generator) -> np.ndarray:
@@ -393,10 +495,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--precision", default="fp32")
-    ap.add_argument("--cpu-sample", type=int, default=100_000)
+    ap.add_argument("--cpu-sample", type=int, default=200_000)
     ap.add_argument("--ref-sample", type=int, default=50_000)
     ap.add_argument("--ot-n", type=int, default=1_000_000,
                     help="seeds of the optimal-transport comparison (0: skip)")
+    ap.add_argument("--extras", type=int, default=1,
+                    help="1: add the ten-iteration workload and the 100k Voronoi line")
     ap.add_argument("--ot-cpu-n", type=int, default=2000,
                     help="seeds of the CPU optimal-transport baseline sample (0: skip)")
     args = ap.parse_args()

@@ -833,7 +833,7 @@ static void cells_range(void* vctx, unsigned b, unsigned e) {
             }
             ++cnt;
         }
-        if (cnt > c->max_nbr) st = 4;
+        if (cnt > c->max_nbr && st != 5) st = 4;
         c->nbr_count[o] = cnt;
         c->k_list[o] = list;
         c->n_clip[o] = jj;
@@ -846,40 +846,82 @@ static void cells_range(void* vctx, unsigned b, unsigned e) {
     cell_free(&C);
 }
 
-/* Cells of seeds [i0, i1) of the n seeds (all n take part as neighbours);
- * outputs are indexed i - i0.  Same per-seed contract as ref_cells in
- * oracle/ref/ref_harness.cpp.  *n_exact receives the number of exact
- * (expansion) predicate evaluations.  status: 0 certified, 1 every seed
- * used, 2 duplicate, 3 list growth stalled, 4 more facets than max_nbr,
- * 5 beyond the 16-bit plane / triangle indices of the reference's cell
- * (the cell as clipped until then). */
+/* Seeds, their 4-d lift and the grid, built once for any number of cell
+ * ranges (the reference builds its kd-tree once per point set too). */
+typedef struct {
+    const double* xyz;
+    const double* w;
+    double* pts;
+    double* hl;
+    unsigned dim, n;
+    grid_t g;
+} prepared_t;
+
+void* orc_cells_prepare(const double* xyz, const double* w, unsigned n) {
+    if (n < 2) return NULL;
+    prepared_t* p = (prepared_t*)calloc(1, sizeof(prepared_t));
+    unsigned dim = w ? 4u : 3u;
+    p->xyz = xyz;
+    p->w = w;
+    p->dim = dim;
+    p->n = n;
+    p->pts = (double*)malloc(sizeof(double) * (size_t)n * dim);
+    p->hl = (double*)calloc(n, sizeof(double));
+    if (w) {
+        double W = w[0];
+        for (unsigned i = 1; i < n; ++i) W = w[i] > W ? w[i] : W;
+        for (unsigned i = 0; i < n; ++i) p->hl[i] = sqrt(W - w[i]);
+    }
+    for (unsigned i = 0; i < n; ++i) {
+        for (int c = 0; c < 3; ++c) p->pts[(size_t)i * dim + c] = xyz[3 * (size_t)i + c];
+        if (dim == 4) p->pts[(size_t)i * dim + 3] = p->hl[i];
+    }
+    grid_build(&p->g, p->pts, dim, n);
+    return p;
+}
+
+void orc_cells_release(void* h) {
+    prepared_t* p = (prepared_t*)h;
+    if (!p) return;
+    grid_free(&p->g);
+    free(p->pts);
+    free(p->hl);
+    free(p);
+}
+
+/* Cells of seeds [i0, i1) of a prepared seed set (all n seeds take part
+ * as neighbours); outputs are indexed i - i0.  Same per-seed contract as
+ * ref_cells in oracle/ref/ref_harness.cpp.  *n_exact receives the number
+ * of exact (expansion) predicate evaluations.  status: 0 certified, 1
+ * every seed used, 2 duplicate, 3 list growth stalled, 4 more facets than
+ * max_nbr, 5 beyond the 16-bit plane / triangle indices of the
+ * reference's cell (the cell as clipped until then). */
+int orc_cells_prepared_range(void* h, unsigned i0, unsigned i1, unsigned k0, int check_sr,
+                             int exact, int nthreads, double* vol, double* mg,
+                             uint32_t* nbr_count, uint32_t* nbr_idx, double* nbr_area,
+                             unsigned max_nbr, uint32_t* k_list, uint32_t* n_clip, int* status,
+                             long* n_exact) {
+    prepared_t* p = (prepared_t*)h;
+    if (!p || i0 > i1 || i1 > p->n) return 1;
+    cells_ctx c = {p->xyz, p->w, p->pts, p->hl, p->dim, p->n, k0, max_nbr, check_sr, exact,
+                   &p->g, vol, mg, nbr_count, nbr_idx, k_list, n_clip, nbr_area, status, 0, i0};
+    run_parallel_range(cells_range, &c, i0, i1, nthreads);
+    if (n_exact) *n_exact = c.n_exact;
+    return 0;
+}
+
+/* Cells of seeds [i0, i1) of the n seeds: prepare, range, release. */
 int orc_cells_range(const double* xyz, const double* w, unsigned n, unsigned i0, unsigned i1,
                     unsigned k0, int check_sr, int exact, int nthreads, double* vol, double* mg,
                     uint32_t* nbr_count, uint32_t* nbr_idx, double* nbr_area, unsigned max_nbr,
                     uint32_t* k_list, uint32_t* n_clip, int* status, long* n_exact) {
     if (n < 2 || i0 > i1 || i1 > n) return 1;
-    unsigned dim = w ? 4u : 3u;
-    double* pts = (double*)malloc(sizeof(double) * (size_t)n * dim);
-    double* hl = (double*)calloc(n, sizeof(double));
-    if (w) {
-        double W = w[0];
-        for (unsigned i = 1; i < n; ++i) W = w[i] > W ? w[i] : W;
-        for (unsigned i = 0; i < n; ++i) hl[i] = sqrt(W - w[i]);
-    }
-    for (unsigned i = 0; i < n; ++i) {
-        for (int c = 0; c < 3; ++c) pts[(size_t)i * dim + c] = xyz[3 * (size_t)i + c];
-        if (dim == 4) pts[(size_t)i * dim + 3] = hl[i];
-    }
-    grid_t g;
-    grid_build(&g, pts, dim, n);
-    cells_ctx c = {xyz, w, pts, hl, dim, n, k0, max_nbr, check_sr, exact, &g,
-                   vol, mg, nbr_count, nbr_idx, k_list, n_clip, nbr_area, status, 0, i0};
-    run_parallel_range(cells_range, &c, i0, i1, nthreads);
-    if (n_exact) *n_exact = c.n_exact;
-    grid_free(&g);
-    free(pts);
-    free(hl);
-    return 0;
+    void* h = orc_cells_prepare(xyz, w, n);
+    int r = orc_cells_prepared_range(h, i0, i1, k0, check_sr, exact, nthreads, vol, mg,
+                                     nbr_count, nbr_idx, nbr_area, max_nbr, k_list, n_clip,
+                                     status, n_exact);
+    orc_cells_release(h);
+    return r;
 }
 
 /* All n cells; same contract as ref_cells in oracle/ref/ref_harness.cpp. */

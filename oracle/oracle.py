@@ -20,7 +20,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_LIB = os.path.join(HERE, "libgbv_oracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libgbv_ref.so")
-REF_SRC = "/root/reference"
+# the reference checkout: GEOGRAM_SRC in the environment, else the usual
+# read-only mount
+REF_SRC = os.environ.get("GEOGRAM_SRC", "/root/reference")
 
 _port = None
 _ref = None
@@ -54,6 +56,12 @@ def port():
         lib.orc_det4_sign.argtypes = [P, P, P, P]
         lib.orc_cells_range.argtypes = [P, P, U, U, U, U, ctypes.c_int, ctypes.c_int,
                                         ctypes.c_int, P, P, P, P, P, U, P, P, P, P]
+        lib.orc_cells_prepare.argtypes = [P, P, U]
+        lib.orc_cells_prepare.restype = ctypes.c_void_p
+        lib.orc_cells_release.argtypes = [P]
+        lib.orc_cells_release.restype = None
+        lib.orc_cells_prepared_range.argtypes = [P, U, U, U, ctypes.c_int, ctypes.c_int,
+                                                 ctypes.c_int, P, P, P, P, P, U, P, P, P, P]
         _port = lib
     return _port
 
@@ -132,27 +140,66 @@ def cells(xyz: np.ndarray, w: np.ndarray | None = None, k0: int = 20, check_sr: 
     return out
 
 
+class PreparedCells:
+    """The CPU restatement's seed set with its grid built once (the
+    reference builds its kd-tree once per point set); cell ranges are then
+    computed against all the seeds.  `build_seconds` is the preparation time,
+    which a per-cell timing amortises over the n seeds."""
+
+    def __init__(self, xyz: np.ndarray, w: np.ndarray | None):
+        import time
+        self.x = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+        self.n = len(self.x)
+        self.w = None if w is None else np.ascontiguousarray(w, dtype=np.float64)
+        t = time.perf_counter()
+        self.h = port().orc_cells_prepare(_p(self.x), _p(self.w), self.n)
+        self.build_seconds = time.perf_counter() - t
+        if not self.h:
+            raise RuntimeError("oracle prepare failed")
+
+    def range(self, i0: int, i1: int, nthreads: int, k0: int = 20, max_nbr: int = 96) -> dict:
+        """Cells [i0, i1): seconds taken, clips per cell and the results."""
+        import time
+        m = i1 - i0
+        out = dict(vol=np.zeros(m), mg=np.zeros(3 * m), cnt=np.zeros(m, np.uint32),
+                   nidx=np.zeros(m * max_nbr, np.uint32), narea=np.zeros(m * max_nbr),
+                   k_list=np.zeros(m, np.uint32), n_clip=np.zeros(m, np.uint32),
+                   status=np.zeros(m, np.int32))
+        ne = ctypes.c_long(0)
+        t = time.perf_counter()
+        r = port().orc_cells_prepared_range(
+            self.h, i0, i1, k0, 1, 1, nthreads, _p(out["vol"]), _p(out["mg"]), _p(out["cnt"]),
+            _p(out["nidx"]), _p(out["narea"]), max_nbr, _p(out["k_list"]), _p(out["n_clip"]),
+            _p(out["status"]), ctypes.byref(ne))
+        out["seconds"] = time.perf_counter() - t
+        if r != 0 or (out["status"] == 4).any():
+            raise RuntimeError("oracle cells failed")
+        out["mean_clips"] = float(out["n_clip"].mean()) if m else 0.0
+        return out
+
+    def close(self) -> None:
+        if self.h:
+            port().orc_cells_release(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def cells_range_time(xyz: np.ndarray, w: np.ndarray | None, i0: int, i1: int,
                      nthreads: int, max_nbr: int = 96) -> float:
-    """Seconds the CPU restatement takes for cells [i0, i1) of all the seeds
-    (the bounded CPU-baseline sample); raises if a cell failed."""
+    """Seconds the CPU restatement takes for cells [i0, i1) of all the seeds,
+    grid build included (the bounded CPU-baseline sample); raises if a cell
+    failed."""
     import time
-    x = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
-    n = len(x)
-    wa = None if w is None else np.ascontiguousarray(w, dtype=np.float64)
-    m = i1 - i0
-    vol = np.zeros(m); mg = np.zeros(3 * m); cnt = np.zeros(m, np.uint32)
-    ni = np.zeros(m * max_nbr, np.uint32); na = np.zeros(m * max_nbr)
-    kl = np.zeros(m, np.uint32); nc = np.zeros(m, np.uint32); st = np.zeros(m, np.int32)
-    ne = ctypes.c_long(0)
     t = time.perf_counter()
-    r = port().orc_cells_range(_p(x), _p(wa), n, i0, i1, 20, 1, 1, nthreads, _p(vol), _p(mg),
-                               _p(cnt), _p(ni), _p(na), max_nbr, _p(kl), _p(nc), _p(st),
-                               ctypes.byref(ne))
-    dt = time.perf_counter() - t
-    if r != 0 or (st == 4).any():
-        raise RuntimeError("oracle cells failed")
-    return dt
+    pc = PreparedCells(xyz, w)
+    pc.range(i0, i1, nthreads, max_nbr=max_nbr)
+    pc.close()
+    return time.perf_counter() - t
 
 
 def det4_sign(p0, p1, p2, p3) -> int:
