@@ -237,15 +237,20 @@ def compute_cells(xyz: np.ndarray, weights: np.ndarray | None = None, *,
     return Cells(vol, mg, rowptr, nbr[:rep.nnz], area[:rep.nnz], status, rep.as_dict())
 
 
-def _dev_arg(t, name: str, n: int | None = None, cols: int | None = None):
+def _dev_arg(t, name: str, n: int | None = None, cols: int | None = None,
+             ctx: Context | None = None):
     """A device argument as the C ABI reads it: a contiguous float64 CUDA
-    tensor, n x cols (cols given) or n (cols None); None passes through.
-    The entry points get raw pointers, so anything else would be misread."""
+    tensor on the context's device, n x cols (cols given) or n (cols None);
+    None passes through.  The entry points get raw pointers, so anything
+    else would be misread (another GPU's tensor would be read without peer
+    access)."""
     if t is None:
         return None
     if not (getattr(t, "is_cuda", False) and str(t.dtype) == "torch.float64"
             and t.is_contiguous()):
         raise ValueError(f"{name} must be a contiguous float64 CUDA tensor")
+    if ctx is not None and t.device.index != ctx.device:
+        raise ValueError(f"{name} is on cuda:{t.device.index}, the context on cuda:{ctx.device}")
     shape = tuple(t.shape)
     want_dim = 1 if cols is None else 2
     if len(shape) != want_dim or (cols is not None and shape[1] != cols) or \
@@ -262,8 +267,8 @@ def compute_cells_device(xyz, weights=None, *, box=((0.0, 0.0, 0.0), (1.0, 1.0, 
     """Same on torch CUDA tensors (float64, n x 3 and n); results stay on
     the device (read them with device_results)."""
     ctx = ctx or default_context()
-    n = _dev_arg(xyz, "xyz", cols=3).shape[0]
-    _dev_arg(weights, "weights", n)
+    n = _dev_arg(xyz, "xyz", cols=3, ctx=ctx).shape[0]
+    _dev_arg(weights, "weights", n, ctx=ctx)
     o = cell_options(box, k0, check_sr, precision, certification)
     rep = CellReport()
     st = ctypes.c_void_p(stream.cuda_stream) if stream is not None else None
@@ -308,8 +313,8 @@ def lloyd_iterations(xyz_dev, iters: int, weights_dev=None, *,
                      ctx: Context | None = None) -> dict:
     """`iters` Lloyd iterations in place on a torch CUDA tensor (n x 3)."""
     ctx = ctx or default_context()
-    n = _dev_arg(xyz_dev, "xyz_dev", cols=3).shape[0]
-    _dev_arg(weights_dev, "weights_dev", n)
+    n = _dev_arg(xyz_dev, "xyz_dev", cols=3, ctx=ctx).shape[0]
+    _dev_arg(weights_dev, "weights_dev", n, ctx=ctx)
     o = cell_options(box, 20, True, precision)
     rep = CellReport()
     st = ctypes.c_void_p(stream.cuda_stream) if stream is not None else None
@@ -344,9 +349,9 @@ def ot_solve_device(xyz_dev, w_dev, nu_dev=None, *, box=((0.0, 0.0, 0.0), (1.0, 
                     stream=None, ctx: Context | None = None) -> dict:
     """ot_solve on torch CUDA tensors; w_dev (float64, n) is updated in place."""
     ctx = ctx or default_context()
-    n = _dev_arg(xyz_dev, "xyz_dev", cols=3).shape[0]
-    _dev_arg(w_dev, "w_dev", n)
-    _dev_arg(nu_dev, "nu_dev", n)
+    n = _dev_arg(xyz_dev, "xyz_dev", cols=3, ctx=ctx).shape[0]
+    _dev_arg(w_dev, "w_dev", n, ctx=ctx)
+    _dev_arg(nu_dev, "nu_dev", n, ctx=ctx)
     o = ot_options(box, tol, max_newton, max_cg, precision, cg_rtol, step_growth)
     rep = OtReport()
     st = ctypes.c_void_p(stream.cuda_stream) if stream is not None else None
@@ -364,7 +369,7 @@ def ot_separable_start_device(xyz_dev, *, box=((0.0, 0.0, 0.0), (1.0, 1.0, 1.0))
     weights is empty for distinct seeds.  xyz_dev: float64 CUDA tensor, n x 3."""
     import torch
     ctx = ctx or default_context()
-    x = _dev_arg(xyz_dev, "xyz_dev", cols=3)
+    x = _dev_arg(xyz_dev, "xyz_dev", cols=3, ctx=ctx)
     w = torch.empty(x.shape[0], dtype=torch.float64, device=x.device)
     o = ot_options(box)
     st = ctypes.c_void_p(stream.cuda_stream) if stream is not None else None
@@ -427,9 +432,9 @@ def ot_solve_levels_device(xyz_dev, w_dev, nu_dev=None, *, ratio: int = 8,
                            stream=None, ctx: Context | None = None) -> dict:
     """ot_solve_levels on torch CUDA tensors; w_dev (float64, n) receives the weights."""
     ctx = ctx or default_context()
-    n = _dev_arg(xyz_dev, "xyz_dev", cols=3).shape[0]
-    _dev_arg(w_dev, "w_dev", n)
-    _dev_arg(nu_dev, "nu_dev", n)
+    n = _dev_arg(xyz_dev, "xyz_dev", cols=3, ctx=ctx).shape[0]
+    _dev_arg(w_dev, "w_dev", n, ctx=ctx)
+    _dev_arg(nu_dev, "nu_dev", n, ctx=ctx)
     o = ot_options(box, tol, max_newton, precision=precision)
     rep = OtReport()
     st = ctypes.c_void_p(stream.cuda_stream) if stream is not None else None

@@ -321,7 +321,7 @@ static void setup_seeds(gbv_context* c, uint32_t n, bool weighted) {
   c->scr.rank = c->buf<uint32_t>("rank", n);
   c->scr.scan_tmp_elems = scan_tmp_elems(((size_t)1 << (3 * L)) + 1);
   c->scr.scan_tmp = c->buf<uint32_t>("scan_tmp", c->scr.scan_tmp_elems);
-  c->scr.red = c->buf<double>("red", 8 * 128);
+  c->scr.red = c->buf<double>("red", 8 * (size_t)kBboxParts);
 }
 
 static inline unsigned nblocks(size_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
@@ -1767,6 +1767,23 @@ static void ot_solve_levels(gbv_context* c, const double* xyz, const double* nu,
   }
 }
 
+// Device arguments must be memory of the context's device (or managed
+// memory): the kernels run on c->device, and another GPU's memory read
+// without peer access is an illegal address.  Checked before any launch.
+static void require_device(const gbv_context* c, const void* p, const char* name) {
+  if (!p) return;
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    throw StatusError{GBV_ERR_INVALID_ARGUMENT, std::string(name) + " is not device memory"};
+  }
+  if (at.type == cudaMemoryTypeManaged) return;
+  if (at.type != cudaMemoryTypeDevice || at.device != c->device)
+    throw StatusError{GBV_ERR_INVALID_ARGUMENT,
+                      std::string(name) + " must be device memory of the context's device " +
+                          std::to_string(c->device)};
+}
+
 template <class F>
 static gbv_status guarded(F&& f) {
   try {
@@ -1880,6 +1897,7 @@ gbv_status gbv_cells_compute_device(gbv_context* c, const double* d_xyz, const d
   if (s != GBV_OK) return s;
   return guarded([&] {
     GBV_CUDA(cudaSetDevice(c->device));
+    require_device(c, d_xyz, "d_xyz"); require_device(c, d_w, "d_w");
     cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
     if (opt->certification == GBV_CERTIFY_POWER_RANGE)
       laguerre_device(c, d_xyz, d_w, n, opt->box_min, opt->box_max,
@@ -1949,6 +1967,7 @@ gbv_status gbv_lloyd_device(gbv_context* c, double* d_xyz, const double* d_w, ui
   if (s != GBV_OK) return s;
   return guarded([&] {
     GBV_CUDA(cudaSetDevice(c->device));
+    require_device(c, d_xyz, "d_xyz"); require_device(c, d_w, "d_w");
     cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
     for (uint32_t it = 0; it < iters; ++it) {
       cells_device(c, d_xyz, d_w, n, *opt, st, report);
@@ -2071,6 +2090,7 @@ gbv_status gbv_mlp_features(gbv_context* c, const double* d_xyz, uint32_t n, flo
   if (!c || !d_xyz || !d_raw) return fail(GBV_ERR_INVALID_ARGUMENT, "NULL argument");
   return guarded([&] {
     GBV_CUDA(cudaSetDevice(c->device));
+    require_device(c, d_xyz, "d_xyz"); require_device(c, d_raw, "d_raw");
     cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
     mlp_features_device(c, d_xyz, n, d_raw, st);
     GBV_CUDA(cudaStreamSynchronize(st));
@@ -2084,6 +2104,8 @@ gbv_status gbv_mlp_forward(gbv_context* c, const float* d_params, const float* d
   if (n == 0) return fail(GBV_ERR_INVALID_ARGUMENT, "n must be > 0");
   return guarded([&] {
     GBV_CUDA(cudaSetDevice(c->device));
+    require_device(c, d_params, "d_params"); require_device(c, d_norm, "d_norm");
+    require_device(c, d_raw, "d_raw"); require_device(c, d_y, "d_y");
     cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
     mlp_forward_all(c, d_params, d_norm, d_raw, n, d_y, st);
     GBV_CUDA(cudaStreamSynchronize(st));
@@ -2099,6 +2121,9 @@ gbv_status gbv_mlp_loss_grad(gbv_context* c, const float* d_params, const float*
     return fail(GBV_ERR_INVALID_ARGUMENT, "batch must hold 1 to GBV_MLP_MAX_BATCH rows");
   return guarded([&] {
     GBV_CUDA(cudaSetDevice(c->device));
+    require_device(c, d_params, "d_params"); require_device(c, d_norm, "d_norm");
+    require_device(c, d_raw, "d_raw"); require_device(c, d_target, "d_target");
+    require_device(c, d_grad, "d_grad");
     cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
     MlpBuffers B = mlp_buffers(c, n);
     mlp_loss_grad(d_params, d_norm, d_raw, d_target, n, d_grad, B, st);
@@ -2120,6 +2145,8 @@ gbv_status gbv_mlp_adam(gbv_context* c, float* d_params, float* d_m, float* d_v,
   if (step == 0) return fail(GBV_ERR_INVALID_ARGUMENT, "step counts from 1");
   return guarded([&] {
     GBV_CUDA(cudaSetDevice(c->device));
+    require_device(c, d_params, "d_params"); require_device(c, d_m, "d_m");
+    require_device(c, d_v, "d_v"); require_device(c, d_grad, "d_grad");
     cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
     mlp_adam(d_params, d_m, d_v, d_grad, step, lr, beta1, beta2, eps, st);
     GBV_CUDA(cudaGetLastError());
@@ -2135,6 +2162,8 @@ gbv_status gbv_ot_warm_start(gbv_context* c, const double* d_xyz, uint32_t n,
   if (s != GBV_OK) return s;
   return guarded([&] {
     GBV_CUDA(cudaSetDevice(c->device));
+    require_device(c, d_xyz, "d_xyz"); require_device(c, d_params, "d_params");
+    require_device(c, d_norm, "d_norm"); require_device(c, d_w, "d_w");
     cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
     gbv_ot_options o = *opt;
     o.max_newton = 0;
@@ -2150,6 +2179,7 @@ gbv_status gbv_ot_separable_start(gbv_context* c, const double* d_xyz, uint32_t 
   if (s != GBV_OK) return s;
   return guarded([&] {
     GBV_CUDA(cudaSetDevice(c->device));
+    require_device(c, d_xyz, "d_xyz"); require_device(c, d_w, "d_w");
     cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
     const size_t m = start_sort_len(n);
     double* key = c->buf<double>("start_key", m);
@@ -2170,6 +2200,8 @@ gbv_status gbv_ot_solve_levels_device(gbv_context* c, const double* d_xyz, const
   if (s != GBV_OK) return s;
   return guarded([&] {
     GBV_CUDA(cudaSetDevice(c->device));
+    require_device(c, d_xyz, "d_xyz"); require_device(c, d_nu, "d_nu");
+    require_device(c, d_w, "d_w");
     cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
     ot_solve_levels(c, d_xyz, d_nu, n, *opt, ratio, min_level, d_w, st, report);
   });
@@ -2205,6 +2237,9 @@ gbv_status gbv_ot_solve_learned_device(gbv_context* c, const double* d_xyz, cons
   if (s != GBV_OK) return s;
   return guarded([&] {
     GBV_CUDA(cudaSetDevice(c->device));
+    require_device(c, d_xyz, "d_xyz"); require_device(c, d_nu, "d_nu");
+    require_device(c, d_params, "d_params"); require_device(c, d_norm, "d_norm");
+    require_device(c, d_w, "d_w");
     cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
     ot_solve(c, d_xyz, d_nu, n, *opt, d_w, st, report, d_params, d_norm);
   });
@@ -2220,6 +2255,7 @@ gbv_status gbv_mlp_gemm_nt(gbv_context* c, const void* d_a, int lda, const void*
     return fail(GBV_ERR_INVALID_ARGUMENT, "operands must be 16-byte aligned");
   return guarded([&] {
     GBV_CUDA(cudaSetDevice(c->device));
+    require_device(c, d_a, "d_a"); require_device(c, d_bt, "d_bt"); require_device(c, d_c, "d_c");
     cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
     gemm_nt((const bf16*)d_a, lda, (const bf16*)d_bt, ldb, d_c, ldc, M, N, K, 1, 0, st);
     GBV_CUDA(cudaStreamSynchronize(st));
@@ -2250,6 +2286,8 @@ gbv_status gbv_ot_solve_device(gbv_context* c, const double* d_xyz, const double
   if (s != GBV_OK) return s;
   return guarded([&] {
     GBV_CUDA(cudaSetDevice(c->device));
+    require_device(c, d_xyz, "d_xyz"); require_device(c, d_nu, "d_nu");
+    require_device(c, d_w, "d_w");
     cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
     ot_solve(c, d_xyz, d_nu, n, *opt, d_w, st, report);
   });

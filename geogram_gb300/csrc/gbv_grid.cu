@@ -73,14 +73,7 @@ __global__ void scan_add_kernel(uint32_t* __restrict__ data, size_t n,
   }
 }
 
-size_t scan_tmp_elems(size_t n) {
-  size_t tot = 0;
-  while (n > (size_t)kScanBlock) {
-    n = (n + kScanBlock - 1) / kScanBlock;
-    tot += n + 1;
-  }
-  return tot + 1;
-}
+static_assert(kScanBlock == kScanBlockElems, "scan block size and scan_tmp_elems disagree");
 
 void exclusive_scan_u32(uint32_t* data, size_t n, uint32_t* tmp, cudaStream_t st) {
   if (n == 0) return;
@@ -452,7 +445,7 @@ int choose_levels(uint32_t n) {
 
 void build_grid(const double* xyz, uint32_t stride, uint32_t dim, const double* w,
                 uint32_t n, int L, SortedSeeds& S, GridScratch& scr, cudaStream_t st) {
-  const int nparts = 120;
+  const int nparts = kBboxParts;
   bbox_partial_kernel<<<nparts, kRedThreads, 0, st>>>(xyz, stride, dim, w, n, scr.red); count_launch();
   bbox_final_kernel<<<1, 32, 0, st>>>(scr.red, nparts, L, w != nullptr, (int)dim, S.gd,
                                       S.aux); count_launch();

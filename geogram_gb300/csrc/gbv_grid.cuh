@@ -32,8 +32,20 @@ struct GridScratch {
 };
 
 // Exclusive scan of n uint32 values in place; tmp must hold
-// scan_tmp_elems(n) entries.
-size_t scan_tmp_elems(size_t n);
+// scan_tmp_elems(n) entries (1024 values per block, partial sums scanned
+// recursively).
+constexpr size_t kScanBlockElems = 1024;
+constexpr size_t scan_tmp_elems(size_t n) {
+  size_t tot = 0;
+  while (n > kScanBlockElems) {
+    n = (n + kScanBlockElems - 1) / kScanBlockElems;
+    tot += n + 1;
+  }
+  return tot + 1;
+}
+// Blocks of the bounding-box reduction of build_grid; GridScratch::red holds
+// 8 doubles per block.
+constexpr int kBboxParts = 120;
 void exclusive_scan_u32(uint32_t* data, size_t n, uint32_t* tmp, cudaStream_t st);
 
 // Chooses L from n (about one seed per fine cell, 1 <= L <= 9).

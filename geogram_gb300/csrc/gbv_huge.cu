@@ -15,11 +15,11 @@
 // 1350-1433): planes are vertices, corners are triangles with their three
 // adjacent triangles, and the valid triangles form a singly linked list
 // through the fourth 16-bit field.  Clipping (clip_by_plane,
-// convex_cell.cpp:812-858) walks the list, moves the triangles in conflict
+// convex_cell.cpp:467-516) walks the list, moves the triangles in conflict
 // to a conflict list and relinks the others in reverse order; the border of
 // the conflict zone is fanned from the last border edge met
-// (triangulate_conflict_zone, convex_cell.cpp:914-1001); freed triangles
-// are reused first (new_triangle, convex_cell.h:1182-1206).  Corners,
+// (triangulate_conflict_zone, convex_cell.cpp:761-865); freed triangles
+// are reused first (new_triangle, convex_cell.h:1143-1166).  Corners,
 // radii, volumes, centroids and facet areas use the reference's FP64
 // formulas operation for operation (gbv_refgeom.cuh), and compute_mg and
 // facet_area walk the same fans in the same order (convex_cell.cpp:

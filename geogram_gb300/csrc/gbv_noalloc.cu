@@ -20,14 +20,16 @@
 // results.  Order them on one stream, or synchronise between them.
 //
 // Host code must not use the array's name as a device address: in host code
-// it names a host-side stand-in.  The first call on each device looks up the
-// array's device address with cudaGetSymbolAddress (with that device
-// current) and caches it; that first call should therefore come before any
+// it names a host-side stand-in.  Every call looks up the array's address in
+// the current device's context with cudaGetSymbolAddress, so the address
+// stays right after cudaDeviceReset or in another context.  The first call
+// in a context loads the library's device code there, array included (that
+// load allocates the 3.2 MB and can synchronise): make the first call on
+// each device outside any region that must not allocate, and before any
 // stream capture begins.
 #include <cuda_runtime.h>
 
 #include <cstring>
-#include <mutex>
 #include <string>
 
 #include "gbv_grid.cuh"
@@ -39,6 +41,12 @@ constexpr int kNoAllocLevels = 5;  // choose_levels(32768): 8^5 fine cells
 constexpr size_t kNoAllocCells = ((size_t)1 << (3 * kNoAllocLevels)) + 1;
 
 constexpr size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// The carve-up must hold what its users write: the scan of the grid counts
+// (8^kNoAllocLevels + 1 entries) and the bounding-box partials of build_grid
+// (checked below).
+constexpr size_t kNoAllocScanTmp = 64;
+constexpr size_t kNoAllocRed = 8 * 128;
 
 // Carve-up of the scratch array (byte offsets).
 struct NoAllocLayout {
@@ -54,31 +62,38 @@ struct NoAllocLayout {
   static constexpr size_t cid = aux + align256(sizeof(double) * 4);
   static constexpr size_t rank = cid + align256(sizeof(uint32_t) * kNoAllocMaxPoints);
   static constexpr size_t scan_tmp = rank + align256(sizeof(uint32_t) * kNoAllocMaxPoints);
-  static constexpr size_t red = scan_tmp + align256(sizeof(uint32_t) * 64);
-  static constexpr size_t flag_count = red + align256(sizeof(double) * 8 * 128);
+  static constexpr size_t red = scan_tmp + align256(sizeof(uint32_t) * kNoAllocScanTmp);
+  static constexpr size_t flag_count = red + align256(sizeof(double) * kNoAllocRed);
   static constexpr size_t flag_list = flag_count + 256;
   static constexpr size_t total = flag_list + align256(sizeof(uint32_t) * kNoAllocMaxPoints);
 };
 
+static_assert(scan_tmp_elems(kNoAllocCells) <= kNoAllocScanTmp,
+              "scan scratch of the allocation-free kNN is too small");
+static_assert(8 * (size_t)kBboxParts <= kNoAllocRed,
+              "bounding-box partials of the allocation-free kNN are too small");
+
 static __device__ __align__(256) unsigned char g_knn_scratch[NoAllocLayout::total];
 
 namespace {
-constexpr int kMaxDevices = 64;
-std::mutex g_noalloc_mutex;
-unsigned char* g_scratch_addr[kMaxDevices] = {};
-
-// Device address of g_knn_scratch on the current device (looked up once
-// per device, with that device current).
-cudaError_t scratch_address(int dev, unsigned char** out) {
-  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (!g_scratch_addr[dev]) {
-    void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_knn_scratch);
-    if (e != cudaSuccess) return e;
-    g_scratch_addr[dev] = static_cast<unsigned char*>(p);
-  }
-  *out = g_scratch_addr[dev];
+// Device address of g_knn_scratch in the current context.
+cudaError_t scratch_address(unsigned char** out) {
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_knn_scratch);
+  if (e != cudaSuccess) return e;
+  *out = static_cast<unsigned char*>(p);
   return cudaSuccess;
+}
+
+// True when p is device memory of device dev (or managed memory).
+bool on_device(const void* p, int dev) {
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (at.type == cudaMemoryTypeManaged) return true;
+  return at.type == cudaMemoryTypeDevice && at.device == dev;
 }
 }  // namespace
 
@@ -105,10 +120,14 @@ extern "C" gbv_status gbv_knn_noalloc(const double* d_pts, uint32_t n, uint32_t 
                 "gbv_knn_noalloc needs 0 < k <= min(n, " + std::to_string(kKnnSmemK) + ")");
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+  if (e != cudaSuccess)
     return fail(GBV_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+  if (!on_device(d_pts, dev) || !on_device(d_idx, dev) || (d_d2 && !on_device(d_d2, dev)))
+    return fail(GBV_ERR_INVALID_ARGUMENT,
+                "gbv_knn_noalloc: arrays must be device memory of the current device " +
+                    std::to_string(dev));
   unsigned char* base = nullptr;
-  e = scratch_address(dev, &base);
+  e = scratch_address(&base);
   if (e != cudaSuccess)
     return fail(GBV_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
   const cudaStream_t st = static_cast<cudaStream_t>(stream);
@@ -129,7 +148,7 @@ extern "C" gbv_status gbv_knn_noalloc(const double* d_pts, uint32_t n, uint32_t 
   scr.cid = reinterpret_cast<uint32_t*>(base + Lay::cid);
   scr.rank = reinterpret_cast<uint32_t*>(base + Lay::rank);
   scr.scan_tmp = reinterpret_cast<uint32_t*>(base + Lay::scan_tmp);
-  scr.scan_tmp_elems = 64;
+  scr.scan_tmp_elems = kNoAllocScanTmp;
   scr.red = reinterpret_cast<double*>(base + Lay::red);
   const int L = choose_levels(n);  // <= kNoAllocLevels for n <= kNoAllocMaxPoints
   // build_grid clears the grid counts (cell_start) before counting

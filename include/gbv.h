@@ -386,8 +386,14 @@ gbv_status gbv_mlp_gemm_nt(gbv_context* ctx, const void* d_a, int lda, const voi
  * stride >= dim doubles, 1 <= k <= min(n, 64).  The scratch is shared by
  * every call and keeps the last call's contents: calls whose work overlaps
  * on the GPU race and corrupt each other's results, so order them on one
- * stream.  The first call on a device looks up the scratch's address on
- * that device; make that first call before any stream capture. */
+ * stream.  Every call looks up the scratch's address in the current
+ * context, so it stays right after cudaDeviceReset.  The first call in a
+ * context loads the library's device code there, scratch included: that
+ * load allocates the 3.2 MB and can synchronise, so make the first call on
+ * each device outside any region that must not allocate, and before any
+ * stream capture.  d_pts, d_idx and d_d2 must be device (or managed) memory
+ * of the current device; anything else returns GBV_ERR_INVALID_ARGUMENT
+ * before any work is enqueued. */
 gbv_status gbv_knn_noalloc(const double* d_pts, uint32_t n, uint32_t dim, uint32_t stride,
                            uint32_t k, uint32_t* d_idx, double* d_d2, void* stream);
 

@@ -70,3 +70,28 @@ def test_device_argument_check():
                     (x[:, 0], dict(n=5))):
         with pytest.raises(ValueError):
             g._dev_arg(bad, "t", **kw)
+
+
+def test_device_argument_must_be_on_the_context_device():
+    """A CUDA tensor on another GPU than the context's is refused before
+    its pointer reaches a kernel (stand-ins: no GPU is needed)."""
+    import types
+
+    import pytest
+    import geogram_gb300 as g
+
+    class FakeCuda:
+        is_cuda = True
+        dtype = "torch.float64"
+        shape = (5, 3)
+
+        def __init__(self, index):
+            self.device = types.SimpleNamespace(index=index)
+
+        def is_contiguous(self):
+            return True
+
+    ctx0 = types.SimpleNamespace(device=0)
+    assert g._dev_arg(FakeCuda(0), "x", cols=3, ctx=ctx0) is not None
+    with pytest.raises(ValueError, match="cuda:1"):
+        g._dev_arg(FakeCuda(1), "x", cols=3, ctx=ctx0)
