@@ -100,8 +100,8 @@ def _precision(precision: str | int) -> int:
 
 
 def cell_options(box=((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)), k0: int = 20, check_sr: bool = True,
-                 precision: str | int = "fp64", certification: str = "security_radius"
-                 ) -> CellOptions:
+                 precision: str | int = "fp64", certification: str = "security_radius",
+                 first_k: int = 0) -> CellOptions:
     o = CellOptions()
     _lib.load().gbv_cell_options_default(ctypes.byref(o))
     for c in range(3):
@@ -112,6 +112,7 @@ def cell_options(box=((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)), k0: int = 20, check_sr:
     o.precision = _precision(precision)
     o.certification = {"security_radius": CERTIFY_SECURITY_RADIUS,
                        "power_range": CERTIFY_POWER_RANGE}[certification]
+    o.first_k = int(first_k)
     return o
 
 
@@ -211,17 +212,19 @@ class Cells:
 def compute_cells(xyz: np.ndarray, weights: np.ndarray | None = None, *,
                   box=((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)), k0: int = 20, check_sr: bool = True,
                   precision: str | int = "fp64", certification: str = "security_radius",
-                  ctx: Context | None = None) -> Cells:
+                  first_k: int = 0, ctx: Context | None = None) -> Cells:
     """Certified Laguerre cells of the seeds xyz (n x 3) with weights (n).
 
     certification "security_radius" reproduces the reference's clipping
     loop; "power_range" finds every seed that can cut a cell by a range
-    query on the power distance (for widely spread weights)."""
+    query on the power distance (for widely spread weights).  first_k: the
+    first kNN list length of the security-radius loop (0: automatic); the
+    cells do not depend on it."""
     ctx = ctx or default_context()
     x = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
     n = len(x)
     w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float64).reshape(n)
-    o = cell_options(box, k0, check_sr, precision, certification)
+    o = cell_options(box, k0, check_sr, precision, certification, first_k)
     rep = CellReport()
     L = ctx._lib
     _lib.check(L.gbv_cells_compute(ctx.handle, _lib.ptr(x), _lib.ptr(w), n, ctypes.byref(o),
@@ -262,14 +265,14 @@ def _dev_arg(t, name: str, n: int | None = None, cols: int | None = None,
 
 def compute_cells_device(xyz, weights=None, *, box=((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)),
                          k0: int = 20, check_sr: bool = True, precision="fp64",
-                         certification: str = "security_radius", stream=None,
-                         ctx: Context | None = None) -> dict:
+                         certification: str = "security_radius", first_k: int = 0,
+                         stream=None, ctx: Context | None = None) -> dict:
     """Same on torch CUDA tensors (float64, n x 3 and n); results stay on
     the device (read them with device_results)."""
     ctx = ctx or default_context()
     n = _dev_arg(xyz, "xyz", cols=3, ctx=ctx).shape[0]
     _dev_arg(weights, "weights", n, ctx=ctx)
-    o = cell_options(box, k0, check_sr, precision, certification)
+    o = cell_options(box, k0, check_sr, precision, certification, first_k)
     rep = CellReport()
     st = ctypes.c_void_p(stream.cuda_stream) if stream is not None else None
     _lib.check(ctx._lib.gbv_cells_compute_device(ctx.handle, _lib.ptr(xyz), _lib.ptr(weights), n,

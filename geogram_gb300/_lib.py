@@ -41,6 +41,8 @@ class CellOptions(ctypes.Structure):
         ("check_sr", ctypes.c_uint32),
         ("precision", ctypes.c_uint32),
         ("certification", ctypes.c_uint32),
+        ("first_k", ctypes.c_uint32),
+        ("reserved", ctypes.c_uint32),
     ]
 
 

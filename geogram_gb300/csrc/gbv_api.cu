@@ -864,9 +864,13 @@ static void cells_device(gbv_context* c, const double* d_xyz, const double* d_w,
   uint32_t* flag_count = c->buf<uint32_t>("knn_flag_count", 1);
   uint32_t* flag_list = c->buf<uint32_t>("knn_flag_list", n);
 
-  // first lists
+  // first lists: the security-radius loop's cells need about 40-70
+  // neighbours (Voronoi / weights on the squared-spacing scale), a few up to
+  // twice that; a list long enough for nearly all of them spares a second
+  // clipping pass (the cells come out the same whatever the list length)
   const uint32_t nm1 = n > 1 ? n - 1 : 0;
-  const uint32_t K = o.check_sr ? std::min<uint32_t>(kKnnSmemK, nm1)
+  const uint32_t auto_k = d_w ? kKnnMaxK : 96u;
+  const uint32_t K = o.check_sr ? std::min<uint32_t>(o.first_k ? o.first_k : auto_k, nm1)
                                 : std::min<uint32_t>(o.k0, nm1);
   uint32_t* knn = c->buf<uint32_t>("knn", (size_t)std::max<uint32_t>(K, 1) * n);
   uint32_t* kcnt = c->buf<uint32_t>("kcnt", n);
@@ -885,7 +889,8 @@ static void cells_device(gbv_context* c, const double* d_xyz, const double* d_w,
     ka.last_idx = klast_i;
     ka.flag_count = flag_count;
     ka.flag_list = flag_list;
-    if (K > kKnnSmemK) {  // only without the security radius
+    ka.coherent = true;  // every slot, in sorted order
+    if (K > kKnnMaxK) {  // only without the security radius
       ka.gl_d2 = c->buf<double>("knn_gd2", (size_t)K * n);
       ka.gl_slot = c->buf<uint32_t>("knn_gslot", (size_t)K * n);
     }
@@ -944,7 +949,7 @@ static void cells_device(gbv_context* c, const double* d_xyz, const double* d_w,
     ka.last_idx = last_i;
     ka.flag_count = flag_count;
     ka.flag_list = flag_list;
-    if (batch > kKnnSmemK) {  // lists beyond the shared-memory heap
+    if (batch > kKnnMaxK) {  // lists beyond the shared-memory lists
       ka.gl_d2 = c->buf<double>("ext_gd2", (size_t)batch * morek);
       ka.gl_slot = c->buf<uint32_t>("ext_gslot", (size_t)batch * morek);
     }
@@ -1054,6 +1059,7 @@ static bool laguerre_device(gbv_context* c, const double* d_xyz, const double* d
     ka.cnt = cnt;
     ka.flag_count = c->buf<uint32_t>("knn_flag_count", 1);
     ka.flag_list = c->buf<uint32_t>("knn_flag_list", n);
+    ka.coherent = true;
     launch_knn(ka, st);
   }
   GBV_CUDA(cudaGetLastError());
@@ -1199,6 +1205,7 @@ static void mlp_features_device(gbv_context* c, const double* d_xyz, uint32_t n,
   ka.exp_d2 = od;
   ka.flag_count = c->buf<uint32_t>("knn_flag_count", 1);
   ka.flag_list = c->buf<uint32_t>("nn_flag_list", n);
+  ka.coherent = true;
   launch_knn(ka, st);
   mlp_features(d_xyz, od, n, d_raw, st);
   GBV_CUDA(cudaGetLastError());
@@ -1808,6 +1815,9 @@ static gbv_status check_opts(const gbv_cell_options* o) {
   if (o->certification != GBV_CERTIFY_SECURITY_RADIUS &&
       o->certification != GBV_CERTIFY_POWER_RANGE)
     return fail(GBV_ERR_INVALID_ARGUMENT, "unknown certification");
+  if (o->first_k > kKnnMaxK)
+    return fail(GBV_ERR_INVALID_ARGUMENT,
+                "first_k must be at most " + std::to_string(kKnnMaxK) + " (0: automatic)");
   return GBV_OK;
 }
 
@@ -2041,7 +2051,7 @@ gbv_status gbv_nn_get_nearest_neighbors(gbv_context* c, uint32_t nq, const doubl
     ka.exp_d2 = od;
     ka.flag_count = c->buf<uint32_t>("knn_flag_count", 1);
     ka.flag_list = c->buf<uint32_t>("nn_flag_list", nq);
-    if (k > kKnnSmemK) {
+    if (k > kKnnMaxK) {
       ka.gl_d2 = c->buf<double>("nn_gd2", (size_t)k * nq);
       ka.gl_slot = c->buf<uint32_t>("nn_gslot", (size_t)k * nq);
     }
@@ -2073,7 +2083,8 @@ gbv_status gbv_nn_get_nearest_neighbors_all(gbv_context* c, uint32_t k, uint32_t
     ka.exp_d2 = od;
     ka.flag_count = c->buf<uint32_t>("knn_flag_count", 1);
     ka.flag_list = c->buf<uint32_t>("nn_flag_list", n);
-    if (k > kKnnSmemK) {
+    ka.coherent = true;
+    if (k > kKnnMaxK) {
       ka.gl_d2 = c->buf<double>("nn_gd2", (size_t)k * n);
       ka.gl_slot = c->buf<uint32_t>("nn_gslot", (size_t)k * n);
     }

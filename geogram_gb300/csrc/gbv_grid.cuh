@@ -137,13 +137,18 @@ struct KnnArgs {
   uint32_t* gl_slot;
   uint32_t* flag_count;
   uint32_t* flag_list;
+  // queries close in space when consecutive (slots in sorted order): the
+  // warp-synchronous search may take them
+  bool coherent;
 };
 
-// Launches the kNN search.  For k <= kKnnSmemK: FP32 screening with an
-// exact FP64 re-rank, then the exact search for the queries it could not
-// settle (needs flag_count / flag_list).  Larger k: the exact search with
-// global lists gl_d2 / gl_slot.
+// Launches the kNN search.  Coherent queries, k <= kKnnMaxK: the
+// warp-synchronous FP32 screening with an exact FP64 re-rank, then the exact
+// search for the queries it could not settle (needs flag_count /
+// flag_list).  Other queries, k <= kKnnSmemK: the same per thread.  Larger
+// k: the exact search with global lists gl_d2 / gl_slot (k > kKnnMaxK).
 constexpr uint32_t kKnnSmemK = 64;
+constexpr uint32_t kKnnMaxK = 128;
 void launch_knn(const KnnArgs& a, cudaStream_t st);
 
 }  // namespace gbv

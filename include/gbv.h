@@ -73,6 +73,13 @@ typedef struct {
     uint32_t check_sr;   /* 1: grow the list until certified (set_check_SR) */
     uint32_t precision;  /* gbv_precision */
     uint32_t certification; /* gbv_certification */
+    uint32_t first_k;    /* no counterpart in the reference: neighbours fetched
+                            by the first kNN pass of the security-radius loop
+                            (the reference starts at k0 and grows by k/8; a
+                            longer first list gives the same cells with fewer
+                            passes); 0: automatic (96 without weights, 128
+                            with), at most 128 */
+    uint32_t reserved;   /* 0 */
 } gbv_cell_options;
 
 typedef enum {

@@ -168,3 +168,13 @@ def test_cells_beyond_fixed_capacity(g, prec):
     assert c.report["n_huge"] >= 1
     assert np.diff(c.rowptr.astype(np.int64)).max() == np.diff(ref["rowptr"]).max() > 600
     assert_cells_equal(c, ref)
+
+
+@pytest.mark.parametrize("first_k", [20, 64, 128])
+@pytest.mark.parametrize("prec", PRECISIONS)
+def test_first_list_length_does_not_change_cells(g, first_k, prec):
+    """A first kNN list shorter than most cells need (20: nearly every cell
+    grows its list) or long enough for all of them gives the same cells."""
+    ref = load_golden("cells_power_1500.npz")
+    c = g.compute_cells(ref["x"], ref["w"], precision=prec, first_k=first_k)
+    assert_cells_equal(c, ref)

@@ -77,3 +77,26 @@ def test_errors(g):
     nn.set_points(np.random.default_rng(0).random((10, 3)))
     with pytest.raises(g.GbvError):
         nn.get_nearest_neighbors(11, np.zeros((1, 3)))  # k > n
+
+
+@pytest.mark.parametrize("kind", ["uniform", "clustered", "lifted"])
+@pytest.mark.parametrize("k", [64, 128])
+def test_warp_search_vs_oracle_at_size(g, oracle_mod, kind, k):
+    """The warp-synchronous search (all points, sorted slots) on 60k points:
+    uniform, tight clusters (leaves far above 32 seeds, many FP32 ties) and
+    4-d lifted points, against the oracle's exact lists."""
+    rng = np.random.default_rng(k + len(kind))
+    n = 60000
+    if kind == "clustered":
+        c = rng.random((6, 3))
+        x = np.clip(c[rng.integers(0, 6, n)] + rng.normal(size=(n, 3)) * 0.003, 0, 1)
+    elif kind == "lifted":
+        x = np.concatenate([rng.random((n, 3)), np.sqrt(rng.random((n, 1)) * 1e-4)], 1)
+    else:
+        x = rng.random((n, 3))
+    nn = g.NearestNeighborSearch(x.shape[1])
+    nn.set_points(x)
+    idx, d2 = nn.get_nearest_neighbors_by_index(k)
+    ri, rd = oracle_mod.knn(x, k, nthreads=8)
+    assert np.array_equal(idx, ri)
+    assert np.array_equal(d2, rd)
