@@ -44,7 +44,8 @@ __all__ = [
     "CELL_STALLED",
     "PRECISION_FP64", "PRECISION_FP32_RECHECK", "cell_options", "CERTIFY_SECURITY_RADIUS",
     "CERTIFY_POWER_RANGE", "ot_options", "ot_solve", "ot_solve_device", "ot_gradient_hessian",
-    "ot_solve_levels", "ot_solve_levels_device", "ot_separable_start_device",
+    "ot_solve_levels", "ot_solve_levels_device", "ot_separable_start_device", "CellMesh",
+    "cells_mesh",
 ]
 
 
@@ -237,7 +238,88 @@ def compute_cells(xyz: np.ndarray, weights: np.ndarray | None = None, *,
     status = np.empty(n, np.int32)
     _lib.check(L.gbv_cells_fetch(ctx.handle, _lib.ptr(vol), _lib.ptr(mg), _lib.ptr(rowptr),
                                  _lib.ptr(nbr), _lib.ptr(area), _lib.ptr(status)))
+    ctx.last_n, ctx.last_nnz = n, rep.nnz
     return Cells(vol, mg, rowptr, nbr[:rep.nnz], area[:rep.nnz], status, rep.as_dict())
+
+
+@dataclass
+class CellMesh:
+    """Polytopes of cells (ConvexCell::save / append_to_mesh,
+    voronoi/convex_cell.cpp:282-352, 371-444), cell after cell.
+
+    cells[k]             original index of the k-th exported cell
+    vertices             corners (x, y, z), in each cell's valid-list order
+    cell_vertex_ptr      cell k owns vertices[cell_vertex_ptr[k]:cell_vertex_ptr[k+1]]
+    cell_face_ptr        ... and polygons cell_face_ptr[k]:cell_face_ptr[k+1]
+    face_ptr, face_vertices
+                         polygon f is face_vertices[face_ptr[f]:face_ptr[f+1]],
+                         corner numbers local to its cell
+    face_seed[f]         the seed across polygon f (v_global_index), or
+                         0xFFFFFFFF for a box face
+    """
+    cells: np.ndarray
+    vertices: np.ndarray
+    cell_vertex_ptr: np.ndarray
+    cell_face_ptr: np.ndarray
+    face_ptr: np.ndarray
+    face_vertices: np.ndarray
+    face_seed: np.ndarray
+
+    def obj_text(self, v_offset: int = 1, shrink: float = 0.0,
+                 barycenters: np.ndarray | None = None) -> str:
+        """The cells as ConvexCell::save writes them one after the other
+        ("v x y z" lines, then "f i j k ..." lines, vertex numbers from
+        v_offset and continuing across cells); shrink moves every corner
+        toward its cell's barycenter (mg / m, one row per exported cell)
+        as p = shrink g + (1 - shrink) p."""
+        if shrink != 0.0 and barycenters is None:
+            raise ValueError("shrink needs the cells' barycenters")
+        out = []
+        off = v_offset
+        for k in range(len(self.cells)):
+            v0, v1 = int(self.cell_vertex_ptr[k]), int(self.cell_vertex_ptr[k + 1])
+            g = barycenters[k] if shrink != 0.0 else None
+            for p in self.vertices[v0:v1]:
+                x, y, z = float(p[0]), float(p[1]), float(p[2])
+                if g is not None:
+                    x = shrink * float(g[0]) + (1.0 - shrink) * x
+                    y = shrink * float(g[1]) + (1.0 - shrink) * y
+                    z = shrink * float(g[2]) + (1.0 - shrink) * z
+                out.append("v %g %g %g\n" % (x, y, z))
+            for f in range(int(self.cell_face_ptr[k]), int(self.cell_face_ptr[k + 1])):
+                ids = self.face_vertices[self.face_ptr[f]:self.face_ptr[f + 1]]
+                out.append("f " + "".join(f"{int(i) + off} " for i in ids) + "\n")
+            off += v1 - v0
+        return "".join(out)
+
+    def save_obj(self, path: str, **kw) -> None:
+        with open(path, "w") as f:
+            f.write(self.obj_text(**kw))
+
+
+def cells_mesh(cells=None, ctx: Context | None = None) -> CellMesh:
+    """Polytopes of cells of the last compute on ctx (all cells when None)."""
+    ctx = ctx or default_context()
+    L = ctx._lib
+    if cells is None:
+        ci = None
+        m = int(getattr(ctx, "last_n", 0))
+    else:
+        ci = np.ascontiguousarray(cells, dtype=np.uint32).reshape(-1)
+        m = len(ci)
+    sz = _lib.MeshSizes()
+    _lib.check(L.gbv_cells_mesh(ctx.handle, _lib.ptr(ci), m, ctypes.byref(sz), None, None, None,
+                                None, None, None))
+    nv, nf = int(sz.n_vertices), int(sz.n_faces)
+    out = CellMesh(cells=ci if ci is not None else np.arange(m, dtype=np.uint32),
+                   vertices=np.empty((nv, 3)), cell_vertex_ptr=np.empty(m + 1, np.uint32),
+                   cell_face_ptr=np.empty(m + 1, np.uint32), face_ptr=np.empty(nf + 1, np.uint32),
+                   face_vertices=np.empty(3 * nv, np.uint32), face_seed=np.empty(nf, np.uint32))
+    _lib.check(L.gbv_cells_mesh(ctx.handle, _lib.ptr(ci), m, ctypes.byref(sz),
+                                _lib.ptr(out.vertices), _lib.ptr(out.cell_vertex_ptr),
+                                _lib.ptr(out.cell_face_ptr), _lib.ptr(out.face_ptr),
+                                _lib.ptr(out.face_vertices), _lib.ptr(out.face_seed)))
+    return out
 
 
 def _dev_arg(t, name: str, n: int | None = None, cols: int | None = None,

@@ -113,6 +113,14 @@ class CellReport(ctypes.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class MeshSizes(ctypes.Structure):
+    _fields_ = [
+        ("n_vertices", ctypes.c_uint64),
+        ("n_faces", ctypes.c_uint64),
+        ("n_face_vertices", ctypes.c_uint64),
+    ]
+
+
 _P = ctypes.c_void_p
 _U32 = ctypes.c_uint32
 
@@ -163,6 +171,8 @@ SIGNATURES = {
     "gbv_ot_separable_start": (ctypes.c_int, [_P, _P, _U32, ctypes.POINTER(OtOptions), _P, _P]),
     "gbv_mlp_gemm_nt": (ctypes.c_int, [_P, _P, ctypes.c_int, _P, ctypes.c_int, _P, ctypes.c_int,
                                        ctypes.c_int, ctypes.c_int, ctypes.c_int, _P]),
+    "gbv_cells_mesh": (ctypes.c_int, [_P, _P, _U32, ctypes.POINTER(MeshSizes), _P, _P, _P, _P,
+                                      _P, _P]),
     "gbv_knn_noalloc": (ctypes.c_int, [_P, _U32, _U32, _U32, _U32, _P, _P, _P]),
 }
 

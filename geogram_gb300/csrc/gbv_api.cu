@@ -27,7 +27,7 @@
 #include <string>
 #include <vector>
 
-#include "gbv_clip.cuh"
+#include "gbv_context.cuh"
 #include "gbv_ot.cuh"
 #include "gbv_mlp.cuh"
 #include "gbv_start.cuh"
@@ -41,70 +41,8 @@ gbv_status fail(gbv_status st, const std::string& msg) {
   return st;
 }
 
-struct CudaError {
-  cudaError_t e;
-  std::string where;
-};
-
-#define GBV_CUDA(call)                                                     \
-  do {                                                                     \
-    cudaError_t e_ = (call);                                               \
-    if (e_ != cudaSuccess) throw CudaError{e_, #call};                     \
-  } while (0)
-
-struct StatusError {
-  gbv_status st;
-  std::string msg;
-};
-
 }  // namespace
 
-struct gbv_context {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  cudaEvent_t ev[8] = {};
-  std::map<std::string, std::pair<void*, size_t>> bufs;
-
-  gbv::SortedSeeds S;
-  gbv::GridScratch scr;
-  unsigned long long* counters = nullptr;  // [0] exact calls [1] max clips
-  uint32_t* list_counts = nullptr;         // [4] classification counters
-  uint32_t* h_counts = nullptr;            // pinned mirror
-
-  // last cell results, caller order
-  uint32_t n = 0;
-  uint64_t nnz = 0;
-  bool has_cells = false;
-  double* vol = nullptr;
-  double* mg = nullptr;
-  uint32_t* rowptr = nullptr;
-  uint32_t* nbr = nullptr;
-  double* area = nullptr;
-  int32_t* status = nullptr;
-
-  // nearest-neighbour search state
-  bool nn_ready = false;
-  uint32_t nn_n = 0, nn_dim = 3;
-
-  template <class T>
-  T* buf(const std::string& name, size_t count) {
-    size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
-    auto it = bufs.find(name);
-    if (it != bufs.end() && it->second.second >= bytes) return (T*)it->second.first;
-    if (it != bufs.end()) {
-      GBV_CUDA(cudaFree(it->second.first));
-      bufs.erase(it);
-    }
-    void* p = nullptr;
-    GBV_CUDA(cudaMalloc(&p, bytes));
-    bufs[name] = {p, bytes};
-    size_t total = 0;
-    for (const auto& kv : bufs) total += kv.second.second;
-    peak_bytes = std::max(peak_bytes, total);
-    return (T*)p;
-  }
-  size_t peak_bytes = 0;  // most device memory the arena held at once
-};
 
 namespace gbv {
 
@@ -494,6 +432,10 @@ struct Pipeline {
            bool fp32_, bool check_sr_, uint32_t k0, cudaStream_t st_)
       : c(ctx), st(st_), n(n_), fp32(fp32_), check_sr(check_sr_) {
     S = c->S;
+    for (int k = 0; k < 3; ++k) {
+      c->box[k] = box_min[k];
+      c->box[3 + k] = box_max[k];
+    }
     status_s = c->buf<int32_t>("status_s", n);
     vol_s = c->buf<double>("vol_s", n);
     mg_s = c->buf<double>("mg_s", 3 * (size_t)n);

@@ -1,0 +1,81 @@
+// The context behind the C ABI's gbv_context handle (device buffers, the
+// stream, the last cell results) and the error types the entry points turn
+// into status codes.  Shared by the .cu files that implement entry points.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <map>
+#include <string>
+
+#include "gbv_clip.cuh"
+
+namespace gbv {
+
+struct CudaError {
+  cudaError_t e;
+  std::string where;
+};
+
+#define GBV_CUDA(call)                                                     \
+  do {                                                                     \
+    cudaError_t e_ = (call);                                               \
+    if (e_ != cudaSuccess) throw ::gbv::CudaError{e_, #call};              \
+  } while (0)
+
+struct StatusError {
+  gbv_status st;
+  std::string msg;
+};
+
+}  // namespace gbv
+
+struct gbv_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[8] = {};
+  std::map<std::string, std::pair<void*, size_t>> bufs;
+
+  gbv::SortedSeeds S;
+  gbv::GridScratch scr;
+  unsigned long long* counters = nullptr;  // [0] exact calls [1] max clips
+  uint32_t* list_counts = nullptr;         // [4] classification counters
+  uint32_t* h_counts = nullptr;            // pinned mirror
+
+  // last cell results, caller order; their combinatorics stay in the
+  // arena's cb_* buffers (by sorted slot) until the seeds are re-sorted
+  uint32_t n = 0;
+  uint64_t nnz = 0;
+  bool has_cells = false;
+  double* vol = nullptr;
+  double* mg = nullptr;
+  uint32_t* rowptr = nullptr;
+  uint32_t* nbr = nullptr;
+  double* area = nullptr;
+  int32_t* status = nullptr;
+  double box[6] = {0.0, 0.0, 0.0, 1.0, 1.0, 1.0};  // the clipping box of the last cells
+
+  // nearest-neighbour search state
+  bool nn_ready = false;
+  uint32_t nn_n = 0, nn_dim = 3;
+
+  template <class T>
+  T* buf(const std::string& name, size_t count) {
+    size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
+    auto it = bufs.find(name);
+    if (it != bufs.end() && it->second.second >= bytes) return (T*)it->second.first;
+    if (it != bufs.end()) {
+      GBV_CUDA(cudaFree(it->second.first));
+      bufs.erase(it);
+    }
+    void* p = nullptr;
+    GBV_CUDA(cudaMalloc(&p, bytes));
+    bufs[name] = {p, bytes};
+    size_t total = 0;
+    for (const auto& kv : bufs) total += kv.second.second;
+    peak_bytes = std::max(peak_bytes, total);
+    return (T*)p;
+  }
+  size_t peak_bytes = 0;  // most device memory the arena held at once
+};

@@ -371,6 +371,38 @@ gbv_status gbv_mlp_gemm_nt(gbv_context* ctx, const void* d_a, int lda, const voi
                            int ldb, float* d_c, int ldc, int M, int N, int K, void* stream);
 
 /* ---------------------------------------------------------------- */
+/* Cell polytopes (output formats)                                   */
+/* ---------------------------------------------------------------- */
+
+typedef struct {
+    uint64_t n_vertices;       /* corners of the requested cells            */
+    uint64_t n_faces;          /* polygons                                  */
+    uint64_t n_face_vertices;  /* polygon entries (3 per corner)            */
+} gbv_mesh_sizes;
+
+/* Replaces ConvexCell::save / append_to_mesh (voronoi/convex_cell.cpp:
+ * 282-352, 371-444) for the cells of the last compute on ctx: cells[0..m)
+ * (original seed indices; NULL = every cell, m ignored).  Per cell, its
+ * corners in the reference's order (the valid-triangle list; coordinates
+ * bit-identical to compute_triangle_point / w) and one polygon per plane
+ * that bounds it, in plane creation order (box faces, then the seeds in
+ * clipping order), each walked as the reference walks it.  Host arrays:
+ *   vertices[3 * n_vertices]       x, y, z of each corner, cell after cell
+ *   cell_vertex_ptr[m + 1]         first corner of each cell
+ *   cell_face_ptr[m + 1]           first polygon of each cell
+ *   face_ptr[n_faces + 1]          first entry of each polygon
+ *   face_vertices[n_face_vertices] corner numbers local to the cell
+ *   face_seed[n_faces]             v_global_index of the plane: the seed
+ *                                  across the face, 0xFFFFFFFF for the box
+ * Call once with the arrays NULL to get *sizes, then with arrays of those
+ * sizes (any may be NULL).  Cells beyond 128 corners return GBV_ERR_CAPACITY
+ * (their polytope is not kept). */
+gbv_status gbv_cells_mesh(gbv_context* ctx, const uint32_t* cells, uint32_t m,
+                          gbv_mesh_sizes* sizes, double* vertices, uint32_t* cell_vertex_ptr,
+                          uint32_t* cell_face_ptr, uint32_t* face_ptr, uint32_t* face_vertices,
+                          uint32_t* face_seed);
+
+/* ---------------------------------------------------------------- */
 /* Allocation-free kNN                                               */
 /* ---------------------------------------------------------------- */
 

@@ -82,6 +82,9 @@ def ref():
         lib.ref_knn.argtypes = [P, U, U, U, P, P, ctypes.c_int]
         lib.ref_cells.argtypes = [P, P, U, U, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P, P, P,
                                   P, U, P, P, P]
+        lib.ref_cells_save.argtypes = [P, P, U, U, ctypes.c_int, P, U, ctypes.c_double, P,
+                                       ctypes.c_size_t]
+        lib.ref_cells_save.restype = ctypes.c_long
         lib.ref_init()
         _ref = lib
     return _ref
@@ -200,6 +203,22 @@ def cells_range_time(xyz: np.ndarray, w: np.ndarray | None, i0: int, i1: int,
     pc.range(i0, i1, nthreads, max_nbr=max_nbr)
     pc.close()
     return time.perf_counter() - t
+
+
+def ref_cells_obj(xyz: np.ndarray, w: np.ndarray | None, which, shrink: float = 0.0,
+                  k0: int = 20) -> str:
+    """The reference's ConvexCell::save text of the cells `which`, one after
+    the other with continuing vertex numbers (reference build only)."""
+    x = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+    wa = None if w is None else np.ascontiguousarray(w, dtype=np.float64)
+    wh = np.ascontiguousarray(which, dtype=np.uint32)
+    cap = 1 << 16
+    while True:
+        buf = ctypes.create_string_buffer(cap)
+        r = ref().ref_cells_save(_p(x), _p(wa), len(x), k0, 1, _p(wh), len(wh), shrink, buf, cap)
+        if r >= 0:
+            return buf.value.decode()
+        cap *= 4
 
 
 def det4_sign(p0, p1, p2, p3) -> int:

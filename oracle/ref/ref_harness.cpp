@@ -13,7 +13,8 @@
  *   - cells: VBW::ConvexCell with exact predicates (voronoi/convex_cell.cpp:
  *     init_with_box :175-215, clip_by_plane :461-516, compute_geometry
  *     :1125-1145, compute_mg :1267-1307, facet_area :1160-1191,
- *     squared_radius :1312-1330).
+ *     squared_radius :1312-1330), and its output ConvexCell::save
+ *     (:282-352).
  * What is composed here (the reference has no meshless Laguerre driver):
  *   - the per-seed neighbour list of Delaunay_NearestNeighbors
  *     (delaunay/delaunay_nn.cpp:104-145: ask k+1, drop self, a duplicate
@@ -40,6 +41,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstring>
+#include <sstream>
 #include <thread>
 #include <vector>
 
@@ -103,6 +105,80 @@ unsigned seed_neighbours(const GEO::NearestNeighborSearch* nn, unsigned n,
     return unsigned(out.size());
 }
 
+/* The lifted points (4-d when weighted) of the seeds. */
+unsigned lifted_points(const double* xyz, const double* w, unsigned n, std::vector<double>& pts,
+                       std::vector<double>& h) {
+    unsigned dim = (w != nullptr) ? 4u : 3u;
+    pts.assign(size_t(n) * dim, 0.0);
+    h.assign(n, 0.0);
+    if (w != nullptr) {
+        double W = w[0];
+        for (unsigned i = 1; i < n; ++i) W = std::max(W, w[i]);
+        for (unsigned i = 0; i < n; ++i) h[i] = ::sqrt(W - w[i]);
+    }
+    for (unsigned i = 0; i < n; ++i) {
+        for (unsigned c = 0; c < 3; ++c) pts[size_t(i) * dim + c] = xyz[3 * size_t(i) + c];
+        if (dim == 4) pts[size_t(i) * dim + 3] = h[i];
+    }
+    return dim;
+}
+
+/* Clips the box [0,1]^3 to the cell of seed i with the security-radius
+ * loop; returns the status, *list_out the list length, *clips_out the
+ * planes clipped. */
+int clip_cell(VBW::ConvexCell& C, const GEO::NearestNeighborSearch* nn, const double* xyz,
+              const double* w, const std::vector<double>& pts, const std::vector<double>& h,
+              unsigned dim, unsigned n, unsigned i, unsigned k0, int check_sr,
+              std::vector<GEO::index_t>& ix, std::vector<double>& dd,
+              std::vector<GEO::index_t>& nbrs, unsigned* list_out, unsigned* clips_out) {
+    const double* pi = &pts[size_t(i) * dim];
+    const double wi = (w != nullptr) ? w[i] : 0.0;
+    const double pi_len2 = xyz[3 * i] * xyz[3 * i] +
+                           xyz[3 * i + 1] * xyz[3 * i + 1] +
+                           xyz[3 * i + 2] * xyz[3 * i + 2];
+    C.init_with_box(0.0, 0.0, 0.0, 1.0, 1.0, 1.0);
+    int st = 1;
+    unsigned jj = 0, prev = 0, nb_req = std::min(k0, n - 1);
+    nbrs.clear();
+    unsigned list = seed_neighbours(nn, n, i, nb_req, ix, dd, nbrs);
+    bool done = false;
+    while (!done) {
+        if (list == 0) { st = 2; break; }
+        if (prev == list) { st = 3; break; }
+        for (; jj < list; ++jj) {
+            GEO::index_t j = nbrs[jj];
+            double R2 = C.squared_radius(
+                VBW::make_vec3(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]));
+            if (dim == 4) R2 += h[i] * h[i];
+            const double* pj = &pts[size_t(j) * dim];
+            double dij = 0.0;
+            for (unsigned c = 0; c < dim; ++c) dij += (pj[c] - pi[c]) * (pj[c] - pi[c]);
+            if (check_sr && dij > 4.1 * R2) { st = 0; done = true; break; }
+            const double wj = (w != nullptr) ? w[j] : 0.0;
+            const double pj_len2 = xyz[3 * j] * xyz[3 * j] +
+                                   xyz[3 * j + 1] * xyz[3 * j + 1] +
+                                   xyz[3 * j + 2] * xyz[3 * j + 2];
+            VBW::vec4 P = VBW::make_vec4(
+                2.0 * (xyz[3 * i] - xyz[3 * j]),
+                2.0 * (xyz[3 * i + 1] - xyz[3 * j + 1]),
+                2.0 * (xyz[3 * i + 2] - xyz[3 * j + 2]),
+                (wi - pi_len2) - (wj - pj_len2));
+            C.clip_by_plane(P, j);
+        }
+        if (done) break;
+        if (!check_sr) { st = 0; break; }
+        if (list >= n - 1) { st = 1; break; }
+        prev = list;
+        unsigned nb = list;
+        nb = (nb > 8) ? nb + nb / 8 : nb + 1;
+        nb = std::min(nb, n - 1);
+        list = seed_neighbours(nn, n, i, nb, ix, dd, nbrs);
+    }
+    *list_out = list;
+    *clips_out = jj;
+    return st;
+}
+
 }  // namespace
 
 extern "C" {
@@ -151,18 +227,8 @@ int ref_cells(const double* xyz, const double* w, unsigned n, unsigned k0,
               int* status) {
     ensure_init();
     if (n < 2) return 1;
-    unsigned dim = (w != nullptr) ? 4u : 3u;
-    std::vector<double> pts(size_t(n) * dim);
-    std::vector<double> h(n, 0.0);
-    if (w != nullptr) {
-        double W = w[0];
-        for (unsigned i = 1; i < n; ++i) W = std::max(W, w[i]);
-        for (unsigned i = 0; i < n; ++i) h[i] = ::sqrt(W - w[i]);
-    }
-    for (unsigned i = 0; i < n; ++i) {
-        for (unsigned c = 0; c < 3; ++c) pts[size_t(i) * dim + c] = xyz[3 * size_t(i) + c];
-        if (dim == 4) pts[size_t(i) * dim + 3] = h[i];
-    }
+    std::vector<double> pts, h;
+    const unsigned dim = lifted_points(xyz, w, n, pts, h);
     GEO::NearestNeighborSearch_var nn =
         GEO::NearestNeighborSearch::create(GEO::coord_index_t(dim), "BNN");
     nn->set_points(n, pts.data());
@@ -173,49 +239,9 @@ int ref_cells(const double* xyz, const double* w, unsigned n, unsigned k0,
         std::vector<GEO::index_t> ix, nbrs;
         std::vector<double> dd;
         for (unsigned i = b; i < e; ++i) {
-            const double* pi = &pts[size_t(i) * dim];
-            const double wi = (w != nullptr) ? w[i] : 0.0;
-            const double pi_len2 = xyz[3 * i] * xyz[3 * i] +
-                                   xyz[3 * i + 1] * xyz[3 * i + 1] +
-                                   xyz[3 * i + 2] * xyz[3 * i + 2];
-            C.init_with_box(0.0, 0.0, 0.0, 1.0, 1.0, 1.0);
-            int st = 1;
-            unsigned jj = 0, prev = 0, nb_req = std::min(k0, n - 1);
-            nbrs.clear();
-            unsigned list = seed_neighbours(nn, n, i, nb_req, ix, dd, nbrs);
-            bool done = false;
-            while (!done) {
-                if (list == 0) { st = 2; break; }
-                if (prev == list) { st = 3; break; }
-                for (; jj < list; ++jj) {
-                    GEO::index_t j = nbrs[jj];
-                    double R2 = C.squared_radius(
-                        VBW::make_vec3(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]));
-                    if (dim == 4) R2 += h[i] * h[i];
-                    const double* pj = &pts[size_t(j) * dim];
-                    double dij = 0.0;
-                    for (unsigned c = 0; c < dim; ++c) dij += (pj[c] - pi[c]) * (pj[c] - pi[c]);
-                    if (check_sr && dij > 4.1 * R2) { st = 0; done = true; break; }
-                    const double wj = (w != nullptr) ? w[j] : 0.0;
-                    const double pj_len2 = xyz[3 * j] * xyz[3 * j] +
-                                           xyz[3 * j + 1] * xyz[3 * j + 1] +
-                                           xyz[3 * j + 2] * xyz[3 * j + 2];
-                    VBW::vec4 P = VBW::make_vec4(
-                        2.0 * (xyz[3 * i] - xyz[3 * j]),
-                        2.0 * (xyz[3 * i + 1] - xyz[3 * j + 1]),
-                        2.0 * (xyz[3 * i + 2] - xyz[3 * j + 2]),
-                        (wi - pi_len2) - (wj - pj_len2));
-                    C.clip_by_plane(P, j);
-                }
-                if (done) break;
-                if (!check_sr) { st = 0; break; }
-                if (list >= n - 1) { st = 1; break; }
-                prev = list;
-                unsigned nb = list;
-                nb = (nb > 8) ? nb + nb / 8 : nb + 1;
-                nb = std::min(nb, n - 1);
-                list = seed_neighbours(nn, n, i, nb, ix, dd, nbrs);
-            }
+            unsigned list = 0, jj = 0;
+            int st = clip_cell(C, nn, xyz, w, pts, h, dim, n, i, k0, check_sr, ix, dd, nbrs,
+                               &list, &jj);
             C.compute_geometry();
             double m = 0.0;
             VBW::vec3 g = VBW::make_vec3(0.0, 0.0, 0.0);
@@ -244,6 +270,41 @@ int ref_cells(const double* xyz, const double* w, unsigned n, unsigned k0,
     });
     nn.reset();
     return 0;
+}
+
+/*
+ * The cells of seeds which[0 .. m) written one after the other by
+ * ConvexCell::save (voronoi/convex_cell.cpp:282-352) into out (at most cap
+ * bytes, NUL-terminated), vertex numbers continuing from one cell to the
+ * next (v_offset 1, then 1 + the vertices written so far), with the given
+ * shrink factor.  Returns the text length, or -1 when cap is too small.
+ */
+long ref_cells_save(const double* xyz, const double* w, unsigned n, unsigned k0,
+                    int check_sr, const unsigned* which, unsigned m, double shrink,
+                    char* out, size_t cap) {
+    ensure_init();
+    if (n < 2) return -1;
+    std::vector<double> pts, h;
+    const unsigned dim = lifted_points(xyz, w, n, pts, h);
+    GEO::NearestNeighborSearch_var nn =
+        GEO::NearestNeighborSearch::create(GEO::coord_index_t(dim), "BNN");
+    nn->set_points(n, pts.data());
+    VBW::ConvexCell C(VBW::WithVGlobal);
+    std::vector<GEO::index_t> ix, nbrs;
+    std::vector<double> dd;
+    std::ostringstream os;
+    GEO::index_t v_offset = 1;
+    for (unsigned q = 0; q < m; ++q) {
+        unsigned list = 0, jj = 0;
+        clip_cell(C, nn, xyz, w, pts, h, dim, n, which[q], k0, check_sr, ix, dd, nbrs, &list,
+                  &jj);
+        v_offset += C.save(os, v_offset, shrink);
+    }
+    nn.reset();
+    const std::string txt = os.str();
+    if (txt.size() + 1 > cap) return -1;
+    std::memcpy(out, txt.c_str(), txt.size() + 1);
+    return long(txt.size());
 }
 
 }  // extern "C"

@@ -102,6 +102,18 @@ def main(only=None):
                             rowptr=r["rowptr"], nbr=r["nbr"], area=r["area"],
                             status=r["status"], n_clip=r["n_clip"], k_list=r["k_list"])
         print(name, len(x), "cells, nnz", len(r["nbr"]))
+    if not only or "obj" in only:
+        # ConvexCell::save text of some cells (interior, at the box, of
+        # weighted seeds), plain and shrunk
+        for src in ("uniform_1500", "power_1500"):
+            d = np.load(os.path.join(HERE, f"cells_{src}.npz"))
+            x, w = d["x"], (d["w"] if d["w"].size else None)
+            which = np.array([0, 1, 2, 7, 42, 100, 333, 777, 1200, 1499], np.uint32)
+            txt = oracle.ref_cells_obj(x, w, which)
+            txt_s = oracle.ref_cells_obj(x, w, which[:4], shrink=0.2)
+            np.savez_compressed(os.path.join(HERE, f"obj_{src}.npz"), which=which,
+                                obj=np.array(txt), obj_shrink=np.array(txt_s))
+            print(f"obj_{src}", len(txt), "bytes")
     if only:
         return
     x = np.random.default_rng(3).random((2000, 3))

@@ -15,6 +15,7 @@ STRUCTS = {
     "gbv_cell_report": "CellReport",
     "gbv_ot_options": "OtOptions",
     "gbv_ot_report": "OtReport",
+    "gbv_mesh_sizes": "MeshSizes",
 }
 
 
