@@ -45,7 +45,7 @@ __all__ = [
     "PRECISION_FP64", "PRECISION_FP32_RECHECK", "cell_options", "CERTIFY_SECURITY_RADIUS",
     "CERTIFY_POWER_RANGE", "ot_options", "ot_solve", "ot_solve_device", "ot_gradient_hessian",
     "ot_solve_levels", "ot_solve_levels_device", "ot_separable_start_device", "CellMesh",
-    "cells_mesh",
+    "cells_mesh", "restricted_cells",
 ]
 
 
@@ -102,7 +102,7 @@ def _precision(precision: str | int) -> int:
 
 def cell_options(box=((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)), k0: int = 20, check_sr: bool = True,
                  precision: str | int = "fp64", certification: str = "security_radius",
-                 first_k: int = 0) -> CellOptions:
+                 first_k: int = 0, predicates: str = "exact") -> CellOptions:
     o = CellOptions()
     _lib.load().gbv_cell_options_default(ctypes.byref(o))
     for c in range(3):
@@ -114,6 +114,7 @@ def cell_options(box=((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)), k0: int = 20, check_sr:
     o.certification = {"security_radius": CERTIFY_SECURITY_RADIUS,
                        "power_range": CERTIFY_POWER_RANGE}[certification]
     o.first_k = int(first_k)
+    o.predicates = {"exact": _lib.PREDICATES_EXACT, "fast": _lib.PREDICATES_FAST}[predicates]
     return o
 
 
@@ -213,19 +214,20 @@ class Cells:
 def compute_cells(xyz: np.ndarray, weights: np.ndarray | None = None, *,
                   box=((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)), k0: int = 20, check_sr: bool = True,
                   precision: str | int = "fp64", certification: str = "security_radius",
-                  first_k: int = 0, ctx: Context | None = None) -> Cells:
+                  first_k: int = 0, predicates: str = "exact", ctx: Context | None = None) -> Cells:
     """Certified Laguerre cells of the seeds xyz (n x 3) with weights (n).
 
     certification "security_radius" reproduces the reference's clipping
     loop; "power_range" finds every seed that can cut a cell by a range
     query on the power distance (for widely spread weights).  first_k: the
     first kNN list length of the security-radius loop (0: automatic); the
-    cells do not depend on it."""
+    cells do not depend on it.  predicates "fast": the reference's
+    use_exact_predicates(false) (FP64 det4x4, conflict iff > 0)."""
     ctx = ctx or default_context()
     x = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
     n = len(x)
     w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float64).reshape(n)
-    o = cell_options(box, k0, check_sr, precision, certification, first_k)
+    o = cell_options(box, k0, check_sr, precision, certification, first_k, predicates)
     rep = CellReport()
     L = ctx._lib
     _lib.check(L.gbv_cells_compute(ctx.handle, _lib.ptr(x), _lib.ptr(w), n, ctypes.byref(o),
@@ -319,6 +321,34 @@ def cells_mesh(cells=None, ctx: Context | None = None) -> CellMesh:
                                 _lib.ptr(out.vertices), _lib.ptr(out.cell_vertex_ptr),
                                 _lib.ptr(out.cell_face_ptr), _lib.ptr(out.face_ptr),
                                 _lib.ptr(out.face_vertices), _lib.ptr(out.face_seed)))
+    return out
+
+
+def restricted_cells(mesh_xyz: np.ndarray, tets: np.ndarray, xyz: np.ndarray,
+                     weights: np.ndarray | None = None, *, k0: int = 20, precision="fp64",
+                     ctx: Context | None = None) -> dict:
+    """Cells of the seeds restricted to a tetrahedral mesh (the reference's
+    volumetric RestrictedVoronoiDiagram, voronoi/RVD.cpp:429-530 and
+    :792-910): per seed the mass m and first moment mg of its cell inside the
+    mesh, the CVT energy f = sum_i int |x - p_i|^2 and its gradient g."""
+    ctx = ctx or default_context()
+    v = np.ascontiguousarray(mesh_xyz, dtype=np.float64).reshape(-1, 3)
+    t = np.ascontiguousarray(tets, dtype=np.uint32).reshape(-1, 4)
+    x = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+    n = len(x)
+    w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float64).reshape(n)
+    o = cell_options(k0=k0, precision=precision)
+    rep = CellReport()
+    out = dict(m=np.empty(n), mg=np.empty((n, 3)), g=np.empty((n, 3)))
+    f = ctypes.c_double(0.0)
+    _lib.check(ctx._lib.gbv_restricted_cells(ctx.handle, _lib.ptr(v), len(v), _lib.ptr(t), len(t),
+                                             _lib.ptr(x), _lib.ptr(w), n, ctypes.byref(o),
+                                             _lib.ptr(out["m"]), _lib.ptr(out["mg"]),
+                                             ctypes.byref(f), _lib.ptr(out["g"]),
+                                             ctypes.byref(rep)))
+    out["f"] = f.value
+    out["report"] = rep.as_dict()
+    ctx.last_n, ctx.last_nnz = n, rep.nnz
     return out
 
 

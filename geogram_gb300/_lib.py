@@ -42,12 +42,15 @@ class CellOptions(ctypes.Structure):
         ("precision", ctypes.c_uint32),
         ("certification", ctypes.c_uint32),
         ("first_k", ctypes.c_uint32),
-        ("reserved", ctypes.c_uint32),
+        ("predicates", ctypes.c_uint32),
     ]
 
 
 CERTIFY_SECURITY_RADIUS = 0
 CERTIFY_POWER_RANGE = 1
+
+PREDICATES_EXACT = 0
+PREDICATES_FAST = 1
 
 
 class OtOptions(ctypes.Structure):
@@ -171,6 +174,10 @@ SIGNATURES = {
     "gbv_ot_separable_start": (ctypes.c_int, [_P, _P, _U32, ctypes.POINTER(OtOptions), _P, _P]),
     "gbv_mlp_gemm_nt": (ctypes.c_int, [_P, _P, ctypes.c_int, _P, ctypes.c_int, _P, ctypes.c_int,
                                        ctypes.c_int, ctypes.c_int, ctypes.c_int, _P]),
+    "gbv_restricted_cells": (ctypes.c_int, [_P, _P, _U32, _P, _U32, _P, _P, _U32,
+                                            ctypes.POINTER(CellOptions), _P, _P,
+                                            ctypes.POINTER(ctypes.c_double), _P,
+                                            ctypes.POINTER(CellReport)]),
     "gbv_cells_mesh": (ctypes.c_int, [_P, _P, _U32, ctypes.POINTER(MeshSizes), _P, _P, _P, _P,
                                       _P, _P]),
     "gbv_knn_noalloc": (ctypes.c_int, [_P, _U32, _U32, _U32, _U32, _P, _P, _P]),

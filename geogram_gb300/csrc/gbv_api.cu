@@ -429,7 +429,7 @@ struct Pipeline {
   int huge_chunks = 0;
 
   Pipeline(gbv_context* ctx, uint32_t n_, const double* box_min, const double* box_max,
-           bool fp32_, bool check_sr_, uint32_t k0, cudaStream_t st_)
+           bool fp32_, bool check_sr_, uint32_t k0, cudaStream_t st_, bool fast_pred = false)
       : c(ctx), st(st_), n(n_), fp32(fp32_), check_sr(check_sr_) {
     S = c->S;
     for (int k = 0; k < 3; ++k) {
@@ -461,6 +461,7 @@ struct Pipeline {
       cbase.box[3 + k] = gbase.box[3 + k] = box_max[k];
     }
     cbase.check_sr = check_sr ? 1 : 0;
+    cbase.fast_pred = fast_pred ? 1 : 0;
     cbase.status = gbase.status = status_s;
     cbase.nclip = nclip;
     gbase.nclip = nclip;
@@ -590,6 +591,7 @@ struct Pipeline {
       h.nq = cm;
       for (int k = 0; k < 6; ++k) h.box[k] = cbase.box[k];
       h.check_sr = cbase.check_sr;
+      h.fast_pred = cbase.fast_pred;
       h.status = status_s;
       h.nclip = nclip;
       h.counters = c->counters;
@@ -802,7 +804,7 @@ static void cells_device(gbv_context* c, const double* d_xyz, const double* d_w,
   build_grid(d_xyz, 3, 3, d_w, n, S.L, S, c->scr, st);
   GBV_CUDA(cudaEventRecord(c->ev[1], st));
   Pipeline P(c, n, o.box_min, o.box_max, o.precision == GBV_PRECISION_FP32_RECHECK,
-             o.check_sr != 0, o.k0, st);
+             o.check_sr != 0, o.k0, st, o.predicates == GBV_PREDICATES_FAST);
   uint32_t* flag_count = c->buf<uint32_t>("knn_flag_count", 1);
   uint32_t* flag_list = c->buf<uint32_t>("knn_flag_list", n);
 
@@ -1318,6 +1320,9 @@ static void ot_solve(gbv_context* c, const double* xyz, const double* nu_in, uin
   double* ones = c->buf<double>("ot_ones", n);
   double* wt = c->buf<double>("ot_wt", n);
   fill_kernel<<<nblocks(n, 256), 256, 0, st>>>(ones, 1.0, n); count_launch();
+  CgScalars* cg_sc = c->buf<CgScalars>("ot_cg_scalars", 1);
+  double* cg_part_a = c->buf<double>("ot_cg_part_a", 2 * kPcgParts);
+  double* cg_part_b = c->buf<double>("ot_cg_part_b", 4 * kPcgParts);
   const double nu_norm = std::sqrt(W.dot(nu, nu));
   // x = H^+ b by Jacobi-preconditioned CG; b (overwritten: the residual) is
   // first projected on mean zero (H has the constants as kernel), and so
@@ -1329,21 +1334,24 @@ static void ot_solve(gbv_context* c, const double* xyz, const double* nu_in, uin
     GBV_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, st));
     cg_precond(b, H.diag, z, n, st);
     GBV_CUDA(cudaMemcpyAsync(p, z, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
-    double rz = W.dot(b, z);
+    const double rz = W.dot(b, z);
+    // the iterations run on the device; the host looks at the iteration
+    // count and the convergence flag every kCgChunk iterations
+    constexpr uint32_t kCgChunk = 16;
+    CgScalars h{};
+    h.rz[0] = rz;
+    h.b2 = bnorm * bnorm;
+    h.tol2 = tol * tol;
+    h.done = (bnorm > 0.0) ? 0u : 1u;
+    GBV_CUDA(cudaMemcpyAsync(cg_sc, &h, sizeof h, cudaMemcpyHostToDevice, st));
     uint32_t k = 0;
-    while (k < o.max_cg) {
-      spmv_dot(H, p, Ap, W.part, kOtParts, st);
-      const double pAp = W.fetch_sum();
-      if (!(pAp > 0.0)) break;
-      const double alpha = rz / pAp;
-      cg_update_xr(x, b, p, Ap, alpha, n, st);
-      ++k;
-      const double rnorm = std::sqrt(W.dot(b, b));
-      if (rnorm <= tol * bnorm) break;
-      cg_precond(b, H.diag, z, n, st);
-      const double rz_new = W.dot(b, z);
-      cg_update_p(p, z, rz_new / rz, n, st);
-      rz = rz_new;
+    while (!h.done && k < o.max_cg) {
+      const uint32_t m = std::min<uint32_t>(kCgChunk, o.max_cg - k);
+      pcg_iterations(H, x, b, p, Ap, z, cg_part_a, cg_part_b, cg_sc, k, m, st);
+      GBV_CUDA(cudaMemcpyAsync(&h, cg_sc, sizeof h, cudaMemcpyDeviceToHost, st));
+      GBV_CUDA(cudaStreamSynchronize(st));
+      k = h.k;
+      if (k % kCgChunk != 0) break;  // stopped inside the chunk
     }
     const double xmean = W.dot(x, ones) / n;
     add_scalar(x, -xmean, n, st);
@@ -1757,6 +1765,8 @@ static gbv_status check_opts(const gbv_cell_options* o) {
   if (o->certification != GBV_CERTIFY_SECURITY_RADIUS &&
       o->certification != GBV_CERTIFY_POWER_RANGE)
     return fail(GBV_ERR_INVALID_ARGUMENT, "unknown certification");
+  if (o->predicates != GBV_PREDICATES_EXACT && o->predicates != GBV_PREDICATES_FAST)
+    return fail(GBV_ERR_INVALID_ARGUMENT, "unknown predicates");
   if (o->first_k > kKnnMaxK)
     return fail(GBV_ERR_INVALID_ARGUMENT,
                 "first_k must be at most " + std::to_string(kKnnMaxK) + " (0: automatic)");
@@ -1876,6 +1886,76 @@ gbv_status gbv_cells_compute(gbv_context* c, const double* xyz, const double* w,
                       report);
     else
       cells_device(c, dx, dw, n, *opt, c->stream, report);
+  });
+}
+
+gbv_status gbv_restricted_cells(gbv_context* c, const double* mesh_xyz, uint32_t nv,
+                                const uint32_t* tets, uint32_t nt, const double* xyz,
+                                const double* w, uint32_t n, const gbv_cell_options* opt,
+                                double* m, double* mg, double* f, double* g,
+                                gbv_cell_report* report) {
+  if (!c || !mesh_xyz || !tets || !xyz) return fail(GBV_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (nv == 0 || nt == 0 || n == 0) return fail(GBV_ERR_INVALID_ARGUMENT, "empty mesh or seeds");
+  gbv_status s = check_opts(opt);
+  if (s != GBV_OK) return s;
+  if (opt->certification != GBV_CERTIFY_SECURITY_RADIUS)
+    return fail(GBV_ERR_INVALID_ARGUMENT, "restricted cells use the security-radius loop");
+  return guarded([&] {
+    GBV_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = c->stream;
+    // the box: bounding box of the mesh and the seeds
+    gbv_cell_options o = *opt;
+    for (int k = 0; k < 3; ++k) {
+      o.box_min[k] = DBL_MAX;
+      o.box_max[k] = -DBL_MAX;
+    }
+    auto grow = [&](const double* p) {
+      for (int k = 0; k < 3; ++k) {
+        o.box_min[k] = std::min(o.box_min[k], p[k]);
+        o.box_max[k] = std::max(o.box_max[k], p[k]);
+      }
+    };
+    for (uint32_t v = 0; v < nv; ++v) grow(mesh_xyz + 3 * (size_t)v);
+    for (uint32_t i = 0; i < n; ++i) grow(xyz + 3 * (size_t)i);
+    for (int k = 0; k < 3; ++k)
+      if (!(o.box_max[k] > o.box_min[k])) throw StatusError{GBV_ERR_INVALID_ARGUMENT, "flat mesh"};
+    double* dx = c->buf<double>("in_xyz", 3 * (size_t)n);
+    double* dw = w ? c->buf<double>("in_w", n) : nullptr;
+    double* dmv = c->buf<double>("rv_mesh_xyz", 3 * (size_t)nv);
+    uint32_t* dt = c->buf<uint32_t>("rv_tets_in", 4 * (size_t)nt);
+    GBV_CUDA(cudaMemcpyAsync(dx, xyz, 24 * (size_t)n, cudaMemcpyHostToDevice, st));
+    if (w) GBV_CUDA(cudaMemcpyAsync(dw, w, 8 * (size_t)n, cudaMemcpyHostToDevice, st));
+    GBV_CUDA(cudaMemcpyAsync(dmv, mesh_xyz, 24 * (size_t)nv, cudaMemcpyHostToDevice, st));
+    GBV_CUDA(cudaMemcpyAsync(dt, tets, 16 * (size_t)nt, cudaMemcpyHostToDevice, st));
+    cells_device(c, dx, dw, n, o, st, report);
+    double* dm = c->buf<double>("rv_m", n);
+    double* dmg = c->buf<double>("rv_mg", 3 * (size_t)n);
+    double* dF = c->buf<double>("rv_F", n);
+    double* dg = c->buf<double>("rv_g", 3 * (size_t)n);
+    restricted_cells(c, dx, dw, n, dmv, nv, dt, nt, st, dm, dmg, dF, dg);
+    if (m) GBV_CUDA(cudaMemcpyAsync(m, dm, 8 * (size_t)n, cudaMemcpyDeviceToHost, st));
+    if (mg) GBV_CUDA(cudaMemcpyAsync(mg, dmg, 24 * (size_t)n, cudaMemcpyDeviceToHost, st));
+    if (g) GBV_CUDA(cudaMemcpyAsync(g, dg, 24 * (size_t)n, cudaMemcpyDeviceToHost, st));
+    if (f) {
+      // deterministic FP64 sum of the per-cell energies
+      double* part = c->buf<double>("rv_part", 2 * kOtParts);
+      double* ones = c->buf<double>("rv_ones", n);
+      fill_kernel<<<nblocks(n, 256), 256, 0, st>>>(ones, 1.0, n); count_launch();
+      dot_parts(dF, ones, n, part, st);
+      std::vector<double> hp(2 * kOtParts);
+      GBV_CUDA(cudaMemcpyAsync(hp.data(), part, 16 * kOtParts, cudaMemcpyDeviceToHost, st));
+      GBV_CUDA(cudaStreamSynchronize(st));
+      double S = 0.0, C = 0.0;
+      for (int b = 0; b < kOtParts; ++b) {
+        const double x = hp[2 * b], t = S + x;
+        if (std::fabs(S) >= std::fabs(x)) C += (S - t) + x;
+        else C += (x - t) + S;
+        S = t;
+        C += hp[2 * b + 1];
+      }
+      *f = S + C;
+    }
+    GBV_CUDA(cudaStreamSynchronize(st));
   });
 }
 

@@ -365,7 +365,7 @@ __global__ void __launch_bounds__(kClipThreads) clip_kernel(ClipArgs a) {
         Real sv;
         if constexpr (kFP64) sv = fma(Pd.z, cz, fma(Pd.y, cy, fma(Pd.x, cx, Pd.w)));
         else sv = fmaf(Pf.z, cz, fmaf(Pf.y, cy, fmaf(Pf.x, cx, Pf.w)));
-        const Real bound = fma(pa1, eps, bw);
+        const Real bound = fma(pa1, eps, bw) * (a.fast_pred ? (Real)kFastPredWide : (Real)1);
         bool in_conflict;
         if (sv < -bound) {
           in_conflict = true;
@@ -376,9 +376,13 @@ __global__ void __launch_bounds__(kClipThreads) clip_kernel(ClipArgs a) {
             const uint32_t v = sm.tv[t][tid];
             const double4 p0 = plane_of(v & 0xFF), p1 = plane_of(v >> 8 & 0xFF),
                           p2 = plane_of(v >> 16 & 0xFF);
-            const double r0[4] = {p0.x, p0.y, p0.z, p0.w}, r1[4] = {p1.x, p1.y, p1.z, p1.w},
-                         rr2[4] = {p2.x, p2.y, p2.z, p2.w}, r3[4] = {Pd.x, Pd.y, Pd.z, Pd.w};
-            in_conflict = det4_sign_exact(r0, r1, rr2, r3) >= 0;
+            if (a.fast_pred) {
+              in_conflict = r_det4x4(p0, p1, p2, Pd) > 0.0;
+            } else {
+              const double r0[4] = {p0.x, p0.y, p0.z, p0.w}, r1[4] = {p1.x, p1.y, p1.z, p1.w},
+                           rr2[4] = {p2.x, p2.y, p2.z, p2.w}, r3[4] = {Pd.x, Pd.y, Pd.z, Pd.w};
+              in_conflict = det4_sign_exact(r0, r1, rr2, r3) >= 0;
+            }
             ++n_exact;
           } else {
             uncertain = true;

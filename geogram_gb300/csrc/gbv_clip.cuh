@@ -40,6 +40,7 @@ struct ClipArgs {
   uint32_t nq;
   double box[6];              // xmin ymin zmin xmax ymax zmax
   int check_sr;
+  int fast_pred;              // 1: the reference's inexact predicates (gbv_predicates)
   int32_t* status;            // by sorted slot
   uint32_t* nclip;            // by sorted slot: neighbours visited
   CombBuf comb;
@@ -120,6 +121,7 @@ struct HugeArgs {
   uint32_t nq;
   double box[6];
   int check_sr;
+  int fast_pred;
   int32_t* status;
   uint32_t* nclip;
   unsigned long long* counters;

@@ -79,3 +79,11 @@ struct gbv_context {
   }
   size_t peak_bytes = 0;  // most device memory the arena held at once
 };
+
+namespace gbv {
+// Cells restricted to a tetrahedral mesh (gbv_restrict.cu), after a cell
+// computation on the mesh's bounding box; device arrays.
+void restricted_cells(gbv_context* c, const double* d_xyz, const double* d_w, uint32_t n,
+                      const double* d_mv, uint32_t nv, const uint32_t* d_tets, uint32_t nt,
+                      cudaStream_t st, double* d_m, double* d_mg, double* d_F, double* d_g);
+}  // namespace gbv

@@ -159,6 +159,9 @@ __global__ void bbox_final_kernel(const double* __restrict__ part, int nparts, i
   if (has_w) m = fmax(m, sqrt(fmax(v[6] + v[7], 0.0)));
   else if (dim == 4) m = fmax(m, v[6]);
   wmax_out[1] = m;
+  // the largest squared difference of two lifts: h_i^2 <= W - min w with
+  // weights, h^2 <= max |h|^2 for 4-d points, 0 in 3-d
+  wmax_out[2] = has_w ? fmax(v[6] + v[7], 0.0) : (dim == 4 ? v[6] * v[6] : 0.0);
 }
 
 __global__ void cell_id_kernel(const double* __restrict__ xyz, uint32_t stride, uint32_t n,
@@ -1048,9 +1051,47 @@ knn_warp_kernel(KnnArgs a, SortedSeeds S, const GridDesc* __restrict__ gdp,
     }
   };
 
+  // ---- a first pruning distance for the warp: the queries are consecutive
+  // sorted slots, so the fine cells from the first to the last one's hold
+  // about 32 seeds; a ball of 1.35x the radius that holds cap seeds at that
+  // density (plus the largest lift difference, 4-d) should hold cap.  Too
+  // small only costs that lane the exact search; it never loses a seed.
+  float t0 = FLT_MAX;
+  if (a.nq > 4 * cap) {
+    const int G = g.G;
+    const uint32_t cfirst = morton3(
+        (uint32_t)clampi((int)__shfl_sync(0xFFFFFFFFu, c.ux, 0), 0, G - 1),
+        (uint32_t)clampi((int)__shfl_sync(0xFFFFFFFFu, c.uy, 0), 0, G - 1),
+        (uint32_t)clampi((int)__shfl_sync(0xFFFFFFFFu, c.uz, 0), 0, G - 1));
+    const uint32_t clast = morton3(
+        (uint32_t)clampi((int)__shfl_sync(0xFFFFFFFFu, c.ux, 31), 0, G - 1),
+        (uint32_t)clampi((int)__shfl_sync(0xFFFFFFFFu, c.uy, 31), 0, G - 1),
+        (uint32_t)clampi((int)__shfl_sync(0xFFFFFFFFu, c.uz, 31), 0, G - 1));
+    const uint32_t lo_c = min(cfirst, clast), hi_c = max(cfirst, clast);
+    const float rho = 32.f / (float)(hi_c - lo_c + 1u);  // seeds per fine cell
+    const float r = 1.35f * cbrtf(3.f * (float)cap / (4.f * 3.14159265f * rho));
+    const float lift = (float)aux[2] * 1.0001f;  // largest squared lift difference
+    t0 = (r * g.h_f) * (r * g.h_f) + lift;
+  }
+  thr = t0;
+
+  // candidates below the lane's pruning distance wait in a register queue;
+  // when one lane's queue is full every lane empties its own into its heap,
+  // so heap updates run together instead of one lane at a time
+  constexpr int kQ = 4;
+  float qd[kQ];
+  uint32_t qs[kQ];
+  int qn = 0;
+  auto flush = [&]() {
+#pragma unroll
+    for (int k = 0; k < kQ; ++k)
+      if (k < qn && qd[k] < thr) offer(qs[k], qd[k]);
+    qn = 0;
+  };
+
   // ---- the traversal, the same for the whole warp
   const float h2f = g.h_f * g.h_f;
-  float wthr = FLT_MAX;  // largest pruning distance of the active lanes
+  float wthr = t0;  // largest pruning distance of the active lanes
   uint32_t stack[8 * 10 + 8];
   int sp = 0;
   stack[sp++] = 0u;  // (code << 4) | level
@@ -1079,9 +1120,19 @@ knn_warp_kernel(KnnArgs a, SortedSeeds S, const GridDesc* __restrict__ gdp,
           const float dx = p.x - c.qf.x, dy = p.y - c.qf.y, dz = p.z - c.qf.z,
                       dh = p.w - c.qf.w;
           const float d32 = dx * dx + dy * dy + dz * dz + dh * dh;
-          if (active && d32 < thr) offer(base + t, d32);
+          const bool take = active && d32 < thr;
+#pragma unroll
+          for (int k = kQ - 1; k > 0; --k) {
+            qd[k] = take ? qd[k - 1] : qd[k];
+            qs[k] = take ? qs[k - 1] : qs[k];
+          }
+          qd[0] = take ? d32 : qd[0];
+          qs[0] = take ? base + t : qs[0];
+          qn += take ? 1 : 0;
+          if (__any_sync(0xFFFFFFFFu, qn == kQ)) flush();
         }
       }
+      flush();
       wthr = active ? thr : 0.f;
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1)
@@ -1128,15 +1179,17 @@ knn_warp_kernel(KnnArgs a, SortedSeeds S, const GridDesc* __restrict__ gdp,
     SL(n - 1) = sr;
     sift_down(0, n - 1);
   }
+  bool unsure = cnt < cap && t0 < FLT_MAX;  // fewer than cap within the first distance
   if (cnt == cap) {
+    // a seed that may belong to the k nearest could have been dropped
     const float r = sqrtf(D(K - 1)) * 1.0000076f + 2.f * delta;
-    if (!(D(cap - 1) > r * r * 1.0000076f)) {
-      // a seed that may belong to the k nearest could have been dropped
-      const uint32_t k = atomicAdd(a.flag_count, 1u);
-      a.flag_list[k] = qi;
-      if (a.cnt) a.cnt[qi] = 0;
-      return;
-    }
+    unsure = !(D(cap - 1) > r * r * 1.0000076f);
+  }
+  if (unsure) {
+    const uint32_t k = atomicAdd(a.flag_count, 1u);
+    a.flag_list[k] = qi;
+    if (a.cnt) a.cnt[qi] = 0;
+    return;
   }
   // ---- exact order: runs of neighbours whose FP32 distances are within
   // their error bound of each other are sorted by exact (d2, index)

@@ -17,7 +17,8 @@ struct SortedSeeds {
   uint32_t* slot_of = nullptr;  // original index -> slot
   uint32_t* cell_start = nullptr;  // G^3 + 1 entries
   GridDesc* gd = nullptr;   // device: grid descriptor
-  double* aux = nullptr;    // device: [0] W = max w, [1] max |coordinate|
+  double* aux = nullptr;    // device: [0] W = max w, [1] max |coordinate|, [2] largest
+                            // squared lift difference, [3] unused
   uint32_t n = 0;
   int L = 0;
 };

@@ -124,25 +124,29 @@ __device__ void init_box(HugeCell& C, const double* box, const double4& pi) {
 // Conflict of triangle t with plane P: det [P_i; P_j; P_k; P] >= 0, exact.
 // Decided, as in the clipping kernels, from the cached corner c: the sign
 // of P . (c, 1) when it exceeds the corner's error bound, else exactly.
+// With the fast predicates, tests near the bound are decided by the
+// reference's FP64 det4x4 instead (conflict iff > 0).
 __device__ __forceinline__ bool in_conflict(const HugeCell& C, int t, const double4& P,
-                                            double pa1, double bw, unsigned long long& n_exact) {
+                                            double pa1, double bw, bool fast,
+                                            unsigned long long& n_exact) {
   const double4 c = C.cor[t];
   const double sv = fma(P.z, c.z, fma(P.y, c.y, fma(P.x, c.x, P.w)));
-  const double bound = fma(pa1, (double)C.eps[t], bw);
+  const double bound = fma(pa1, (double)C.eps[t], bw) * (fast ? kFastPredWide : 1.0);
   if (sv < -bound) return true;
   if (sv > bound) return false;
   const ushort4 tv = C.t[t];
   const double4 a = C.pl[tv.x], b = C.pl[tv.y], d = C.pl[tv.z];
+  ++n_exact;
+  if (fast) return r_det4x4(a, b, d, P) > 0.0;
   const double r0[4] = {a.x, a.y, a.z, a.w}, r1[4] = {b.x, b.y, b.z, b.w},
                r2[4] = {d.x, d.y, d.z, d.w}, r3[4] = {P.x, P.y, P.z, P.w};
-  ++n_exact;
   return det4_sign_exact(r0, r1, r2, r3) >= 0;
 }
 
 // clip_by_plane.  Returns false when a capacity is exhausted.  R2 receives
 // the squared radius of the clipped cell (max over its corners).
 __device__ bool clip(HugeCell& C, const double4& P, uint32_t j, const double4& pi, double& R2,
-                     unsigned long long& n_exact) {
+                     bool fast, unsigned long long& n_exact) {
   int head = kEnd, tail = kEnd;
   int t = C.first_valid;
   C.first_valid = kEnd;
@@ -152,7 +156,7 @@ __device__ bool clip(HugeCell& C, const double4& P, uint32_t j, const double4& p
   while (t != kEnd) {
     const int next = C.t[t].w;
     ++C.tests;
-    if (in_conflict(C, t, P, pa1, bw, n_exact)) {
+    if (in_conflict(C, t, P, pa1, bw, fast, n_exact)) {
       C.t[t].w = (uint16_t)(head | kConf);
       head = t;
       if (tail == kEnd) tail = t;
@@ -385,7 +389,7 @@ __global__ void __launch_bounds__(1) huge_kernel(HugeArgs a) {
       }
       const double4 P = make_double4(2.0 * __dsub_rn(pi.x, pj.x), 2.0 * __dsub_rn(pi.y, pj.y),
                                      2.0 * __dsub_rn(pi.z, pj.z), __dsub_rn(qi_, S.q[j]));
-      if (!clip(C, P, j, pi, R2, n_exact)) {
+      if (!clip(C, P, j, pi, R2, a.fast_pred != 0, n_exact)) {
         st = CELL_OVERFLOW;
         break;
       }

@@ -235,4 +235,169 @@ void scale_copy(double* y, const double* x, double alpha, uint32_t n, cudaStream
   scale_copy_kernel<<<nb(n), kOtThreads, 0, st>>>(y, x, alpha, n); count_launch();
 }
 
+// ---------------------------------------------------------------------
+// Device-resident preconditioned CG
+// ---------------------------------------------------------------------
+// (s, c) pairs added in a fixed order: a Neumaier sum of the s parts, the
+// c parts summed alongside.
+__device__ __forceinline__ void pair_add(double& s, double& c, double s2, double c2) {
+  neu_add(s, c, s2);
+  c += c2;
+}
+
+// Fixed-order tree over the warp, then over the block's warps: the (s, c)
+// pair of the whole block in thread 0 (blockDim.x a multiple of 32, <= 1024).
+__device__ __forceinline__ void block_pair(double& s, double& c) {
+  __shared__ double ws[32], wc[32];
+  const unsigned FULL = 0xFFFFFFFFu;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const double s2 = __shfl_down_sync(FULL, s, o), c2 = __shfl_down_sync(FULL, c, o);
+    if (lane < o) pair_add(s, c, s2, c2);
+  }
+  __syncthreads();  // ws/wc may still be read by a previous call
+  if (lane == 0) {
+    ws[warp] = s;
+    wc[warp] = c;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = blockDim.x >> 5;
+    s = lane < nw ? ws[lane] : 0.0;
+    c = lane < nw ? wc[lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double s2 = __shfl_down_sync(FULL, s, o), c2 = __shfl_down_sync(FULL, c, o);
+      if (lane < o) pair_add(s, c, s2, c2);
+    }
+  }
+}
+
+// Sum of the partial pairs part[stride * b + off], b < nparts, the same in
+// every block: each lane of warp 0 adds a fixed stretch, then a fixed tree;
+// the result is broadcast through shared memory.
+__device__ __forceinline__ double sum_parts(const double* __restrict__ part, int nparts,
+                                            int stride, int off) {
+  __shared__ double res;
+  __syncthreads();  // res may still be read after a previous call
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    const int per = (nparts + 31) / 32;
+    double s = 0.0, c = 0.0;
+    for (int b = lane * per; b < min(nparts, (lane + 1) * per); ++b)
+      pair_add(s, c, part[stride * b + off], part[stride * b + off + 1]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double s2 = __shfl_down_sync(0xFFFFFFFFu, s, o);
+      const double c2 = __shfl_down_sync(0xFFFFFFFFu, c, o);
+      if (lane < o) pair_add(s, c, s2, c2);
+    }
+    if (lane == 0) res = s + c;
+  }
+  __syncthreads();
+  return res;
+}
+
+// Ap = H p, partial pairs of p . Ap to part[2 b]; 8 lanes per row.
+__global__ void __launch_bounds__(kOtThreads)
+pcg_spmv_kernel(const uint32_t* __restrict__ rowptr, const uint32_t* __restrict__ col,
+                const double* __restrict__ val, const double* __restrict__ diag,
+                const double* __restrict__ x, uint32_t n, double* __restrict__ y,
+                double* __restrict__ part, const CgScalars* __restrict__ sc) {
+  if (sc->done) return;
+  const int sub = threadIdx.x & (kRowLanes - 1);
+  const unsigned FULL = 0xFFFFFFFFu;
+  double s = 0.0, cc = 0.0;
+  const uint32_t rows_per_block = kOtThreads / kRowLanes;
+  const uint32_t nblk = (n + rows_per_block - 1) / rows_per_block;
+  const uint32_t per = (nblk + gridDim.x - 1) / gridDim.x;  // contiguous row blocks
+  for (uint32_t rb = blockIdx.x * per; rb < min(nblk, (blockIdx.x + 1) * per); ++rb) {
+    const uint32_t i = rb * rows_per_block + threadIdx.x / kRowLanes;
+    double acc = 0.0;
+    if (i < n)
+      for (uint32_t k = rowptr[i] + sub; k < rowptr[i + 1]; k += kRowLanes) acc += val[k] * x[col[k]];
+#pragma unroll
+    for (int o = kRowLanes / 2; o > 0; o >>= 1) acc += __shfl_down_sync(FULL, acc, o, kRowLanes);
+    if (sub == 0 && i < n) {
+      const double yi = diag[i] * x[i] + acc;
+      y[i] = yi;
+      neu_add(s, cc, x[i] * yi);
+    }
+  }
+  block_pair(s, cc);
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = s;
+    part[2 * blockIdx.x + 1] = cc;
+  }
+}
+
+// alpha = rz / pAp; x += alpha p; r -= alpha Ap; z = r / diag; partial
+// pairs of r . r and r . z to part_b[4 b .. 4 b + 3].
+__global__ void __launch_bounds__(kOtThreads)
+pcg_xr_kernel(const double* __restrict__ part_a, double* __restrict__ x, double* __restrict__ r,
+              const double* __restrict__ p, const double* __restrict__ Ap,
+              const double* __restrict__ diag, double* __restrict__ z, uint32_t n,
+              double* __restrict__ part_b, CgScalars* __restrict__ sc, uint32_t k) {
+  if (sc->done) return;
+  const double pAp = sum_parts(part_a, gridDim.x, 2, 0);
+  if (!(pAp > 0.0)) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) sc->done = 1;
+    return;
+  }
+  const double alpha = sc->rz[k & 1] / pAp;
+  const uint32_t chunk = (n + gridDim.x - 1) / gridDim.x;
+  const uint32_t lo = blockIdx.x * chunk, hi = min(n, lo + chunk);
+  double s1 = 0.0, c1 = 0.0, s2 = 0.0, c2 = 0.0;
+  for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+    x[i] = fma(alpha, p[i], x[i]);
+    const double ri = fma(-alpha, Ap[i], r[i]);
+    r[i] = ri;
+    const double d = diag[i];
+    const double zi = d > 0.0 ? ri / d : ri;
+    z[i] = zi;
+    neu_add(s1, c1, ri * ri);
+    neu_add(s2, c2, ri * zi);
+  }
+  block_pair(s1, c1);
+  block_pair(s2, c2);
+  if (threadIdx.x == 0) {
+    part_b[4 * blockIdx.x] = s1;
+    part_b[4 * blockIdx.x + 1] = c1;
+    part_b[4 * blockIdx.x + 2] = s2;
+    part_b[4 * blockIdx.x + 3] = c2;
+  }
+}
+
+// beta = rz' / rz; p = z + beta p; block 0 records rz', the iteration and
+// convergence.
+__global__ void __launch_bounds__(kOtThreads)
+pcg_p_kernel(const double* __restrict__ part_b, double* __restrict__ p,
+             const double* __restrict__ z, uint32_t n, CgScalars* __restrict__ sc, uint32_t k) {
+  if (sc->done) return;
+  const double rr = sum_parts(part_b, gridDim.x, 4, 0);
+  const double rz_new = sum_parts(part_b, gridDim.x, 4, 2);
+  const double beta = rz_new / sc->rz[k & 1];
+  const uint32_t chunk = (n + gridDim.x - 1) / gridDim.x;
+  const uint32_t lo = blockIdx.x * chunk, hi = min(n, lo + chunk);
+  for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x) p[i] = fma(beta, p[i], z[i]);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    sc->rz[(k + 1) & 1] = rz_new;
+    sc->k = k + 1;
+    if (rr <= sc->tol2 * sc->b2) sc->done = 1;
+  }
+}
+
+void pcg_iterations(const Hessian& H, double* x, double* r, double* p, double* Ap, double* z,
+                    double* part_a, double* part_b, CgScalars* sc, uint32_t k0, uint32_t count,
+                    cudaStream_t st) {
+  for (uint32_t j = 0; j < count; ++j) {
+    pcg_spmv_kernel<<<kPcgParts, kOtThreads, 0, st>>>(H.rowptr, H.col, H.val, H.diag, p, H.n,
+                                                      Ap, part_a, sc); count_launch();
+    pcg_xr_kernel<<<kPcgParts, kOtThreads, 0, st>>>(part_a, x, r, p, Ap, H.diag, z, H.n,
+                                                    part_b, sc, k0 + j); count_launch();
+    pcg_p_kernel<<<kPcgParts, kOtThreads, 0, st>>>(part_b, p, z, H.n, sc, k0 + j); count_launch();
+  }
+}
+
 }  // namespace gbv

@@ -45,6 +45,27 @@ void cg_update_xr(double* x, double* r, const double* p, const double* Ap, doubl
 void cg_precond(const double* r, const double* diag, double* z, uint32_t n, cudaStream_t st);
 void cg_update_p(double* p, const double* z, double beta, uint32_t n, cudaStream_t st);
 void axpy(double* y, const double* x, double alpha, uint32_t n, cudaStream_t st);
+
+// Preconditioned CG iterations with every scalar on the device: the host
+// launches `count` iterations (numbered k0, k0 + 1, ...) without waiting,
+// and reads k and done afterwards.  Iteration k: Ap = H p and p . Ap
+// (per-block Neumaier partials), alpha = rz / pAp, x += alpha p,
+// r -= alpha Ap, z = r / diag, then rr = r . r and rz' = r . z, p = z +
+// (rz' / rz) p; done once rr <= tol2 * b2 (or pAp <= 0).  Every block
+// combines the same partials in the same order, so the run is
+// deterministic; rz alternates between two slots so that no block reads a
+// value another block of the same launch is writing.
+struct CgScalars {
+  double rz[2];
+  double b2;     // squared norm of the right-hand side
+  double tol2;   // squared relative tolerance
+  uint32_t k;    // iterations done
+  uint32_t done;
+};
+constexpr int kPcgParts = 8 * 152;  // blocks of the CG kernels (8 per SM)
+void pcg_iterations(const Hessian& H, double* x, double* r, double* p, double* Ap, double* z,
+                    double* part_a, double* part_b, CgScalars* sc, uint32_t k0, uint32_t count,
+                    cudaStream_t st);
 void add_scalar(double* y, double c, uint32_t n, cudaStream_t st);
 void scale_copy(double* y, const double* x, double alpha, uint32_t n, cudaStream_t st);
 

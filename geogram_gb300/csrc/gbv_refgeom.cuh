@@ -74,4 +74,39 @@ __device__ __forceinline__ double r_tet_volume(const double3& p1, const double3&
   return __ddiv_rn(fabs(d), 6.0);
 }
 
+// det4x4 of convex_cell.h:383-402 with the reference's operation order (no
+// fused multiply-add): the sign of the fast-predicate conflict test
+// (convex_cell.cpp:947-966, conflict iff > 0).  Columns: the planes of the
+// triangle's three vertices and the clipping plane.
+__device__ __forceinline__ double r_det4x4(const double4& p1, const double4& p2,
+                                           const double4& p3, const double4& e) {
+  const double a11 = p1.x, a12 = p2.x, a13 = p3.x, a14 = e.x;
+  const double a21 = p1.y, a22 = p2.y, a23 = p3.y, a24 = e.y;
+  const double a31 = p1.z, a32 = p2.z, a33 = p3.z, a34 = e.z;
+  const double a41 = p1.w, a42 = p2.w, a43 = p3.w, a44 = e.w;
+  const double m12 = __dsub_rn(__dmul_rn(a21, a12), __dmul_rn(a11, a22));
+  const double m13 = __dsub_rn(__dmul_rn(a31, a12), __dmul_rn(a11, a32));
+  const double m14 = __dsub_rn(__dmul_rn(a41, a12), __dmul_rn(a11, a42));
+  const double m23 = __dsub_rn(__dmul_rn(a31, a22), __dmul_rn(a21, a32));
+  const double m24 = __dsub_rn(__dmul_rn(a41, a22), __dmul_rn(a21, a42));
+  const double m34 = __dsub_rn(__dmul_rn(a41, a32), __dmul_rn(a31, a42));
+  const double m123 =
+      __dadd_rn(__dsub_rn(__dmul_rn(m23, a13), __dmul_rn(m13, a23)), __dmul_rn(m12, a33));
+  const double m124 =
+      __dadd_rn(__dsub_rn(__dmul_rn(m24, a13), __dmul_rn(m14, a23)), __dmul_rn(m12, a43));
+  const double m134 =
+      __dadd_rn(__dsub_rn(__dmul_rn(m34, a13), __dmul_rn(m14, a33)), __dmul_rn(m13, a43));
+  const double m234 =
+      __dadd_rn(__dsub_rn(__dmul_rn(m34, a23), __dmul_rn(m24, a33)), __dmul_rn(m23, a43));
+  return __dsub_rn(__dadd_rn(__dsub_rn(__dmul_rn(m234, a14), __dmul_rn(m134, a24)),
+                             __dmul_rn(m124, a34)),
+                   __dmul_rn(m123, a44));
+}
+
+// With the fast predicates a conflict test whose filter margin is below
+// this multiple of its error bound is decided by r_det4x4 (whose own
+// rounding could then differ from the exact sign); beyond it every
+// evaluation has the exact sign.
+constexpr double kFastPredWide = 64.0;
+
 }  // namespace gbv

@@ -79,8 +79,17 @@ typedef struct {
                             longer first list gives the same cells with fewer
                             passes); 0: automatic (96 without weights, 128
                             with), at most 128 */
-    uint32_t reserved;   /* 0 */
+    uint32_t predicates; /* gbv_predicates */
 } gbv_cell_options;
+
+typedef enum {
+    /* PCK::det_4d, the ConvexCell default (convex_cell.cpp:873-912) */
+    GBV_PREDICATES_EXACT = 0,
+    /* use_exact_predicates(false): the FP64 det4x4 of convex_cell.h:383-402,
+     * conflict iff > 0 (convex_cell.cpp:947-966); differs from the exact
+     * mode only on degenerate configurations */
+    GBV_PREDICATES_FAST = 1
+} gbv_predicates;
 
 typedef enum {
     /* the reference's security-radius loop (generic_RVD.h:2278-2352) on
@@ -369,6 +378,31 @@ gbv_status gbv_ot_separable_start(gbv_context* ctx, const double* d_xyz, uint32_
  * multiple of 32, lda and ldb multiples of 8. */
 gbv_status gbv_mlp_gemm_nt(gbv_context* ctx, const void* d_a, int lda, const void* d_bt,
                            int ldb, float* d_c, int ldc, int M, int N, int K, void* stream);
+
+/* ---------------------------------------------------------------- */
+/* Cells restricted to a tetrahedral mesh                            */
+/* ---------------------------------------------------------------- */
+
+/* Replaces RestrictedVoronoiDiagram with set_volumetric(true)
+ * (voronoi/RVD.h:180) and its compute_centroids (RVD.h:284-290;
+ * RVD.cpp:429-530) and compute_CVT_func_grad (RVD.h:295-320;
+ * RVD.cpp:792-910): the cells of the seeds (Voronoi, or Laguerre with
+ * weights w) restricted to the union of the tetrahedra, for CVT and optimal
+ * transport on non-cube domains.  Host arrays: mesh_xyz[3 nv], tets[4 nt]
+ * (vertex indices, any orientation), xyz[3 n], w[n] or NULL.  opt gives
+ * k0, check_sr and precision; its box is replaced by the bounding box of
+ * the mesh and the seeds.  Outputs (any may be NULL): m[n] and mg[3 n], the
+ * mass and first moment of each restricted cell; *f and g[3 n], the CVT
+ * energy sum_i int_{cell_i} |x - p_i|^2 and its gradient formed as the
+ * reference forms them: cones from each seed to the border of its
+ * restricted cell with unsigned volumes (for a cell star-shaped from its
+ * seed, the exact integral and 2 (m_i p_i - mg_i)).  Afterwards the
+ * context holds the unrestricted cells (gbv_cells_fetch). */
+gbv_status gbv_restricted_cells(gbv_context* ctx, const double* mesh_xyz, uint32_t nv,
+                                const uint32_t* tets, uint32_t nt, const double* xyz,
+                                const double* w, uint32_t n, const gbv_cell_options* opt,
+                                double* m, double* mg, double* f, double* g,
+                                gbv_cell_report* report);
 
 /* ---------------------------------------------------------------- */
 /* Cell polytopes (output formats)                                   */

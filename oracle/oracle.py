@@ -85,6 +85,8 @@ def ref():
         lib.ref_cells_save.argtypes = [P, P, U, U, ctypes.c_int, P, U, ctypes.c_double, P,
                                        ctypes.c_size_t]
         lib.ref_cells_save.restype = ctypes.c_long
+        lib.ref_rvd_volume.argtypes = [P, U, P, U, P, U, P, P, P, P]
+        lib.ref_set_walk.argtypes = [ctypes.c_int]
         lib.ref_init()
         _ref = lib
     return _ref
@@ -109,8 +111,11 @@ def knn(pts: np.ndarray, k: int, nthreads: int = 1, which: str = "port"):
 
 
 def cells(xyz: np.ndarray, w: np.ndarray | None = None, k0: int = 20, check_sr: bool = True,
-          exact: bool = True, nthreads: int = 1, which: str = "port", max_nbr: int = 96) -> dict:
-    """Certified cells in the unit box; dict of per-seed arrays plus CSR."""
+          exact: bool = True, nthreads: int = 1, which: str = "port", max_nbr: int = 96,
+          walk: bool = False) -> dict:
+    """Certified cells in the unit box; dict of per-seed arrays plus CSR.
+    exact=False: the reference's inexact predicates; walk=True (reference
+    build only): clipped by ConvexCell::clip_by_plane_fast."""
     x = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
     n = len(x)
     wa = None if w is None else np.ascontiguousarray(w, dtype=np.float64)
@@ -126,13 +131,15 @@ def cells(xyz: np.ndarray, w: np.ndarray | None = None, k0: int = 20, check_sr: 
         r = port().orc_cells(*args, ctypes.byref(ne))
         out["n_exact"] = ne.value
     else:
+        ref().ref_set_walk(1 if walk else 0)
         r = ref().ref_cells(*args)
+        ref().ref_set_walk(0)
     if r != 0:
         raise RuntimeError("cells failed")
     cnt = out["cnt"].astype(np.int64)
     if (out["status"] == 4).any():
         # a cell with more facets than max_nbr: again with room for all
-        return cells(x, wa, k0, check_sr, exact, nthreads, which, int(cnt.max()) + 1)
+        return cells(x, wa, k0, check_sr, exact, nthreads, which, int(cnt.max()) + 1, walk)
     rowptr = np.zeros(n + 1, np.int64)
     rowptr[1:] = np.cumsum(cnt)
     mask = np.arange(max_nbr)[None, :] < cnt[:, None]
@@ -219,6 +226,24 @@ def ref_cells_obj(xyz: np.ndarray, w: np.ndarray | None, which, shrink: float = 
         if r >= 0:
             return buf.value.decode()
         cap *= 4
+
+
+def ref_rvd_volume(mesh_xyz: np.ndarray, tets: np.ndarray, seeds: np.ndarray) -> dict:
+    """The reference's volumetric RestrictedVoronoiDiagram of the seeds in
+    the tetrahedral mesh: mass and first moment per cell (compute_centroids),
+    CVT energy and gradient (compute_CVT_func_grad).  Reference build only."""
+    v = np.ascontiguousarray(mesh_xyz, dtype=np.float64).reshape(-1, 3)
+    t = np.ascontiguousarray(tets, dtype=np.uint32).reshape(-1, 4)
+    x = np.ascontiguousarray(seeds, dtype=np.float64).reshape(-1, 3)
+    n = len(x)
+    out = dict(m=np.zeros(n), mg=np.zeros((n, 3)), g=np.zeros((n, 3)))
+    f = ctypes.c_double(0.0)
+    r = ref().ref_rvd_volume(_p(v), len(v), _p(t), len(t), _p(x), n, _p(out["mg"]), _p(out["m"]),
+                             ctypes.byref(f), _p(out["g"]))
+    if r != 0:
+        raise RuntimeError("ref_rvd_volume failed")
+    out["f"] = f.value
+    return out
 
 
 def det4_sign(p0, p1, p2, p3) -> int:

@@ -30,12 +30,16 @@
 #include <geogram/basic/logger.h>
 #include <geogram/basic/process.h>
 #include <geogram/basic/command_line.h>
+#include <geogram/basic/command_line_args.h>
 #include <geogram/basic/file_system.h>
 #include <geogram/basic/progress.h>
 #include <geogram/basic/stopwatch.h>
 #include <geogram/numerics/predicates.h>
 #include <geogram/points/nn_search.h>
 #include <geogram/voronoi/convex_cell.h>
+#include <geogram/voronoi/RVD.h>
+#include <geogram/delaunay/delaunay.h>
+#include <geogram/mesh/mesh.h>
 
 #include <algorithm>
 #include <atomic>
@@ -48,6 +52,8 @@
 namespace {
 
 bool g_initialised = false;
+// 1: clip with ConvexCell::clip_by_plane_fast (convex_cell.cpp:599-757)
+int g_walk = 0;
 
 void ensure_init() {
     if (g_initialised) return;
@@ -58,6 +64,11 @@ void ensure_init() {
     GEO::CmdLine::initialize();
     GEO::Stopwatch::initialize();
     GEO::PCK::initialize();
+    GEO::Delaunay::initialize();
+    // the argument groups the Delaunay and RVD factories read
+    // (algo:delaunay, algo:predicates, dbg:*), with their defaults
+    GEO::CmdLine::import_arg_group("standard");
+    GEO::CmdLine::import_arg_group("algo");
     GEO::Logger::instance()->set_quiet(true);
     g_initialised = true;
 }
@@ -163,7 +174,8 @@ int clip_cell(VBW::ConvexCell& C, const GEO::NearestNeighborSearch* nn, const do
                 2.0 * (xyz[3 * i + 1] - xyz[3 * j + 1]),
                 2.0 * (xyz[3 * i + 2] - xyz[3 * j + 2]),
                 (wi - pi_len2) - (wj - pj_len2));
-            C.clip_by_plane(P, j);
+            if (g_walk) C.clip_by_plane_fast(P, j);
+            else C.clip_by_plane(P, j);
         }
         if (done) break;
         if (!check_sr) { st = 0; break; }
@@ -185,6 +197,13 @@ extern "C" {
 
 int ref_init(void) {
     ensure_init();
+    return 0;
+}
+
+/* Selects clip_by_plane_fast (walk = 1) or clip_by_plane (walk = 0) for
+ * the cell functions below. */
+int ref_set_walk(int walk) {
+    g_walk = walk;
     return 0;
 }
 
@@ -305,6 +324,50 @@ long ref_cells_save(const double* xyz, const double* w, unsigned n, unsigned k0,
     if (txt.size() + 1 > cap) return -1;
     std::memcpy(out, txt.c_str(), txt.size() + 1);
     return long(txt.size());
+}
+
+/*
+ * Voronoi cells restricted to a tetrahedral mesh (volumetric RVD,
+ * voronoi/RVD.cpp compute_centroids_in_volume :500-530 and
+ * compute_CVT_func_grad_in_volume :878-910) of the seeds, with the
+ * reference's own Delaunay triangulation ("BDEL") and
+ * RestrictedVoronoiDiagram.
+ *   verts[3 nv], tets[4 nt] (vertex indices), seeds[3 n]
+ * Outputs: mg[3 n], m[n] (mass and first moment of each restricted cell),
+ * *f and g[3 n] (the CVT energy sum_i int |x - p_i|^2 over the restricted
+ * cells and its gradient).  nthreads = 1 keeps the reference single-threaded.
+ */
+int ref_rvd_volume(const double* verts, unsigned nv, const unsigned* tets, unsigned nt,
+                   const double* seeds, unsigned n, double* mg, double* m, double* f,
+                   double* g) {
+    ensure_init();
+    GEO::Process::set_max_threads(1);
+    GEO::Mesh M(3);
+    M.vertices.create_vertices(nv);
+    for (unsigned v = 0; v < nv; ++v)
+        for (unsigned c = 0; c < 3; ++c) M.vertices.point_ptr(v)[c] = verts[3 * size_t(v) + c];
+    M.cells.create_tets(nt);
+    for (unsigned t = 0; t < nt; ++t)
+        for (unsigned k = 0; k < 4; ++k) M.cells.set_vertex(t, k, tets[4 * size_t(t) + k]);
+    M.cells.connect();
+    // the RVD configures the triangulation it observes: created first, as
+    // compute_RVD/main.cpp and CVT.cpp:55-75 do, then the seeds are set
+    GEO::Delaunay_var del = GEO::Delaunay::create(3, "BDEL");
+    GEO::RestrictedVoronoiDiagram_var rvd = GEO::RestrictedVoronoiDiagram::create(del, &M);
+    del->set_vertices(n, seeds);
+    rvd->set_volumetric(true);
+    for (size_t k = 0; k < size_t(n); ++k) {
+        m[k] = 0.0;
+        for (int c = 0; c < 3; ++c) {
+            mg[3 * k + c] = 0.0;
+            g[3 * k + c] = 0.0;
+        }
+    }
+    rvd->compute_centroids(mg, m);
+    double fv = 0.0;
+    rvd->compute_CVT_func_grad(fv, g);
+    *f = fv;
+    return 0;
 }
 
 }  // extern "C"

@@ -79,6 +79,44 @@ def laguerre_cases():
     yield "laguerre_ot_1200", x, w
 
 
+def kuhn_grid(k: int, keep=lambda i, j, l: True):
+    """The cubes (i, j, l) of a k^3 grid on [0,1]^3 that keep() accepts, each
+    split into the 6 Kuhn tetrahedra (conforming across cubes), positively
+    oriented."""
+    import itertools
+    vid = lambda i, j, l: (l * (k + 1) + j) * (k + 1) + i
+    g = np.arange(k + 1) / k
+    verts = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).transpose(2, 1, 0, 3).reshape(-1, 3)
+    tets = []
+    for i, j, l in itertools.product(range(k), repeat=3):
+        if not keep(i, j, l):
+            continue
+        for perm in itertools.permutations(range(3)):
+            p = [i, j, l]
+            tv = [vid(*p)]
+            for a in perm:
+                p[a] += 1
+                tv.append(vid(*p))
+            a, b, c, d = verts[tv]
+            if np.dot(np.cross(b - a, c - a), d - a) < 0:
+                tv[1], tv[2] = tv[2], tv[1]
+            tets.append(tv)
+    return verts, np.array(tets, np.uint32)
+
+
+def rvd_cases():
+    cases = {}
+    v, t = kuhn_grid(1)
+    cases["cube_300"] = (v, t, np.random.default_rng(6).random((300, 3)))
+    # an L-shaped (non-convex) domain: the 4^3 grid without the cubes where
+    # x > 1/2 and z > 1/2; seeds inside it
+    v, t = kuhn_grid(4, lambda i, j, l: not (i >= 2 and l >= 2))
+    x = np.random.default_rng(7).random((1200, 3))
+    x = x[~((x[:, 0] > 0.5) & (x[:, 2] > 0.5))][:500]
+    cases["lshape_500"] = (v, t, x)
+    return cases
+
+
 def main(only=None):
     """Writes every fixture, or only those whose names are listed."""
     oracle.build_ref()
@@ -102,6 +140,24 @@ def main(only=None):
                             rowptr=r["rowptr"], nbr=r["nbr"], area=r["area"],
                             status=r["status"], n_clip=r["n_clip"], k_list=r["k_list"])
         print(name, len(x), "cells, nnz", len(r["nbr"]))
+    if not only or "fast" in only:
+        # the reference's other clipping variants: inexact predicates
+        # (use_exact_predicates(false)) and clip_by_plane_fast.  Not on the
+        # lattice: with inexact predicates the reference crashes there
+        # (inconsistent signs on exactly degenerate configurations).
+        variants = [("fast_clustered_1500", "clustered_1500", False, False),
+                    ("walk_power_1500", "power_1500", True, True),
+                    ("fastwalk_uniform_1500", "uniform_1500", False, True)]
+        for name, src, exact, walk in variants:
+            d = np.load(os.path.join(HERE, f"cells_{src}.npz"))
+            x, w = d["x"], (d["w"] if d["w"].size else None)
+            r = oracle.cells(x, w, exact=exact, walk=walk, nthreads=8, which="ref", max_nbr=2100)
+            np.savez_compressed(os.path.join(HERE, f"cells_{name}.npz"), x=x,
+                                w=np.zeros(0) if w is None else w, vol=r["vol"], mg=r["mg"],
+                                rowptr=r["rowptr"], nbr=r["nbr"], area=r["area"],
+                                status=r["status"], n_clip=r["n_clip"], k_list=r["k_list"],
+                                exact=np.array(exact), walk=np.array(walk))
+            print(name, "exact" if exact else "fast", "walk" if walk else "scan")
     if not only or "obj" in only:
         # ConvexCell::save text of some cells (interior, at the box, of
         # weighted seeds), plain and shrunk
@@ -114,6 +170,14 @@ def main(only=None):
             np.savez_compressed(os.path.join(HERE, f"obj_{src}.npz"), which=which,
                                 obj=np.array(txt), obj_shrink=np.array(txt_s))
             print(f"obj_{src}", len(txt), "bytes")
+    if not only or "rvd" in only:
+        # cells restricted to tetrahedral meshes, by the reference's own
+        # Delaunay + RestrictedVoronoiDiagram (volumetric)
+        for name, (v, t, x) in rvd_cases().items():
+            r = oracle.ref_rvd_volume(v, t, x)
+            np.savez_compressed(os.path.join(HERE, f"rvd_{name}.npz"), mesh_xyz=v, tets=t, x=x,
+                                m=r["m"], mg=r["mg"], f=np.array(r["f"]), g=r["g"])
+            print(f"rvd_{name}", len(t), "tets", len(x), "seeds, sum m", r["m"].sum())
     if only:
         return
     x = np.random.default_rng(3).random((2000, 3))

@@ -178,3 +178,16 @@ def test_first_list_length_does_not_change_cells(g, first_k, prec):
     ref = load_golden("cells_power_1500.npz")
     c = g.compute_cells(ref["x"], ref["w"], precision=prec, first_k=first_k)
     assert_cells_equal(c, ref)
+
+
+@pytest.mark.parametrize("prec", PRECISIONS)
+@pytest.mark.parametrize("name", ["fast_clustered_1500", "walk_power_1500",
+                                  "fastwalk_uniform_1500"])
+def test_fast_predicates_and_walk_vs_reference(g, name, prec):
+    """The reference run with use_exact_predicates(false) and/or
+    clip_by_plane_fast: the fast-predicate mode (and the default mode for the
+    walk) reproduces it bit for bit."""
+    ref = load_golden(f"cells_{name}.npz")
+    c = g.compute_cells(ref["x"], ref["w"], precision=prec,
+                        predicates="exact" if bool(ref["exact"]) else "fast")
+    assert_cells_equal(c, ref)

@@ -107,3 +107,32 @@ def test_reference_confirms_ot_weights():
     n = len(g["x"])
     assert np.max(np.abs(g["vol"] * n - 1.0)) < 1e-8
     assert abs(g["vol"].sum() - 1.0) < 1e-12
+
+
+@pytest.mark.parametrize("name,volume", [("cube_300", 1.0), ("lshape_500", 0.75)])
+def test_restricted_fixtures_consistent(name, volume):
+    """The reference's restricted cells tile their domain; on the cube, where
+    every restricted cell is convex and holds its seed, its CVT gradient is
+    2 (m p - mg) (RVD.cpp:792-870).  (On the L-shape it is not: the
+    reference fans each cell's border from the seed with unsigned volumes.)"""
+    from conftest import load_golden
+    d = load_golden(f"rvd_{name}.npz")
+    assert abs(d["m"].sum() - volume) < 1e-12
+    if name == "cube_300":  # convex cells: the exact gradient
+        assert np.max(np.abs(d["g"] - 2 * (d["m"][:, None] * d["x"] - d["mg"]))) < 1e-15
+
+
+@pytest.mark.parametrize("name,src", [("fast_clustered_1500", "clustered_1500"),
+                                      ("walk_power_1500", "power_1500"),
+                                      ("fastwalk_uniform_1500", "uniform_1500")])
+def test_fast_and_walk_variants_pinned(oracle_mod, name, src):
+    """The reference's inexact predicates and its walk-based
+    clip_by_plane_fast give, on these non-degenerate sets, the exact scan's
+    cells bit for bit (fixtures from the reference build); the port in its
+    fast mode reproduces them."""
+    f, e = load_golden(f"cells_{name}.npz"), load_golden(f"cells_{src}.npz")
+    for key in ("vol", "mg", "rowptr", "nbr", "area", "status"):
+        assert np.array_equal(f[key], e[key]), key
+    r = oracle_mod.cells(f["x"], f["w"], exact=bool(f["exact"]), nthreads=4)
+    assert np.array_equal(r["vol"], f["vol"]) and np.array_equal(r["nbr"], f["nbr"])
+    assert np.array_equal(r["area"], f["area"])
