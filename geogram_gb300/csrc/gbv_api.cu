@@ -834,6 +834,7 @@ static void cells_device(gbv_context* c, const double* d_xyz, const double* d_w,
     ka.flag_count = flag_count;
     ka.flag_list = flag_list;
     ka.coherent = true;  // every slot, in sorted order
+    ka.tile_scratch = c->buf<uint32_t>("knn_tiles", knn_tile_scratch_elems(n, S.L));
     if (K > kKnnMaxK) {  // only without the security radius
       ka.gl_d2 = c->buf<double>("knn_gd2", (size_t)K * n);
       ka.gl_slot = c->buf<uint32_t>("knn_gslot", (size_t)K * n);
@@ -1004,6 +1005,7 @@ static bool laguerre_device(gbv_context* c, const double* d_xyz, const double* d
     ka.flag_count = c->buf<uint32_t>("knn_flag_count", 1);
     ka.flag_list = c->buf<uint32_t>("knn_flag_list", n);
     ka.coherent = true;
+    ka.tile_scratch = c->buf<uint32_t>("knn_tiles", knn_tile_scratch_elems(n, S.L));
     launch_knn(ka, st);
   }
   GBV_CUDA(cudaGetLastError());
@@ -1150,6 +1152,7 @@ static void mlp_features_device(gbv_context* c, const double* d_xyz, uint32_t n,
   ka.flag_count = c->buf<uint32_t>("knn_flag_count", 1);
   ka.flag_list = c->buf<uint32_t>("nn_flag_list", n);
   ka.coherent = true;
+  ka.tile_scratch = c->buf<uint32_t>("knn_tiles", knn_tile_scratch_elems(n, S.L));
   launch_knn(ka, st);
   mlp_features(d_xyz, od, n, d_raw, st);
   GBV_CUDA(cudaGetLastError());
@@ -2106,6 +2109,7 @@ gbv_status gbv_nn_get_nearest_neighbors_all(gbv_context* c, uint32_t k, uint32_t
     ka.flag_count = c->buf<uint32_t>("knn_flag_count", 1);
     ka.flag_list = c->buf<uint32_t>("nn_flag_list", n);
     ka.coherent = true;
+    ka.tile_scratch = c->buf<uint32_t>("knn_tiles", knn_tile_scratch_elems(n, c->S.L));
     if (k > kKnnMaxK) {
       ka.gl_d2 = c->buf<double>("nn_gd2", (size_t)k * n);
       ka.gl_slot = c->buf<uint32_t>("nn_gslot", (size_t)k * n);

@@ -919,21 +919,29 @@ static void launch_knn_exact(const KnnArgs& a, const uint32_t* qsel, const uint3
   }
 }
 
-// ---- warp-synchronous search: lists up to kKnnMaxK in shared memory --------
-// A warp takes 32 consecutive queries (consecutive sorted slots are close in
-// space) and walks the implicit octree once for all of them: a node is
-// skipped when its box is farther from the box around the 32 queries than
-// every query's pruning distance, and each leaf's seeds are staged in shared
-// memory (coalesced loads) and offered to all 32 queries, each keeping its
-// k + kKnnExtra nearest by FP32 distance in its own max-heap (column `lane`
-// of a [k][32] array: conflict-free).  The traversal, the loads and the
-// distance computations are the same for all lanes; only heap updates
-// diverge.  The kept seeds are sorted by FP32 distance; two neighbours in
-// that order whose FP32 distances are farther apart than their error bound
-// are in exact order already, and runs of closer ones are re-ranked in FP64
-// by (d2, original index), so the lists equal the exact search's.
-constexpr int kWarpKnnWarps = 2;
+// ---- tiled search: lists up to kKnnMaxK in shared memory --------------------
+// The queries are cut into tiles: the largest octree nodes with at most
+// kTileMax seeds (a fine cell with more is cut into pieces of 32
+// consecutive slots), 32 queries at most per tile, one warp per tile.  A
+// warp reads the seeds of the 27 nodes of the tile's level around the tile,
+// then those of the surrounding nodes that its pruning distance still
+// reaches, gathered 32 at a time across node boundaries (a warp scan of the
+// node counts) and staged in shared memory; every lane tests every staged
+// seed against its own query.  A seed nearer than the lane's pruning
+// distance goes to the lane's buffer; after each chunk of 32 the lanes empty
+// their buffers into their own max-heaps of the k + kKnnExtra nearest by
+// FP32 distance together (column `lane` of [k][32] arrays: conflict-free).
+// The first pruning distance comes from the tile's seed density; a lane
+// that finds fewer seeds than the heap holds within it takes the exact
+// search instead.  The kept seeds are sorted by FP32 distance; neighbours in
+// that order farther apart than their error bound are in exact order
+// already, and runs of closer ones are re-ranked in FP64 by (d2, original
+// index), so the lists equal the exact search's.
+constexpr uint32_t kTileMax = 64;
 
+// Squared distance (fine-cell units) between the box of node (ix, iy, iz)
+// of side `side` and the box [lo, hi], shrunk by a small slack as
+// node_box_d2.
 __device__ __forceinline__ float box_box_d2(uint32_t ix, uint32_t iy, uint32_t iz, float side,
                                             const float* lo, const float* hi) {
   const float bx = ix * side, by = iy * side, bz = iz * side;
@@ -946,55 +954,116 @@ __device__ __forceinline__ float box_box_d2(uint32_t ix, uint32_t iy, uint32_t i
   return dx * dx + dy * dy + dz * dz;
 }
 
-size_t knn_warp_smem(uint32_t k) {
-  return sizeof(float4) * 32 * kWarpKnnWarps +
-         (size_t)kWarpKnnWarps * (k + kKnnExtra) * 32 * (sizeof(float) + sizeof(uint32_t));
+size_t knn_tile_smem(uint32_t k) {
+  // staged seeds (float4 + slot), the lane buffers, the heaps
+  return 32 * (sizeof(float4) + sizeof(uint32_t)) + 32 * 32 * sizeof(uint2) +
+         (size_t)(k + kKnnExtra) * 32 * (sizeof(float) + sizeof(uint32_t));
 }
 
-__global__ void __launch_bounds__(32 * kWarpKnnWarps)
-knn_warp_kernel(KnnArgs a, SortedSeeds S, const GridDesc* __restrict__ gdp,
-                const double* __restrict__ aux) {
+size_t knn_tile_scratch_elems(uint32_t n, int L) {
+  const size_t nf = ((size_t)1 << (3 * L)) + 1;
+  return nf + scan_tmp_elems(nf) + 2 * ((size_t)n + nf) + 2;
+}
+
+// Level of the tile holding fine cell f (the highest ancestor with at most
+// kTileMax seeds, or L); its seed range in b/e.
+__device__ __forceinline__ int tile_level(const uint32_t* __restrict__ cs, uint32_t f, int L,
+                                          uint32_t& b, uint32_t& e) {
+  int lev = L;
+  b = cs[f];
+  e = cs[f + 1];
+  for (int l = L - 1; l >= 0; --l) {
+    const int sh = 3 * (L - l);
+    const uint32_t node = f >> sh;
+    const uint32_t bb = cs[node << sh], ee = cs[(node + 1u) << sh];
+    if (ee - bb > kTileMax) break;
+    lev = l;
+    b = bb;
+    e = ee;
+  }
+  return lev;
+}
+
+// Tiles per fine cell: the cell that starts its tile emits ceil(count / 32).
+__global__ void tile_count_kernel(const uint32_t* __restrict__ cs, int L, uint32_t nf,
+                                  uint32_t* __restrict__ cnt) {
+  const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f > nf) return;
+  if (f == nf) {
+    cnt[nf] = 0;
+    return;
+  }
+  uint32_t b, e;
+  const int lev = tile_level(cs, f, L, b, e);
+  const int sh = 3 * (L - lev);
+  const bool first = ((f >> sh) << sh) == f;
+  cnt[f] = first ? (e - b + 31u) / 32u : 0u;
+}
+
+// items[t] = (first slot, count | level << 8)
+__global__ void tile_fill_kernel(const uint32_t* __restrict__ cs, int L, uint32_t nf,
+                                 const uint32_t* __restrict__ off, uint2* __restrict__ items) {
+  const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nf) return;
+  const uint32_t m = off[f + 1] - off[f];
+  if (m == 0) return;
+  uint32_t b, e;
+  const int lev = tile_level(cs, f, L, b, e);
+  for (uint32_t k = 0; k < m; ++k) {
+    const uint32_t s0 = b + 32u * k;
+    items[off[f] + k] = make_uint2(s0, min(32u, e - s0) | ((uint32_t)lev << 8));
+  }
+}
+
+__global__ void __launch_bounds__(32)
+knn_tile_kernel(KnnArgs a, SortedSeeds S, const GridDesc* __restrict__ gdp,
+                const double* __restrict__ aux, const uint32_t* __restrict__ ntiles,
+                const uint2* __restrict__ items) {
   extern __shared__ __align__(16) unsigned char knn_smem[];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x;
+  const unsigned FULL = 0xFFFFFFFFu;
   const uint32_t K = a.k;
   const uint32_t cap = K + kKnnExtra;
-  float4* s_leaf = reinterpret_cast<float4*>(knn_smem) + warp * 32;
-  float* hd = reinterpret_cast<float*>(knn_smem + sizeof(float4) * 32 * kWarpKnnWarps) +
-              (size_t)warp * cap * 64;
+  float4* s_pt = reinterpret_cast<float4*>(knn_smem);
+  uint32_t* s_sl = reinterpret_cast<uint32_t*>(s_pt + 32);
+  uint2* s_buf = reinterpret_cast<uint2*>(s_sl + 32);  // [32][32] (d32 bits, slot)
+  float* hd = reinterpret_cast<float*>(s_buf + 32 * 32);
   uint32_t* hs = reinterpret_cast<uint32_t*>(hd + (size_t)cap * 32);
-  const uint32_t q0 = (blockIdx.x * kWarpKnnWarps + warp) * 32u;
-  if (q0 >= a.nq) return;  // the whole warp
-  const uint32_t qi = q0 + lane;
-  const bool active = qi < a.nq;
+  if (blockIdx.x >= *ntiles) return;
+  const uint2 item = items[blockIdx.x];
+  const uint32_t nq_tile = item.y & 0xFFu;
+  const int tlev = (int)(item.y >> 8);
+  const bool active = (uint32_t)lane < nq_tile;
+  const uint32_t qi = item.x + (active ? lane : 0);
   const GridDesc g = *gdp;
-  // lanes past the end mirror the last query and take no part
-  const QueryCtx c = make_query(a, S, g, active ? qi : a.nq - 1);
+  const QueryCtx c = make_query(a, S, g, qi);
   const float delta = 8.0f * (float)aux[1] * 5.9604645e-8f + 1e-30f;
   auto D = [&](uint32_t r) -> float& { return hd[(size_t)r * 32 + lane]; };
   auto SL = [&](uint32_t r) -> uint32_t& { return hs[(size_t)r * 32 + lane]; };
 
-  // box of the warp's queries, fine-cell units
+  // the tile's node, its box and seed count; the box of its queries
+  const int tsh = g.L - tlev;                    // node side = 2^tsh fine cells
+  const float tside = (float)(1u << tsh);
+  const int NG = 1 << tlev;                      // nodes per axis at that level
+  const int G = g.G;
+  const uint32_t fx = (uint32_t)clampi((int)c.ux, 0, G - 1);
+  const uint32_t fy = (uint32_t)clampi((int)c.uy, 0, G - 1);
+  const uint32_t fz = (uint32_t)clampi((int)c.uz, 0, G - 1);
+  const int nx = (int)__shfl_sync(FULL, fx >> tsh, 0);
+  const int ny = (int)__shfl_sync(FULL, fy >> tsh, 0);
+  const int nz = (int)__shfl_sync(FULL, fz >> tsh, 0);
   float lo[3] = {c.ux, c.uy, c.uz}, hi[3] = {c.ux, c.uy, c.uz};
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-      lo[d] = fminf(lo[d], __shfl_xor_sync(0xFFFFFFFFu, lo[d], o));
-      hi[d] = fmaxf(hi[d], __shfl_xor_sync(0xFFFFFFFFu, hi[d], o));
+      lo[d] = fminf(lo[d], __shfl_xor_sync(FULL, lo[d], o));
+      hi[d] = fmaxf(hi[d], __shfl_xor_sync(FULL, hi[d], o));
     }
   }
 
   uint32_t cnt = 0, copies = 0;
-  float thr = FLT_MAX;
   bool dup_lower = false;
-  float lo_skip = -1.f, lo_check = -1.f;
-  if (c.has_lo) {
-    const float r = sqrtf(__double2float_rd(c.lo_d));
-    const float r1 = fmaxf(r * 0.9999924f - delta, 0.f);
-    const float r2 = r * 1.0000076f + delta;
-    lo_skip = r1 * r1 * 0.9999924f;
-    lo_check = r2 * r2 * 1.0000076f;
-  }
   auto sift_down = [&](uint32_t i, uint32_t n) {
     const float d = D(i);
     const uint32_t sl = SL(i);
@@ -1017,12 +1086,9 @@ knn_warp_kernel(KnnArgs a, SortedSeeds S, const GridDesc* __restrict__ gdp,
     D(i) = d;
     SL(i) = sl;
   };
+  float thr;
   auto offer = [&](uint32_t s2, float d32) {
     if (a.mode == KNN_CELLS && s2 == c.qslot) return;
-    if (c.has_lo) {
-      if (d32 < lo_skip) return;
-      if (d32 <= lo_check && !after_lo(c, dist2_exact(c.q, S.xd[s2]), S.perm[s2])) return;
-    }
     if (a.mode == KNN_CELLS && d32 <= 0.f) {
       if (dist2_exact(c.q, S.xd[s2]) == 0.0) {
         if (S.perm[s2] < c.qperm) dup_lower = true;
@@ -1042,7 +1108,7 @@ knn_warp_kernel(KnnArgs a, SortedSeeds S, const GridDesc* __restrict__ gdp,
       }
       D(i) = d32;
       SL(i) = s2;
-      if (cnt == cap) thr = D(0);
+      if (cnt == cap) thr = fminf(thr, D(0));
     } else {
       D(0) = d32;
       SL(0) = s2;
@@ -1051,121 +1117,114 @@ knn_warp_kernel(KnnArgs a, SortedSeeds S, const GridDesc* __restrict__ gdp,
     }
   };
 
-  // ---- a first pruning distance for the warp: the queries are consecutive
-  // sorted slots, so the fine cells from the first to the last one's hold
-  // about 32 seeds; a ball of 1.35x the radius that holds cap seeds at that
-  // density (plus the largest lift difference, 4-d) should hold cap.  Too
-  // small only costs that lane the exact search; it never loses a seed.
+  // ---- first pruning distance: a ball of 1.35x the radius that holds cap
+  // seeds at the tile's density (plus the largest lift difference, 4-d)
   float t0 = FLT_MAX;
   if (a.nq > 4 * cap) {
-    const int G = g.G;
-    const uint32_t cfirst = morton3(
-        (uint32_t)clampi((int)__shfl_sync(0xFFFFFFFFu, c.ux, 0), 0, G - 1),
-        (uint32_t)clampi((int)__shfl_sync(0xFFFFFFFFu, c.uy, 0), 0, G - 1),
-        (uint32_t)clampi((int)__shfl_sync(0xFFFFFFFFu, c.uz, 0), 0, G - 1));
-    const uint32_t clast = morton3(
-        (uint32_t)clampi((int)__shfl_sync(0xFFFFFFFFu, c.ux, 31), 0, G - 1),
-        (uint32_t)clampi((int)__shfl_sync(0xFFFFFFFFu, c.uy, 31), 0, G - 1),
-        (uint32_t)clampi((int)__shfl_sync(0xFFFFFFFFu, c.uz, 31), 0, G - 1));
-    const uint32_t lo_c = min(cfirst, clast), hi_c = max(cfirst, clast);
-    const float rho = 32.f / (float)(hi_c - lo_c + 1u);  // seeds per fine cell
+    const uint32_t tcode = morton3((uint32_t)nx, (uint32_t)ny, (uint32_t)nz);
+    const uint32_t tb = S.cell_start[tcode << (3 * tsh)];
+    const uint32_t te = S.cell_start[(tcode + 1u) << (3 * tsh)];
+    const float rho = (float)max(te - tb, 8u) / (tside * tside * tside);
     const float r = 1.35f * cbrtf(3.f * (float)cap / (4.f * 3.14159265f * rho));
-    const float lift = (float)aux[2] * 1.0001f;  // largest squared lift difference
-    t0 = (r * g.h_f) * (r * g.h_f) + lift;
+    t0 = (r * g.h_f) * (r * g.h_f) + (float)aux[2] * 1.0001f;
   }
   thr = t0;
+  float wthr = t0;
+  const float h2f = g.h_f * g.h_f;
+  uint2* mybuf = s_buf + lane;  // entry j at mybuf[32 * j]
+  uint32_t bn = 0;
 
-  // candidates below the lane's pruning distance wait in a register queue;
-  // when one lane's queue is full every lane empties its own into its heap,
-  // so heap updates run together instead of one lane at a time
-  constexpr int kQ = 4;
-  float qd[kQ];
-  uint32_t qs[kQ];
-  int qn = 0;
-  auto flush = [&]() {
+  // Offers the seeds of up to 32 nodes (one per lane: first slot b, count
+  // n) to every query, 32 at a time.
+  auto gather = [&](uint32_t b, uint32_t n) {
+    uint32_t incl = n;
 #pragma unroll
-    for (int k = 0; k < kQ; ++k)
-      if (k < qn && qd[k] < thr) offer(qs[k], qd[k]);
-    qn = 0;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(FULL, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const uint32_t total = __shfl_sync(FULL, incl, 31);
+    const uint32_t excl = incl - n;
+    for (uint32_t base = 0; base < total; base += 32) {
+      const uint32_t i = base + lane;
+      // the last lane whose range starts at or before i owns it
+      int own = 0;
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1) {
+        const uint32_t e = __shfl_sync(FULL, excl, own + step);
+        if (e <= i) own += step;
+      }
+      const uint32_t ob = __shfl_sync(FULL, b, own);
+      const uint32_t oe = __shfl_sync(FULL, excl, own);
+      __syncwarp();
+      if (i < total) {
+        const uint32_t s2 = ob + (i - oe);
+        s_pt[lane] = S.xf[s2];
+        s_sl[lane] = s2;
+      }
+      __syncwarp();
+      const uint32_t m = min(32u, total - base);
+      for (uint32_t t = 0; t < m; ++t) {
+        const float4 p = s_pt[t];
+        const float dx = p.x - c.qf.x, dy = p.y - c.qf.y, dz = p.z - c.qf.z,
+                    dh = p.w - c.qf.w;
+        const float d32 = dx * dx + dy * dy + dz * dz + dh * dh;
+        if (active && d32 < thr) {
+          mybuf[32 * bn] = make_uint2(__float_as_uint(d32), s_sl[t]);
+          ++bn;
+        }
+      }
+      // every lane empties its buffer into its heap
+      for (uint32_t j = 0; j < bn; ++j) {
+        const uint2 v = mybuf[32 * j];
+        const float d32 = __uint_as_float(v.x);
+        if (d32 < thr) offer(v.y, d32);
+      }
+      bn = 0;
+    }
+    wthr = active ? thr : 0.f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) wthr = fmaxf(wthr, __shfl_xor_sync(FULL, wthr, o));
   };
 
-  // ---- the traversal, the same for the whole warp
-  const float h2f = g.h_f * g.h_f;
-  float wthr = t0;  // largest pruning distance of the active lanes
-  uint32_t stack[8 * 10 + 8];
-  int sp = 0;
-  stack[sp++] = 0u;  // (code << 4) | level
-  while (sp > 0) {
-    const uint32_t e = stack[--sp];
-    const int lev = (int)(e & 15u);
-    const uint32_t code = e >> 4;
-    const int shift = g.L - lev;
-    const float side = (float)(1u << shift);
-    if (wthr < FLT_MAX) {
-      const float bd = box_box_d2(compact3(code), compact3(code >> 1), compact3(code >> 2), side,
-                                  lo, hi) * h2f;
-      if (bd > wthr) continue;
+  // squared distance (world units) from the query box to node (x, y, z)
+  auto node_d2 = [&](int x, int y, int z) {
+    return box_box_d2((uint32_t)x, (uint32_t)y, (uint32_t)z, tside, lo, hi) * h2f;
+  };
+  auto node_range = [&](int x, int y, int z, uint32_t& b, uint32_t& n) {
+    const uint32_t code = morton3((uint32_t)x, (uint32_t)y, (uint32_t)z);
+    b = S.cell_start[code << (3 * tsh)];
+    n = S.cell_start[(code + 1u) << (3 * tsh)] - b;
+  };
+
+  // ---- the 27 nodes around the tile
+  {
+    uint32_t b = 0, n = 0;
+    if (lane < 27) {
+      const int x = nx + lane % 3 - 1, y = ny + (lane / 3) % 3 - 1, z = nz + lane / 9 - 1;
+      if (x >= 0 && y >= 0 && z >= 0 && x < NG && y < NG && z < NG) node_range(x, y, z, b, n);
     }
-    const uint32_t b = S.cell_start[code << (3 * shift)];
-    const uint32_t en = S.cell_start[(code + 1u) << (3 * shift)];
-    if (b == en) continue;
-    if (en - b <= kLeaf || lev == g.L) {
-      for (uint32_t base = b; base < en; base += 32) {
-        const uint32_t m = min(32u, en - base);
-        __syncwarp();
-        if ((uint32_t)lane < m) s_leaf[lane] = S.xf[base + lane];
-        __syncwarp();
-        for (uint32_t t = 0; t < m; ++t) {
-          const float4 p = s_leaf[t];
-          const float dx = p.x - c.qf.x, dy = p.y - c.qf.y, dz = p.z - c.qf.z,
-                      dh = p.w - c.qf.w;
-          const float d32 = dx * dx + dy * dy + dz * dz + dh * dh;
-          const bool take = active && d32 < thr;
-#pragma unroll
-          for (int k = kQ - 1; k > 0; --k) {
-            qd[k] = take ? qd[k - 1] : qd[k];
-            qs[k] = take ? qs[k - 1] : qs[k];
-          }
-          qd[0] = take ? d32 : qd[0];
-          qs[0] = take ? base + t : qs[0];
-          qn += take ? 1 : 0;
-          if (__any_sync(0xFFFFFFFFu, qn == kQ)) flush();
-        }
+    gather(b, n);
+  }
+  // ---- the nodes beyond them that the pruning distance still reaches
+  {
+    // reach in fine cells, with a margin for the FP32 arithmetic
+    const float rr = (wthr < FLT_MAX) ? sqrtf(wthr) / g.h_f * 1.001f + 0.01f : 2.f * (float)G;
+    const int x0 = max(0, (int)floorf((lo[0] - rr) / tside)), x1 = min(NG - 1, (int)floorf((hi[0] + rr) / tside));
+    const int y0 = max(0, (int)floorf((lo[1] - rr) / tside)), y1 = min(NG - 1, (int)floorf((hi[1] + rr) / tside));
+    const int z0 = max(0, (int)floorf((lo[2] - rr) / tside)), z1 = min(NG - 1, (int)floorf((hi[2] + rr) / tside));
+    const int sx = x1 - x0 + 1, sy = y1 - y0 + 1, sz = z1 - z0 + 1;
+    const int total = (x1 >= x0 && y1 >= y0 && z1 >= z0) ? sx * sy * sz : 0;
+    for (int base = 0; base < total; base += 32) {
+      uint32_t b = 0, n = 0;
+      const int idx = base + lane;
+      if (idx < total) {
+        const int x = x0 + idx % sx, y = y0 + (idx / sx) % sy, z = z0 + idx / (sx * sy);
+        const bool inner = abs(x - nx) <= 1 && abs(y - ny) <= 1 && abs(z - nz) <= 1;
+        if (!inner && !(wthr < FLT_MAX && node_d2(x, y, z) > wthr)) node_range(x, y, z, b, n);
       }
-      flush();
-      wthr = active ? thr : 0.f;
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1)
-        wthr = fmaxf(wthr, __shfl_xor_sync(0xFFFFFFFFu, wthr, o));
-      continue;
+      gather(b, n);
     }
-    const float cside = side * 0.5f;
-    float cd[8];
-    uint32_t cc[8];
-#pragma unroll
-    for (int ch = 0; ch < 8; ++ch) {
-      const uint32_t cw = (code << 3) | (uint32_t)ch;
-      cd[ch] = box_box_d2(compact3(cw), compact3(cw >> 1), compact3(cw >> 2), cside, lo, hi) *
-               h2f;
-      cc[ch] = cw;
-    }
-#pragma unroll
-    for (int i = 1; i < 8; ++i) {
-#pragma unroll
-      for (int j = i; j > 0; --j) {
-        if (cd[j] > cd[j - 1]) {
-          const float td = cd[j];
-          cd[j] = cd[j - 1];
-          cd[j - 1] = td;
-          const uint32_t tc = cc[j];
-          cc[j] = cc[j - 1];
-          cc[j - 1] = tc;
-        }
-      }
-    }
-#pragma unroll
-    for (int ch = 0; ch < 8; ++ch)
-      if (cd[ch] <= wthr) stack[sp++] = (cc[ch] << 4) | (uint32_t)(lev + 1);
   }
   if (!active) return;
 
@@ -1249,15 +1308,26 @@ knn_warp_kernel(KnnArgs a, SortedSeeds S, const GridDesc* __restrict__ gdp,
 
 void launch_knn(const KnnArgs& a, cudaStream_t st) {
   if (a.nq == 0) return;
-  if (a.k <= kKnnMaxK && a.flag_count && a.coherent) {
-    // warp-synchronous search, then the exact search of the queries whose
-    // FP32 screening could not settle the list
-    const size_t sh = knn_warp_smem(a.k);
-    cudaFuncSetAttribute(knn_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh);
+  if (a.k <= kKnnMaxK && a.flag_count && a.coherent && a.tile_scratch && !a.qlist &&
+      a.nq == a.S->n) {
+    // tiles of the octree, the tiled search, then the exact search of the
+    // queries whose FP32 screening could not settle the list
+    const int L = a.S->L;
+    const uint32_t nf = 1u << (3 * L);
+    uint32_t* off = a.tile_scratch;                       // nf + 1
+    uint32_t* tmp = off + nf + 1;                         // scan scratch
+    size_t items_at = (size_t)nf + 1 + scan_tmp_elems((size_t)nf + 1);
+    items_at += items_at & 1;  // 8-byte aligned
+    uint2* items = reinterpret_cast<uint2*>(a.tile_scratch + items_at);
+    tile_count_kernel<<<(nf + 256) / 256, 256, 0, st>>>(a.S->cell_start, L, nf, off); count_launch();
+    exclusive_scan_u32(off, (size_t)nf + 1, tmp, st);
+    tile_fill_kernel<<<(nf + 255) / 256, 256, 0, st>>>(a.S->cell_start, L, nf, off, items); count_launch();
+    const size_t sh = knn_tile_smem(a.k);
+    cudaFuncSetAttribute(knn_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh);
     cudaMemsetAsync(a.flag_count, 0, sizeof(uint32_t), st);
-    const unsigned nw = (a.nq + 31) / 32;
-    const unsigned nb = (nw + kWarpKnnWarps - 1) / kWarpKnnWarps;
-    knn_warp_kernel<<<nb, 32 * kWarpKnnWarps, sh, st>>>(a, *a.S, a.S->gd, a.S->aux); count_launch();
+    // tiles <= fine cells + queries / 32
+    const unsigned grid = nf + (a.nq + 31) / 32;
+    knn_tile_kernel<<<grid, 32, sh, st>>>(a, *a.S, a.S->gd, a.S->aux, off + nf, items); count_launch();
     launch_knn_exact(a, a.flag_list, a.flag_count, st);
     return;
   }

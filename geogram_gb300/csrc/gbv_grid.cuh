@@ -138,18 +138,21 @@ struct KnnArgs {
   uint32_t* gl_slot;
   uint32_t* flag_count;
   uint32_t* flag_list;
-  // queries close in space when consecutive (slots in sorted order): the
-  // warp-synchronous search may take them
+  // every stored point as a query, in slot order (qlist null, nq = n): the
+  // tiled search may take them, with tile_scratch of
+  // knn_tile_scratch_elems(n, L) entries
   bool coherent;
+  uint32_t* tile_scratch;
 };
 
-// Launches the kNN search.  Coherent queries, k <= kKnnMaxK: the
-// warp-synchronous FP32 screening with an exact FP64 re-rank, then the exact
-// search for the queries it could not settle (needs flag_count /
+// Launches the kNN search.  Every stored point in slot order, k <=
+// kKnnMaxK: the tiled FP32 screening with an exact FP64 re-rank, then the
+// exact search for the queries it could not settle (needs flag_count /
 // flag_list).  Other queries, k <= kKnnSmemK: the same per thread.  Larger
 // k: the exact search with global lists gl_d2 / gl_slot (k > kKnnMaxK).
 constexpr uint32_t kKnnSmemK = 64;
 constexpr uint32_t kKnnMaxK = 128;
+size_t knn_tile_scratch_elems(uint32_t n, int L);
 void launch_knn(const KnnArgs& a, cudaStream_t st);
 
 }  // namespace gbv

@@ -163,7 +163,6 @@ extern "C" gbv_status gbv_knn_noalloc(const double* d_pts, uint32_t n, uint32_t 
   // launch_knn clears the flag count before the search
   ka.flag_count = reinterpret_cast<uint32_t*>(base + Lay::flag_count);
   ka.flag_list = reinterpret_cast<uint32_t*>(base + Lay::flag_list);
-  ka.coherent = true;
   launch_knn(ka, st);
   e = cudaGetLastError();
   if (e != cudaSuccess) return fail(GBV_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e));
