@@ -45,7 +45,7 @@ __all__ = [
     "PRECISION_FP64", "PRECISION_FP32_RECHECK", "cell_options", "CERTIFY_SECURITY_RADIUS",
     "CERTIFY_POWER_RANGE", "ot_options", "ot_solve", "ot_solve_device", "ot_gradient_hessian",
     "ot_solve_levels", "ot_solve_levels_device", "ot_separable_start_device", "CellMesh",
-    "cells_mesh", "restricted_cells",
+    "cells_mesh", "restricted_cells", "periodic_cells",
 ]
 
 
@@ -321,6 +321,35 @@ def cells_mesh(cells=None, ctx: Context | None = None) -> CellMesh:
                                 _lib.ptr(out.vertices), _lib.ptr(out.cell_vertex_ptr),
                                 _lib.ptr(out.cell_face_ptr), _lib.ptr(out.face_ptr),
                                 _lib.ptr(out.face_vertices), _lib.ptr(out.face_seed)))
+    return out
+
+
+def periodic_cells(xyz: np.ndarray, weights: np.ndarray | None = None, *, period: float = 1.0,
+                   k0: int = 20, precision="fp64", ctx: Context | None = None) -> dict:
+    """Laguerre cells in the periodic cube [0, period)^3 (the reference's
+    PeriodicDelaunay3d + copy_Laguerre_cell_from_Delaunay,
+    delaunay/periodic_delaunay_3d.cpp:3634-3734): volume, mg, and per
+    facet the seed across it, its image translation code shift =
+    (tx+1)*9 + (ty+1)*3 + (tz+1) (13: none) and the facet area (CSR)."""
+    ctx = ctx or default_context()
+    x = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+    n = len(x)
+    w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float64).reshape(n)
+    o = cell_options(k0=k0, precision=precision)
+    rep = CellReport()
+    L = ctx._lib
+    _lib.check(L.gbv_periodic_cells(ctx.handle, _lib.ptr(x), _lib.ptr(w), n, float(period),
+                                    ctypes.byref(o), ctypes.byref(rep)))
+    k = max(rep.nnz, 1)
+    out = dict(volume=np.empty(n), mg=np.empty((n, 3)), rowptr=np.empty(n + 1, np.uint32),
+               neighbors=np.empty(k, np.uint32), shift=np.empty(k, np.uint8),
+               facet_area=np.empty(k))
+    _lib.check(L.gbv_periodic_fetch(ctx.handle, _lib.ptr(out["volume"]), _lib.ptr(out["mg"]),
+                                    _lib.ptr(out["rowptr"]), _lib.ptr(out["neighbors"]),
+                                    _lib.ptr(out["shift"]), _lib.ptr(out["facet_area"])))
+    for key in ("neighbors", "shift", "facet_area"):
+        out[key] = out[key][:rep.nnz]
+    out["report"] = rep.as_dict()
     return out
 
 

@@ -174,6 +174,9 @@ SIGNATURES = {
     "gbv_ot_separable_start": (ctypes.c_int, [_P, _P, _U32, ctypes.POINTER(OtOptions), _P, _P]),
     "gbv_mlp_gemm_nt": (ctypes.c_int, [_P, _P, ctypes.c_int, _P, ctypes.c_int, _P, ctypes.c_int,
                                        ctypes.c_int, ctypes.c_int, ctypes.c_int, _P]),
+    "gbv_periodic_cells": (ctypes.c_int, [_P, _P, _P, _U32, ctypes.c_double,
+                                          ctypes.POINTER(CellOptions), ctypes.POINTER(CellReport)]),
+    "gbv_periodic_fetch": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P]),
     "gbv_restricted_cells": (ctypes.c_int, [_P, _P, _U32, _P, _U32, _P, _P, _U32,
                                             ctypes.POINTER(CellOptions), _P, _P,
                                             ctypes.POINTER(ctypes.c_double), _P,

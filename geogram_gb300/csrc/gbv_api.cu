@@ -799,6 +799,7 @@ static void cells_device(gbv_context* c, const double* d_xyz, const double* d_w,
   if (n == 0) throw StatusError{GBV_ERR_INVALID_ARGUMENT, "n must be > 0"};
   setup_seeds(c, n, d_w != nullptr);
   c->nn_ready = false;
+  c->has_periodic = false;
   SortedSeeds& S = c->S;
   GBV_CUDA(cudaEventRecord(c->ev[0], st));
   build_grid(d_xyz, 3, 3, d_w, n, S.L, S, c->scr, st);
@@ -1889,6 +1890,85 @@ gbv_status gbv_cells_compute(gbv_context* c, const double* xyz, const double* w,
                       report);
     else
       cells_device(c, dx, dw, n, *opt, c->stream, report);
+  });
+}
+
+gbv_status gbv_periodic_cells(gbv_context* c, const double* xyz, const double* w, uint32_t n,
+                              double period, const gbv_cell_options* opt,
+                              gbv_cell_report* report) {
+  if (!c || !xyz) return fail(GBV_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (n < 2) return fail(GBV_ERR_INVALID_ARGUMENT, "n must be >= 2");
+  if (!(period > 0.0)) return fail(GBV_ERR_INVALID_ARGUMENT, "period must be > 0");
+  gbv_status s = check_opts(opt);
+  if (s != GBV_OK) return s;
+  if (opt->certification != GBV_CERTIFY_SECURITY_RADIUS || !opt->check_sr)
+    return fail(GBV_ERR_INVALID_ARGUMENT, "periodic cells use the security-radius loop");
+  for (uint32_t i = 0; i < 3 * n; ++i)
+    if (!(xyz[i] >= 0.0 && xyz[i] < period))
+      return fail(GBV_ERR_INVALID_ARGUMENT, "seeds must lie in [0, period)^3");
+  return guarded([&] {
+    GBV_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = c->stream;
+    c->has_periodic = false;
+    double W = 0.0, wmin = 0.0;
+    if (w) {
+      W = wmin = w[0];
+      for (uint32_t i = 1; i < n; ++i) {
+        W = std::max(W, w[i]);
+        wmin = std::min(wmin, w[i]);
+      }
+    }
+    double* dx = c->buf<double>("per_in_xyz", 3 * (size_t)n);
+    double* dw = w ? c->buf<double>("per_in_w", n) : nullptr;
+    GBV_CUDA(cudaMemcpyAsync(dx, xyz, 24 * (size_t)n, cudaMemcpyHostToDevice, st));
+    if (w) GBV_CUDA(cudaMemcpyAsync(dw, w, 8 * (size_t)n, cudaMemcpyHostToDevice, st));
+    // a first layer of about four seed spacings plus the lift range; widened
+    // (doubling) while some cell's security ball leaves the ghost box
+    double delta = std::min(period, 4.0 * period * std::cbrt(1.0 / n) + 2.0 * std::sqrt(W - wmin));
+    for (int round = 0;; ++round) {
+      double *ax = nullptr, *aw = nullptr;
+      const uint32_t na = periodic_ghosts(c, dx, dw, n, period, delta, st, &ax, &aw);
+      gbv_cell_options o = *opt;
+      for (int k = 0; k < 3; ++k) {
+        o.box_min[k] = -delta;
+        o.box_max[k] = period + delta;
+      }
+      cells_device(c, ax, aw, na, o, st, report);
+      const uint32_t fails = periodic_reach_failures(c, n, ax, aw, W, period, delta, st);
+      if (fails == 0) break;
+      if (delta >= period || round >= 8)
+        throw StatusError{GBV_ERR_NOT_CONVERGED,
+                          std::to_string(fails) + " periodic cell(s) reach beyond one period"};
+      delta = std::min(period, 2.0 * delta);
+    }
+    uint32_t nnz = 0;
+    periodic_remap(c, n, st, &c->per_nbr, &c->per_shift, &nnz);
+    GBV_CUDA(cudaStreamSynchronize(st));
+    c->per_n = n;
+    c->per_nnz = nnz;
+    c->has_periodic = true;
+    if (report) {
+      report->n_cells = n;
+      report->nnz = nnz;
+    }
+  });
+}
+
+gbv_status gbv_periodic_fetch(gbv_context* c, double* vol, double* mg, uint32_t* rowptr,
+                              uint32_t* nbr, uint8_t* shift, double* area) {
+  if (!c) return fail(GBV_ERR_INVALID_ARGUMENT, "NULL context");
+  if (!c->has_periodic || !c->has_cells) return fail(GBV_ERR_STATE, "no periodic cells computed");
+  return guarded([&] {
+    GBV_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = c->stream;
+    const size_t n = c->per_n, nnz = c->per_nnz;
+    if (vol) GBV_CUDA(cudaMemcpyAsync(vol, c->vol, 8 * n, cudaMemcpyDeviceToHost, st));
+    if (mg) GBV_CUDA(cudaMemcpyAsync(mg, c->mg, 24 * n, cudaMemcpyDeviceToHost, st));
+    if (rowptr) GBV_CUDA(cudaMemcpyAsync(rowptr, c->rowptr, 4 * (n + 1), cudaMemcpyDeviceToHost, st));
+    if (nbr && nnz) GBV_CUDA(cudaMemcpyAsync(nbr, c->per_nbr, 4 * nnz, cudaMemcpyDeviceToHost, st));
+    if (shift && nnz) GBV_CUDA(cudaMemcpyAsync(shift, c->per_shift, nnz, cudaMemcpyDeviceToHost, st));
+    if (area && nnz) GBV_CUDA(cudaMemcpyAsync(area, c->area, 8 * nnz, cudaMemcpyDeviceToHost, st));
+    GBV_CUDA(cudaStreamSynchronize(st));
   });
 }
 

@@ -55,6 +55,12 @@ struct gbv_context {
   double* area = nullptr;
   int32_t* status = nullptr;
   double box[6] = {0.0, 0.0, 0.0, 1.0, 1.0, 1.0};  // the clipping box of the last cells
+  // last periodic cells: the first per_n cells above are the original
+  // seeds; their facets' seeds and image translations
+  bool has_periodic = false;
+  uint32_t per_n = 0, per_nnz = 0;
+  uint32_t* per_nbr = nullptr;
+  uint8_t* per_shift = nullptr;
 
   // nearest-neighbour search state
   bool nn_ready = false;
@@ -86,4 +92,19 @@ namespace gbv {
 void restricted_cells(gbv_context* c, const double* d_xyz, const double* d_w, uint32_t n,
                       const double* d_mv, uint32_t nv, const uint32_t* d_tets, uint32_t nt,
                       cudaStream_t st, double* d_m, double* d_mg, double* d_F, double* d_g);
+}  // namespace gbv
+
+namespace gbv {
+// Periodic cells (gbv_periodic.cu): the seeds and their ghost images in
+// the layer of width delta (returns the augmented count), the original
+// cells whose security ball leaves the ghost box, and the originals'
+// facets as (seed, translation code).
+uint32_t periodic_ghosts(gbv_context* c, const double* d_xyz, const double* d_w, uint32_t n,
+                         double P, double delta, cudaStream_t st, double** aug_xyz,
+                         double** aug_w);
+uint32_t periodic_reach_failures(gbv_context* c, uint32_t n, const double* aug_xyz,
+                                 const double* aug_w, double W, double P, double delta,
+                                 cudaStream_t st);
+void periodic_remap(gbv_context* c, uint32_t n, cudaStream_t st, uint32_t** out_nbr,
+                    uint8_t** out_shift, uint32_t* nnz);
 }  // namespace gbv

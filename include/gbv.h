@@ -380,6 +380,31 @@ gbv_status gbv_mlp_gemm_nt(gbv_context* ctx, const void* d_a, int lda, const voi
                            int ldb, float* d_c, int ldc, int M, int N, int K, void* stream);
 
 /* ---------------------------------------------------------------- */
+/* Periodic cells                                                    */
+/* ---------------------------------------------------------------- */
+
+/* Replaces PeriodicDelaunay3d(periodic = true, period) with
+ * copy_Laguerre_cell_from_Delaunay (delaunay/periodic_delaunay_3d.h:126-156,
+ * periodic_delaunay_3d.cpp:3634-3734): the Laguerre cells of the seeds
+ * xyz[3 n] (in [0, period)^3; weights w[n] or NULL) in the periodic cube.
+ * opt gives k0 and precision (security-radius certification; its box is
+ * ignored).  The cells are computed here and kept in the context; read
+ * them with gbv_periodic_fetch (report->nnz facets). */
+gbv_status gbv_periodic_cells(gbv_context* ctx, const double* xyz, const double* w, uint32_t n,
+                              double period, const gbv_cell_options* opt,
+                              gbv_cell_report* report);
+
+/* The last periodic cells, host arrays (any may be NULL): vol[n], mg[3 n]
+ * (about the seed's own position, which may lie outside the cube for a
+ * cell that wraps), rowptr[n + 1], and per facet the seed across it
+ * (nbr, an index < n), the translation of that seed's image as
+ * shift = (tx + 1) * 9 + (ty + 1) * 3 + (tz + 1) with t in {-1, 0, 1}
+ * periods (13: no translation; the reference's instance, translated by
+ * Periodic::translation), and the facet area. */
+gbv_status gbv_periodic_fetch(gbv_context* ctx, double* vol, double* mg, uint32_t* rowptr,
+                              uint32_t* nbr, uint8_t* shift, double* area);
+
+/* ---------------------------------------------------------------- */
 /* Cells restricted to a tetrahedral mesh                            */
 /* ---------------------------------------------------------------- */
 

@@ -87,6 +87,7 @@ def ref():
         lib.ref_cells_save.restype = ctypes.c_long
         lib.ref_rvd_volume.argtypes = [P, U, P, U, P, U, P, P, P, P]
         lib.ref_set_walk.argtypes = [ctypes.c_int]
+        lib.ref_periodic_cells.argtypes = [P, P, U, ctypes.c_double, P, P, P, P, P, P, U]
         lib.ref_init()
         _ref = lib
     return _ref
@@ -244,6 +245,30 @@ def ref_rvd_volume(mesh_xyz: np.ndarray, tets: np.ndarray, seeds: np.ndarray) ->
         raise RuntimeError("ref_rvd_volume failed")
     out["f"] = f.value
     return out
+
+
+def ref_periodic_cells(xyz: np.ndarray, w: np.ndarray | None = None, period: float = 1.0,
+                       max_nbr: int = 96) -> dict:
+    """Laguerre cells in the periodic cube by the reference's
+    PeriodicDelaunay3d (reference build only): vol, mg and per-cell facets
+    (real index, image translation code, area) as CSR."""
+    x = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+    n = len(x)
+    wa = None if w is None else np.ascontiguousarray(w, dtype=np.float64)
+    out = dict(vol=np.zeros(n), mg=np.zeros((n, 3)), cnt=np.zeros(n, np.uint32),
+               nidx=np.zeros((n, max_nbr), np.uint32), nsh=np.zeros((n, max_nbr), np.uint8),
+               narea=np.zeros((n, max_nbr)))
+    r = ref().ref_periodic_cells(_p(x), _p(wa), n, period, _p(out["vol"]), _p(out["mg"]),
+                                 _p(out["cnt"]), _p(out["nidx"]), _p(out["nsh"]),
+                                 _p(out["narea"]), max_nbr)
+    if r != 0 or (out["cnt"] > max_nbr).any():
+        raise RuntimeError("ref_periodic_cells failed")
+    cnt = out["cnt"].astype(np.int64)
+    rowptr = np.zeros(n + 1, np.int64)
+    rowptr[1:] = np.cumsum(cnt)
+    mask = np.arange(max_nbr)[None, :] < cnt[:, None]
+    return dict(vol=out["vol"], mg=out["mg"], rowptr=rowptr, nbr=out["nidx"][mask],
+                shift=out["nsh"][mask], area=out["narea"][mask])
 
 
 def det4_sign(p0, p1, p2, p3) -> int:

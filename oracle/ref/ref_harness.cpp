@@ -39,6 +39,7 @@
 #include <geogram/voronoi/convex_cell.h>
 #include <geogram/voronoi/RVD.h>
 #include <geogram/delaunay/delaunay.h>
+#include <geogram/delaunay/periodic_delaunay_3d.h>
 #include <geogram/mesh/mesh.h>
 
 #include <algorithm>
@@ -367,6 +368,57 @@ int ref_rvd_volume(const double* verts, unsigned nv, const unsigned* tets, unsig
     double fv = 0.0;
     rvd->compute_CVT_func_grad(fv, g);
     *f = fv;
+    return 0;
+}
+
+/*
+ * Laguerre cells of the seeds in the periodic cube [0, period)^3, by the
+ * reference's PeriodicDelaunay3d (delaunay/periodic_delaunay_3d.cpp:
+ * compute, copy_Laguerre_cell_from_Delaunay :3634-3734) and ConvexCell
+ * geometry.  Per seed i: vol[i], mg[3i..], and its facets (at most max_nbr):
+ * the real index of the seed across the facet, the translation of that
+ * image as the code (tx+1)*9 + (ty+1)*3 + (tz+1) (13: none), the facet's
+ * area.  xyz must lie in [0, period).
+ */
+int ref_periodic_cells(const double* xyz, const double* w, unsigned n, double period,
+                       double* vol, double* mg, unsigned* nbr_count, unsigned* nbr_idx,
+                       unsigned char* nbr_shift, double* nbr_area, unsigned max_nbr) {
+    ensure_init();
+    if (n < 2) return 1;
+    // reference-counted: heap-allocated and held by a SmartPointer
+    GEO::SmartPointer<GEO::PeriodicDelaunay3d> dp = new GEO::PeriodicDelaunay3d(true, period);
+    GEO::PeriodicDelaunay3d& del = *dp;
+    del.set_vertices(n, xyz);
+    if (w != nullptr) del.set_weights(w);
+    del.compute();
+    VBW::ConvexCell C(VBW::WithVGlobal);
+    for (unsigned i = 0; i < n; ++i) {
+        del.copy_Laguerre_cell_from_Delaunay(i, C);
+        C.compute_geometry();
+        double m = 0.0;
+        VBW::vec3 g = VBW::make_vec3(0.0, 0.0, 0.0);
+        C.compute_mg(m, g);
+        vol[i] = m;
+        mg[3 * i] = g.x;
+        mg[3 * i + 1] = g.y;
+        mg[3 * i + 2] = g.z;
+        unsigned cnt = 0;
+        for (VBW::index_t v = 1; v < C.nb_v(); ++v) {
+            if (!C.vertex_is_contributing(v)) continue;
+            const VBW::global_index_t j = C.v_global_index(v);
+            if (j == VBW::global_index_t(-1)) continue;
+            if (cnt < max_nbr) {
+                const unsigned inst = unsigned(j) / n;
+                const int* T = GEO::Periodic::translation[inst];
+                nbr_idx[size_t(i) * max_nbr + cnt] = unsigned(j) % n;
+                nbr_shift[size_t(i) * max_nbr + cnt] =
+                    (unsigned char)((T[0] + 1) * 9 + (T[1] + 1) * 3 + (T[2] + 1));
+                nbr_area[size_t(i) * max_nbr + cnt] = C.facet_area(v);
+            }
+            ++cnt;
+        }
+        nbr_count[i] = cnt;
+    }
     return 0;
 }
 

@@ -158,6 +158,19 @@ def main(only=None):
                                 status=r["status"], n_clip=r["n_clip"], k_list=r["k_list"],
                                 exact=np.array(exact), walk=np.array(walk))
             print(name, "exact" if exact else "fast", "walk" if walk else "scan")
+    if not only or "periodic" in only:
+        # Laguerre cells in the periodic unit cube by the reference's
+        # PeriodicDelaunay3d (weights at 0.2 x the squared spacing: the
+        # reference crashes once cells become empty)
+        x = np.random.default_rng(8).random((1000, 3))
+        for name, w in (("periodic_1000", None),
+                        ("periodic_power_1000",
+                         np.random.default_rng(9).random(1000) * 0.2 * (1 / 1000) ** (2 / 3))):
+            r = oracle.ref_periodic_cells(x, w)
+            np.savez_compressed(os.path.join(HERE, f"{name}.npz"), x=x,
+                                w=np.zeros(0) if w is None else w, vol=r["vol"], mg=r["mg"],
+                                rowptr=r["rowptr"], nbr=r["nbr"], shift=r["shift"], area=r["area"])
+            print(name, "facets", len(r["nbr"]), "volume", r["vol"].sum())
     if not only or "obj" in only:
         # ConvexCell::save text of some cells (interior, at the box, of
         # weighted seeds), plain and shrunk

@@ -136,3 +136,18 @@ def test_fast_and_walk_variants_pinned(oracle_mod, name, src):
     r = oracle_mod.cells(f["x"], f["w"], exact=bool(f["exact"]), nthreads=4)
     assert np.array_equal(r["vol"], f["vol"]) and np.array_equal(r["nbr"], f["nbr"])
     assert np.array_equal(r["area"], f["area"])
+
+
+@pytest.mark.parametrize("name", ["periodic_1000", "periodic_power_1000"])
+def test_periodic_fixtures_consistent(name):
+    """The reference's periodic cells tile the unit torus, and each facet is
+    seen from its other side with the opposite image translation."""
+    d = load_golden(f"{name}.npz")
+    n = len(d["x"])
+    assert abs(d["vol"].sum() - 1.0) < 1e-12
+    rp = d["rowptr"].astype(np.int64)
+    row = np.repeat(np.arange(n), np.diff(rp))
+    sh = d["shift"].astype(np.int64)
+    fwd = (row * n + d["nbr"]) * 27 + sh
+    back = (d["nbr"].astype(np.int64) * n + row) * 27 + (26 - sh)
+    assert np.array_equal(np.sort(fwd), np.sort(back))
