@@ -109,7 +109,10 @@ class CellReport(ctypes.Structure):
         ("ms_retry", ctypes.c_double),
         ("ms_total", ctypes.c_double),
         ("n_huge", ctypes.c_uint32),
-        ("reserved", ctypes.c_uint32),
+        ("n_knn_exact", ctypes.c_uint32),
+        ("n_conflict_tests", ctypes.c_uint64),
+        ("n_corners_created", ctypes.c_uint64),
+        ("ms_clip_kernel", ctypes.c_double),
     ]
 
     def as_dict(self) -> dict:

@@ -436,6 +436,7 @@ struct Pipeline {
       c->box[k] = box_min[k];
       c->box[3 + k] = box_max[k];
     }
+    c->h_counts[4] = 0;  // first-pass kNN exact fallbacks (cells_device sets it)
     status_s = c->buf<int32_t>("status_s", n);
     vol_s = c->buf<double>("vol_s", n);
     mg_s = c->buf<double>("mg_s", 3 * (size_t)n);
@@ -481,8 +482,10 @@ struct Pipeline {
     mr = c->buf<uint32_t>("cls_mr", n);
     mk_s = c->buf<uint32_t>("mk_s", n);
     mk_r = c->buf<uint32_t>("mk_r", n);
-    GBV_CUDA(cudaMemsetAsync(c->counters, 0, 2 * sizeof(unsigned long long), st));
+    GBV_CUDA(cudaMemsetAsync(c->counters, 0, 4 * sizeof(unsigned long long), st));
   }
+
+  bool timed_first = false;  // the first clipping pass has been timed
 
   // certification counters (GBV_CERT_STATS in the environment)
   unsigned long long* cert_stats = nullptr;
@@ -532,7 +535,8 @@ struct Pipeline {
   }
 
   // clip + geometry of a set of cells with the given lists
-  // (kind 0: the pipeline's precision, 1: FP64 small, 2: FP64 large)
+  // (kind 0: the pipeline's precision, 1: FP64 small, 2: FP64 large,
+  // 3: FP32 large, 4: FP32 small with exact signs where FP32 cannot decide)
   void run(const ListSet& L, const uint32_t* ql, const uint32_t* qr, uint32_t nq, int kind) {
     ClipArgs a = cbase;
     a.nbr = L.lists;
@@ -542,9 +546,19 @@ struct Pipeline {
     a.qlist = ql;
     a.qrow = qr;
     a.nq = nq;
-    const bool f32 = kind == 0 && fp32;
-    if (f32) launch_clip_fp32(a, st);
-    else launch_clip_fp64(a, kind == 2 ? CLIP_LARGE : CLIP_SMALL, st);
+    const bool f32 = (kind == 0 && fp32) || kind == 3 || kind == 4;
+    const int shape = (kind == 2 || kind == 3) ? CLIP_LARGE : CLIP_SMALL;
+    // the first pass over every cell: its kernel time and counters alone
+    const bool first = kind == 0 && !timed_first;
+    if (first) GBV_CUDA(cudaEventRecord(c->ev[6], st));
+    if (f32) launch_clip_fp32(a, shape, kind != 0, st);
+    else launch_clip_fp64(a, shape, st);
+    if (first) {
+      timed_first = true;
+      GBV_CUDA(cudaEventRecord(c->ev[7], st));
+      GBV_CUDA(cudaMemcpyAsync(c->h_clipc, c->counters + 2, 2 * sizeof(unsigned long long),
+                               cudaMemcpyDeviceToHost, st));
+    }
     GBV_CUDA(last_launch_error);
     GeomArgs g = gbase;
     g.nbr = L.lists;
@@ -553,7 +567,7 @@ struct Pipeline {
     g.qrow = qr;
     g.nq = nq;
     g.verify_sr = (f32 && check_sr) ? 1 : 0;
-    g.shape = kind == 2 ? CLIP_LARGE : CLIP_SMALL;
+    g.shape = shape;
     if (node_wmax) {
       g.node_wmax = node_wmax;
       g.node_lin = node_lin;
@@ -671,8 +685,25 @@ struct Pipeline {
     append(ov_r, 0, orw, nov);
     append(mk_s, 0, ms, nmk);
     append(mk_r, 0, mr, nmk);
-    if (nrc) {
+    if (nrc && fp32) {
+      // FP32 again, undecided signs taken exactly; what is left (stops of
+      // the security radius FP32 could not certify) goes to FP64 below
       n_recheck += nrc;
+      run(L, rc_s, rc_r, nrc, 4);
+      uint32_t c6[4];
+      classify(rc_s, rc_r, nrc, c6);
+      append(ov_s, nov, os, c6[1]);
+      append(ov_r, nov, orw, c6[1]);
+      nov += c6[1];
+      append(mk_s, nmk, ms, c6[2]);
+      append(mk_r, nmk, mr, c6[2]);
+      nmk += c6[2];
+      append(rc_s, 0, rs, c6[0]);
+      append(rc_r, 0, rr, c6[0]);
+      nrc = c6[0];
+    }
+    if (nrc) {
+      if (!fp32) n_recheck += nrc;
       run(L, rc_s, rc_r, nrc, 1);
       uint32_t c2[4];
       classify(rc_s, rc_r, nrc, c2);
@@ -683,8 +714,30 @@ struct Pipeline {
       append(mk_r, nmk, mr, c2[2]);
       nmk += c2[2];
     }
-    if (nov) {
+    if (nov && fp32) {
+      // the large shape in FP32 first; its rechecks go to FP64 below
       n_over += nov;
+      run(L, ov_s, ov_r, nov, 3);
+      uint32_t c5[4];
+      classify(ov_s, ov_r, nov, c5);
+      uint32_t* lr_s = c->buf<uint32_t>("lr_s", n);
+      uint32_t* lr_r = c->buf<uint32_t>("lr_r", n);
+      append(lr_s, 0, rs, c5[0]);
+      append(lr_r, 0, rr, c5[0]);
+      append(mk_s, nmk, ms, c5[2]);
+      append(mk_r, nmk, mr, c5[2]);
+      nmk += c5[2];
+      // beyond the large shape, and the large cells FP32 could not certify:
+      // the FP64 large pass
+      append(ov_s, 0, os, c5[1]);
+      append(ov_r, 0, orw, c5[1]);
+      append(ov_s, c5[1], lr_s, c5[0]);
+      append(ov_r, c5[1], lr_r, c5[0]);
+      nov = c5[1] + c5[0];
+      n_recheck += c5[0];
+    }
+    if (nov) {
+      if (!fp32) n_over += nov;
       run(L, ov_s, ov_r, nov, 2);
       uint32_t c3[4];
       classify(ov_s, ov_r, nov, c3);
@@ -761,10 +814,10 @@ struct Pipeline {
     GBV_CUDA(cudaMemsetAsync(clips, 0, 8, st));
     sum_u32_kernel<<<256, 256, 0, st>>>(nclip, n, clips); count_launch();
     double vs = 0;
-    unsigned long long cs = 0, hc[2] = {0, 0};
+    unsigned long long cs = 0, hc[4] = {0, 0, 0, 0};
     GBV_CUDA(cudaMemcpyAsync(&vs, out, 8, cudaMemcpyDeviceToHost, st));
     GBV_CUDA(cudaMemcpyAsync(&cs, clips, 8, cudaMemcpyDeviceToHost, st));
-    GBV_CUDA(cudaMemcpyAsync(hc, c->counters, 16, cudaMemcpyDeviceToHost, st));
+    GBV_CUDA(cudaMemcpyAsync(hc, c->counters, 32, cudaMemcpyDeviceToHost, st));
     GBV_CUDA(cudaStreamSynchronize(st));
     rep->nnz = c->nnz;
     rep->n_cells = n;
@@ -782,7 +835,12 @@ struct Pipeline {
     rep->ms_retry = t_retry;
     rep->ms_total = t_total;
     rep->n_huge = n_huge;
-    rep->reserved = 0;
+    rep->n_knn_exact = c->h_counts[4];
+    rep->n_conflict_tests = timed_first ? c->h_clipc[0] : 0;
+    rep->n_corners_created = timed_first ? c->h_clipc[1] : 0;
+    float ms = 0.f;
+    if (timed_first) GBV_CUDA(cudaEventElapsedTime(&ms, c->ev[6], c->ev[7]));
+    rep->ms_clip_kernel = ms;
   }
 };
 
@@ -840,8 +898,15 @@ static void cells_device(gbv_context* c, const double* d_xyz, const double* d_w,
       ka.gl_d2 = c->buf<double>("knn_gd2", (size_t)K * n);
       ka.gl_slot = c->buf<uint32_t>("knn_gslot", (size_t)K * n);
     }
-    if (K > 0) launch_knn(ka, st);
-    else GBV_CUDA(cudaMemsetAsync(kcnt, 0, sizeof(uint32_t) * n, st));
+    c->h_counts[4] = 0;
+    if (K > 0) {
+      launch_knn(ka, st);
+      // read with the report (the pipeline synchronises before it)
+      GBV_CUDA(cudaMemcpyAsync(&c->h_counts[4], flag_count, sizeof(uint32_t),
+                               cudaMemcpyDeviceToHost, st));
+    } else {
+      GBV_CUDA(cudaMemsetAsync(kcnt, 0, sizeof(uint32_t) * n, st));
+    }
     GBV_CUDA(cudaGetLastError());
   }
   GBV_CUDA(cudaEventRecord(c->ev[2], st));
@@ -860,11 +925,13 @@ static void cells_device(gbv_context* c, const double* d_xyz, const double* d_w,
   while (morek > 0) {
     P.n_morek += morek;
     if (cur.k >= nm1) throw StatusError{GBV_ERR_STATE, "list growth did not terminate"};
-    // geometric growth: every round at least doubles the lists, so a cell
-    // that needs k neighbours (outer seeds of clustered inputs need
-    // thousands) takes O(log k) rounds and O(k) clips in all, instead of
-    // being re-clipped every 64 more
-    const uint32_t batch = std::min<uint32_t>(std::max<uint32_t>(kKnnSmemK, cur.k), nm1 - cur.k);
+    // Up to 256 neighbours the lists grow by 64 (the FP32-screened search,
+    // a cell needing fewer than 256 takes at most two extra rounds); beyond,
+    // every round doubles them, so a cell that needs k neighbours (outer
+    // seeds of clustered inputs need thousands) takes O(log k) rounds and
+    // O(k) clips in all
+    const uint32_t want = cur.k < 4 * kKnnSmemK ? kKnnSmemK : cur.k;
+    const uint32_t batch = std::min<uint32_t>(want, nm1 - cur.k);
     const uint32_t newk = cur.k + batch;
     const std::string tag = std::to_string(round & 1);
     uint32_t* q_s = c->buf<uint32_t>("ext_s" + tag, morek);
@@ -1831,9 +1898,10 @@ gbv_status gbv_create(int device, gbv_context** out) {
     GBV_CUDA(cudaSetDevice(device));
     GBV_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     for (auto& e : c->ev) GBV_CUDA(cudaEventCreate(&e));
-    c->counters = c->buf<unsigned long long>("counters", 2);
+    c->counters = c->buf<unsigned long long>("counters", 4);
     c->list_counts = c->buf<uint32_t>("list_counts", 4);
-    GBV_CUDA(cudaMallocHost(&c->h_counts, 4 * sizeof(uint32_t)));
+    GBV_CUDA(cudaMallocHost(&c->h_counts, 8 * sizeof(uint32_t)));
+    GBV_CUDA(cudaMallocHost(&c->h_clipc, 2 * sizeof(unsigned long long)));
   });
   if (st != GBV_OK) {
     gbv_destroy(c);  // releases whatever was created before the failure
@@ -1848,6 +1916,7 @@ gbv_status gbv_destroy(gbv_context* c) {
   cudaSetDevice(c->device);
   for (auto& kv : c->bufs) cudaFree(kv.second.first);
   if (c->h_counts) cudaFreeHost(c->h_counts);
+  if (c->h_clipc) cudaFreeHost(c->h_clipc);
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);
   if (c->stream) cudaStreamDestroy(c->stream);

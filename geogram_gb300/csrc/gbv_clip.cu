@@ -179,10 +179,26 @@ __device__ __forceinline__ float4 box_plane_fp32(int b, const SeedCtx& sc) {
   }
 }
 
+// The reference's conflict decision for the triangle of planes p0, p1, p2
+// and the clipping plane pj: det4 >= 0 exactly (PCK::det_4d), or the FP64
+// det4x4 > 0 with the fast predicates.  Out of line: the FP32 kernel needs
+// it only when its own bound cannot decide, and its expansion arithmetic
+// would otherwise weigh on the registers of the conflict loop.
+__device__ __noinline__ bool exact_conflict(double4 p0, double4 p1, double4 p2, double4 pj,
+                                            int fast) {
+  if (fast) return r_det4x4(p0, p1, p2, pj) > 0.0;
+  const double r0[4] = {p0.x, p0.y, p0.z, p0.w}, r1[4] = {p1.x, p1.y, p1.z, p1.w},
+               r2[4] = {p2.x, p2.y, p2.z, p2.w}, r3[4] = {pj.x, pj.y, pj.z, pj.w};
+  return det4_sign_exact(r0, r1, r2, r3) >= 0;
+}
+
 // ---------------------------------------------------------------------
 // The kernel
 // ---------------------------------------------------------------------
-template <typename Real, int T, int P>
+// XF (FP32 only): a sign the FP32 bound cannot decide is taken exactly from
+// the FP64 planes; without it the cell is marked for a recheck (a leaner
+// loop for the first pass over every cell).
+template <typename Real, int T, int P, bool XF>
 __global__ void __launch_bounds__(kClipThreads) clip_kernel(ClipArgs a) {
   constexpr int BS = kClipThreads;
   constexpr int NWT = (T + 63) / 64;
@@ -215,6 +231,21 @@ __global__ void __launch_bounds__(kClipThreads) clip_kernel(ClipArgs a) {
   auto plane_of = [&](uint32_t p) {
     if constexpr (kFP64) return plane_fp64(sm.pown[p][tid], sc.pi, sc.qi, sc.box, S);
     else return sm.pl[p][tid];
+  };
+  // The reference's FP64 plane of plane slot p (FP32 kernel: from its list
+  // position, box faces keep their slots 0-5) and of seed slot j.
+  auto plane64_of = [&](uint32_t j) -> double4 {
+    return plane_fp64(j, sc.pi, S.q[s], sc.box, S);
+  };
+  auto plane64 = [&](uint32_t p) -> double4 {
+    if constexpr (kFP64) {
+      return plane_fp64(sm.pown[p][tid], sc.pi, sc.qi, sc.box, S);
+    } else {
+      const uint16_t rk = sm.prank[p][tid];
+      const uint32_t own =
+          (rk == 0xFFFF) ? kBoxBase + p : a.nbr[(size_t)rk * a.nbr_stride + row];
+      return plane_fp64(own, sc.pi, S.q[s], sc.box, S);
+    }
   };
   // Creates the corner of triangle t from its planes; returns its r2.
   auto make_corner = [&](uint32_t t, const auto& pa, const auto& pb, const auto& pc) -> Real {
@@ -281,6 +312,7 @@ __global__ void __launch_bounds__(kClipThreads) clip_kernel(ClipArgs a) {
   int32_t st = -1;
   uint32_t jj = 0;
   unsigned long long n_exact = 0;
+  uint32_t n_tests = 0, n_created = 0;  // conflict tests, corners made (the flop model)
 
   if (dup) {
     st = CELL_DUPLICATE;
@@ -346,6 +378,7 @@ __global__ void __launch_bounds__(kClipThreads) clip_kernel(ClipArgs a) {
       int keep_max_eff = -0x7FFF;
       bool uncertain = false;
       auto test = [&](int t) {
+        ++n_tests;
         Real cx, cy, cz, r2, eps;
         if constexpr (kFP64) {
           const double2 xy = sm.cxy[t][tid], zr = sm.czr[t][tid];
@@ -383,6 +416,13 @@ __global__ void __launch_bounds__(kClipThreads) clip_kernel(ClipArgs a) {
                            rr2[4] = {p2.x, p2.y, p2.z, p2.w}, r3[4] = {Pd.x, Pd.y, Pd.z, Pd.w};
               in_conflict = det4_sign_exact(r0, r1, rr2, r3) >= 0;
             }
+            ++n_exact;
+          } else if constexpr (XF) {
+            // FP32 cannot decide: the exact sign of the reference's FP64
+            // planes decides, as in the FP64 kernel
+            const uint32_t v = sm.tv[t][tid];
+            in_conflict = exact_conflict(plane64(v & 0xFF), plane64(v >> 8 & 0xFF),
+                                         plane64(v >> 16 & 0xFF), plane64_of(j), a.fast_pred);
             ++n_exact;
           } else {
             uncertain = true;
@@ -529,6 +569,7 @@ __global__ void __launch_bounds__(kClipThreads) clip_kernel(ClipArgs a) {
         }
         prev_t = nt;
         ++created;
+        ++n_created;
         v = x;
         Pv = Px;
       } while (v != first_v);
@@ -555,8 +596,13 @@ __global__ void __launch_bounds__(kClipThreads) clip_kernel(ClipArgs a) {
     if (n_exact) atomicAdd(&a.counters[0], n_exact);
     const unsigned amask = __activemask();
     const unsigned mx = __reduce_max_sync(amask, jj);
-    if ((unsigned)(tid & 31) == (unsigned)(__ffs(amask) - 1))
+    const unsigned nt = __reduce_add_sync(amask, n_tests);
+    const unsigned nc = __reduce_add_sync(amask, n_created);
+    if ((unsigned)(tid & 31) == (unsigned)(__ffs(amask) - 1)) {
       atomicMax(&a.counters[1], (unsigned long long)mx);
+      atomicAdd(&a.counters[2], (unsigned long long)nt);
+      atomicAdd(&a.counters[3], (unsigned long long)nc);
+    }
   }
   a.status[s] = st;
   a.nclip[s] = jj;
@@ -595,24 +641,29 @@ __global__ void __launch_bounds__(kClipThreads) clip_kernel(ClipArgs a) {
   cb.flags[s] = parity < 0 ? 1u : 0u;
 }
 
-template <typename Real, int T, int P>
+template <typename Real, int T, int P, bool XF>
 static void launch_clip(const ClipArgs& a, cudaStream_t st) {
   if (a.nq == 0) return;
   const size_t sh = sizeof(CellSmem<Real, kClipThreads, T, P>);
-  cudaFuncSetAttribute(clip_kernel<Real, T, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaFuncSetAttribute(clip_kernel<Real, T, P, XF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)sh);
   const unsigned nb = (a.nq + kClipThreads - 1) / kClipThreads;
-  clip_kernel<Real, T, P><<<nb, kClipThreads, sh, st>>>(a); count_launch();
+  clip_kernel<Real, T, P, XF><<<nb, kClipThreads, sh, st>>>(a); count_launch();
   last_launch_error = cudaGetLastError();
 }
 
 void launch_clip_fp64(const ClipArgs& a, int shape, cudaStream_t st) {
-  if (shape == CLIP_SMALL) launch_clip<double, kSmallT, kSmallP>(a, st);
-  else launch_clip<double, kLargeT, kLargeP>(a, st);
+  if (shape == CLIP_SMALL) launch_clip<double, kSmallT, kSmallP, false>(a, st);
+  else launch_clip<double, kLargeT, kLargeP, false>(a, st);
 }
 
-void launch_clip_fp32(const ClipArgs& a, cudaStream_t st) {
-  launch_clip<float, kSmallT, kSmallP>(a, st);
+void launch_clip_fp32(const ClipArgs& a, int shape, bool exact_fallback, cudaStream_t st) {
+  if (shape == CLIP_SMALL) {
+    if (exact_fallback) launch_clip<float, kSmallT, kSmallP, true>(a, st);
+    else launch_clip<float, kSmallT, kSmallP, false>(a, st);
+  } else {
+    launch_clip<float, kLargeT, kLargeP, true>(a, st);
+  }
 }
 
 }  // namespace gbv

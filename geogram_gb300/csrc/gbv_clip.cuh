@@ -44,7 +44,8 @@ struct ClipArgs {
   int32_t* status;            // by sorted slot
   uint32_t* nclip;            // by sorted slot: neighbours visited
   CombBuf comb;
-  unsigned long long* counters;  // [0] exact predicate calls, [1] max clips
+  unsigned long long* counters;  // [0] exact predicate calls, [1] max clips,
+                                 // [2] conflict tests, [3] corners created
 };
 
 enum ClipShape : int { CLIP_SMALL = 0, CLIP_LARGE = 1 };
@@ -55,9 +56,11 @@ extern cudaError_t last_launch_error;
 
 // FP64 clipping (exact conflict signs).
 void launch_clip_fp64(const ClipArgs& a, int shape, cudaStream_t st);
-// FP32 clipping with certified signs; cells that FP32 cannot certify get
-// status GBV_CELL_RECHECK.
-void launch_clip_fp32(const ClipArgs& a, cudaStream_t st);
+// FP32 clipping with certified signs.  A sign the FP32 bound cannot decide
+// is taken exactly from the FP64 planes when exact_fallback is set (always
+// for the large shape), else the cell gets status GBV_CELL_RECHECK; so do
+// cells whose security-radius stop FP32 cannot certify.
+void launch_clip_fp32(const ClipArgs& a, int shape, bool exact_fallback, cudaStream_t st);
 
 struct GeomArgs {
   SortedSeeds S;

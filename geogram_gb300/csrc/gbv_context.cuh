@@ -40,8 +40,10 @@ struct gbv_context {
   gbv::SortedSeeds S;
   gbv::GridScratch scr;
   unsigned long long* counters = nullptr;  // [0] exact calls [1] max clips
+                                           // [2] conflict tests [3] corners created
   uint32_t* list_counts = nullptr;         // [4] classification counters
   uint32_t* h_counts = nullptr;            // pinned mirror
+  unsigned long long* h_clipc = nullptr;   // pinned: first clipping pass's tests, corners
 
   // last cell results, caller order; their combinatorics stay in the
   // arena's cb_* buffers (by sorted slot) until the seeds are re-sorted

@@ -116,7 +116,12 @@ typedef struct {
     uint64_t n_exact;          /* exact (expansion) predicate evaluations   */
     double ms_grid, ms_knn, ms_clip, ms_retry, ms_total;
     uint32_t n_huge;     /* cells beyond 128 corners / 64 planes (one-thread path) */
-    uint32_t reserved;
+    uint32_t n_knn_exact; /* first-pass queries the FP32 kNN screening passed to
+                             the exact search                          */
+    uint64_t n_conflict_tests;  /* corner-versus-plane tests (triangle_is_in_conflict)
+                                   of the first clipping pass over every cell */
+    uint64_t n_corners_created; /* corners that pass created             */
+    double ms_clip_kernel;      /* that pass's kernel alone               */
 } gbv_cell_report;
 
 /* ---------------------------------------------------------------- */
