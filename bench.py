@@ -45,9 +45,16 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 N_SEEDS = 1_000_000
-# DRAM bytes of one knn_fast_kernel launch (k = 64) on this workload, from an
-# ncu capture (67.10 MB read + 229.45 MB written)
-KNN_TRAFFIC_BYTES = 296.55e6
+# the clipping flop model (per conflict test of a plane against a corner, per
+# corner created: Cramer's rule, four 3x3 determinants and three divides)
+FLOP_TEST, FLOP_CORNER = 7, 59
+# FP32 lanes per SM and SMs of a GB300: the CUDA-core FP32 rate is
+# 2 flop x lanes x SMs x clock (no measured FP32 figure exists for the part)
+FP32_LANES, N_SM = 128, 152
+# DRAM bytes of one launch on this workload, from ncu captures
+# (dram__bytes_read.sum + dram__bytes_write.sum); None where not captured
+CLIP_TRAFFIC_BYTES = None
+KNN_TRAFFIC_BYTES = None
 W_MAX = 1e-4
 METRIC = ("Laguerre cells/s (power diagram, 1M seeds, FP32 clip + FP64 re-clip, "
           "Lloyd step from the seeded start)")
@@ -122,6 +129,18 @@ def load_peaks() -> tuple[float, str]:
             return float(json.load(f)["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
+
+
+def fp32_peak() -> tuple[float, str]:
+    """FP32 CUDA-core rate in TFLOP/s at the part's maximum SM clock."""
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            mhz, kind = float(json.load(f)["sm_max_mhz"]), "measured max clock"
+    except Exception:
+        mhz, kind = 2070.0, "nominal max clock"
+    tf = 2 * FP32_LANES * N_SM * mhz * 1e6 / 1e12
+    return tf, f"nominal 2 x {FP32_LANES} lanes x {N_SM} SMs at {mhz:.0f} MHz ({kind})"
 
 
 def cpu_sample(pc, i0: int, m: int, cores: int) -> tuple[float, float]:
@@ -265,13 +284,21 @@ def run_ours(args) -> None:
     e2e_value = world * N_SEEDS / statistics.mean(e2e_t[1:])
 
     if rank == 0:
-        # ---- the dominant kernel's roofline (kNN, HBM): algorithmic bytes per
-        # seed = query float4 (16) + k list entries (4 k) + count, last
-        # (d2, index) (16), timed by the library's CUDA events on its stream
+        # ---- the dominant kernel: the first FP32 clipping pass over every
+        # cell (clip_kernel<float,64,32>), FP32-pipe bound.  Algorithmic flops
+        # = 7 per conflict test + 59 per corner created, counted by the kernel
+        # itself; its time from the library's CUDA events around that launch
         rep = reports[-1]
+        clip_ms = statistics.median(r["ms_clip_kernel"] for r in reports)
+        clip_flop = FLOP_TEST * rep["n_conflict_tests"] + FLOP_CORNER * rep["n_corners_created"]
+        clip_tf = clip_flop / (clip_ms / 1e3) / 1e12
+        tf_peak, tf_kind = fp32_peak()
+        # ---- kNN (HBM): algorithmic bytes per seed = query float4 (16) + k
+        # list entries (4 k) + count, last (d2, index) (16) + the Morton
+        # counting sort (48), timed by the library's events (grid + kNN)
         k = rep["knn_k"]
-        bytes_per_seed = 16 + 4 * k + 16
-        knn_ms = statistics.median(r["ms_knn"] for r in reports)
+        bytes_per_seed = 16 + 4 * k + 16 + 48
+        knn_ms = statistics.median(r["ms_knn"] + r["ms_grid"] for r in reports)
         achieved = bytes_per_seed * N_SEEDS / (knn_ms / 1e3) / 1e9
         peak, peak_kind = load_peaks()
         # ---- plain FP64 path on the same seeds, and the error of this mode
@@ -311,22 +338,32 @@ def run_ours(args) -> None:
                        "seeds": "reset to the seeded positions before each step, outside "
                                 "the timed region",
                        "parallelism": "replicas only" if world > 1 else "1 GPU"},
-            "roofline": {"kernel": "knn_fast_kernel (first kNN pass)", "bound": "hbm",
-                         "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "peak_kind": peak_kind,
-                         "bytes_per_seed": bytes_per_seed,
-                         # ncu dram__bytes_read.sum + dram__bytes_write.sum of this kernel's
-                         # first pass on this workload (one capture, bytes per launch)
-                         "traffic": KNN_TRAFFIC_BYTES},
+            "roofline": {"kernel": "clip_kernel<float,64,32> (first clipping pass, all cells)",
+                         "bound": "fp32", "achieved": clip_tf, "peak": tf_peak,
+                         "unit": "TFLOP/s", "frac": clip_tf / tf_peak, "peak_kind": tf_kind,
+                         "ms": clip_ms, "flop": clip_flop,
+                         "counts": {"conflict_tests": rep["n_conflict_tests"],
+                                    "corners_created": rep["n_corners_created"],
+                                    "flop_per_test": FLOP_TEST,
+                                    "flop_per_corner": FLOP_CORNER},
+                         "traffic": CLIP_TRAFFIC_BYTES},
+            "roofline_knn": {"kernel": "grid + knn_tile_kernel + flagged exact queries",
+                             "bound": "hbm", "achieved": achieved, "peak": peak,
+                             "unit": "GB/s", "frac": achieved / peak,
+                             "peak_kind": peak_kind + " (hbm_gbs)", "ms": knn_ms,
+                             "bytes_per_seed": bytes_per_seed, "k": k,
+                             "traffic": KNN_TRAFFIC_BYTES},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "cells/s",
                     "h2d_bytes_per_step": 32 * N_SEEDS, "d2h_bytes_per_step": 24 * N_SEEDS},
             "gpu_launches": int(launches),
             "clocks": clk.summary(),
             "phases_ms": {kk: round(statistics.median(r[kk] for r in reports), 3)
-                          for kk in ("ms_grid", "ms_knn", "ms_clip", "ms_retry", "ms_total")},
+                          for kk in ("ms_grid", "ms_knn", "ms_clip", "ms_clip_kernel",
+                                     "ms_retry", "ms_total")},
             "cells": {kk: rep[kk] for kk in ("n_recheck_fp64", "n_more_k", "n_overflow",
-                                             "mean_clips", "max_clips", "nnz", "knn_k")},
+                                             "n_exact", "n_knn_exact", "mean_clips",
+                                             "max_clips", "nnz", "knn_k")},
             "fp64_plain": {"cells_per_s": fp64_cps, "ms": statistics.median(t64),
                            "speedup_of_this_mode": statistics.median(t64) / t32,
                            "max_rel_vol_err_vs_fp64": rel_vol, "max_abs_mg_err_vs_fp64": abs_mg,

@@ -1342,8 +1342,10 @@ static void save_adjacency(gbv_context* c, uint32_t n, cudaStream_t st, uint32_t
     GBV_CUDA(cudaMemcpyAsync(*ix, c->nbr, sizeof(uint32_t) * c->nnz, cudaMemcpyDeviceToDevice, st));
 }
 
-// Hessian of the current cells, in buffers of the context.
-static Hessian current_hessian(gbv_context* c, const double* xyz, uint32_t n, cudaStream_t st) {
+// Hessian of the current cells, in buffers of the context; with `sell`,
+// also its sliced-ELL copy for the CG product.
+static Hessian current_hessian(gbv_context* c, const double* xyz, uint32_t n, cudaStream_t st,
+                               bool sell = true) {
   Hessian H;
   uint32_t* rp = c->buf<uint32_t>("ot_h_rp", (size_t)n + 1);
   uint32_t* col = c->buf<uint32_t>("ot_h_col", std::max<uint64_t>(c->nnz, 1));
@@ -1353,7 +1355,32 @@ static Hessian current_hessian(gbv_context* c, const double* xyz, uint32_t n, cu
     GBV_CUDA(cudaMemcpyAsync(col, c->nbr, sizeof(uint32_t) * c->nnz, cudaMemcpyDeviceToDevice, st));
   H.val = c->buf<double>("ot_h_val", std::max<uint64_t>(c->nnz, 1));
   H.diag = c->buf<double>("ot_h_diag", n);
+  H.invd = c->buf<double>("ot_h_invd", n);
   assemble_hessian(xyz, rp, col, c->area, n, H, st);
+  if (!sell) return H;
+  const uint32_t nsl = sell_slices(n);
+  uint32_t* sl_off = c->buf<uint32_t>("ot_sl_off", (size_t)nsl + 1);
+  GBV_CUDA(cudaMemsetAsync(sl_off, 0, sizeof(uint32_t) * ((size_t)nsl + 1), st));
+  sell_widths(H, sl_off, st);
+  if (32ull * c->nnz > 0xffffffffull) {  // the slices may not fit 32-bit offsets
+    unsigned long long* tot = c->buf<unsigned long long>("ot_sl_total", 1);
+    GBV_CUDA(cudaMemsetAsync(tot, 0, sizeof(unsigned long long), st));
+    sum_u32_kernel<<<256, 256, 0, st>>>(sl_off, nsl, tot); count_launch();
+    unsigned long long h_tot = 0;
+    GBV_CUDA(cudaMemcpyAsync(&h_tot, tot, sizeof h_tot, cudaMemcpyDeviceToHost, st));
+    GBV_CUDA(cudaStreamSynchronize(st));
+    if (h_tot > 0xffffffffull)
+      throw StatusError{GBV_ERR_CAPACITY, std::to_string(h_tot) +
+                                              " padded Hessian entries exceed 32-bit offsets"};
+  }
+  uint32_t* stmp = c->buf<uint32_t>("ot_sl_scan_tmp", scan_tmp_elems((size_t)nsl + 1));
+  exclusive_scan_u32(sl_off, (size_t)nsl + 1, stmp, st);
+  uint32_t total = 0;
+  GBV_CUDA(cudaMemcpyAsync(&total, sl_off + nsl, 4, cudaMemcpyDeviceToHost, st));
+  GBV_CUDA(cudaStreamSynchronize(st));
+  uint32_t* s_col = c->buf<uint32_t>("ot_sl_col", std::max<uint32_t>(total, 1));
+  double* s_val = c->buf<double>("ot_sl_val", std::max<uint32_t>(total, 1));
+  sell_pack(H, sl_off, s_col, s_val, st);
   return H;
 }
 
@@ -1392,8 +1419,7 @@ static void ot_solve(gbv_context* c, const double* xyz, const double* nu_in, uin
   double* wt = c->buf<double>("ot_wt", n);
   fill_kernel<<<nblocks(n, 256), 256, 0, st>>>(ones, 1.0, n); count_launch();
   CgScalars* cg_sc = c->buf<CgScalars>("ot_cg_scalars", 1);
-  double* cg_part_a = c->buf<double>("ot_cg_part_a", 2 * kPcgParts);
-  double* cg_part_b = c->buf<double>("ot_cg_part_b", 4 * kPcgParts);
+  double* cg_part = c->buf<double>("ot_cg_part", 2 * kPcgParts);
   const double nu_norm = std::sqrt(W.dot(nu, nu));
   // x = H^+ b by Jacobi-preconditioned CG; b (overwritten: the residual) is
   // first projected on mean zero (H has the constants as kernel), and so
@@ -1403,14 +1429,14 @@ static void ot_solve(gbv_context* c, const double* xyz, const double* nu_in, uin
     add_scalar(b, -mean, n, st);
     const double bnorm = std::sqrt(W.dot(b, b));
     GBV_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, st));
-    cg_precond(b, H.diag, z, n, st);
+    cg_precond(b, H.invd, z, n, st);
     GBV_CUDA(cudaMemcpyAsync(p, z, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
     const double rz = W.dot(b, z);
     // the iterations run on the device; the host looks at the iteration
     // count and the convergence flag every kCgChunk iterations
     constexpr uint32_t kCgChunk = 16;
     CgScalars h{};
-    h.rz[0] = rz;
+    h.rz = rz;
     h.b2 = bnorm * bnorm;
     h.tol2 = tol * tol;
     h.done = (bnorm > 0.0) ? 0u : 1u;
@@ -1418,7 +1444,7 @@ static void ot_solve(gbv_context* c, const double* xyz, const double* nu_in, uin
     uint32_t k = 0;
     while (!h.done && k < o.max_cg) {
       const uint32_t m = std::min<uint32_t>(kCgChunk, o.max_cg - k);
-      pcg_iterations(H, x, b, p, Ap, z, cg_part_a, cg_part_b, cg_sc, k, m, st);
+      pcg_iterations(H, x, b, p, Ap, z, cg_part, cg_sc, m, st);
       GBV_CUDA(cudaMemcpyAsync(&h, cg_sc, sizeof h, cudaMemcpyDeviceToHost, st));
       GBV_CUDA(cudaStreamSynchronize(st));
       k = h.k;
@@ -2528,7 +2554,7 @@ gbv_status gbv_ot_gradient_hessian(gbv_context* c, const double* xyz, const doub
     }
     if (h_capacity > 0) {
       if (h_capacity < c->nnz) throw StatusError{GBV_ERR_CAPACITY, "Hessian capacity too small"};
-      Hessian H = current_hessian(c, dx, n, st);
+      Hessian H = current_hessian(c, dx, n, st, false);
       if (h_rowptr) GBV_CUDA(cudaMemcpyAsync(h_rowptr, H.rowptr, 4 * ((size_t)n + 1), cudaMemcpyDeviceToHost, st));
       if (h_col) GBV_CUDA(cudaMemcpyAsync(h_col, H.col, 4 * c->nnz, cudaMemcpyDeviceToHost, st));
       if (h_val) GBV_CUDA(cudaMemcpyAsync(h_val, H.val, 8 * c->nnz, cudaMemcpyDeviceToHost, st));

@@ -1,6 +1,5 @@
-// Laguerre cell clipping: one thread per cell, the polytope in shared
-// memory laid out [slot][thread] so that a warp's 32 cells touch 32
-// consecutive words.
+// Laguerre cell clipping: one warp per cell, the polytope in a shared
+// memory record of the warp, its triangles spread over the lanes.
 //
 // The cell is kept in the dual form of the reference's VBW::ConvexCell
 // (voronoi/convex_cell.h:419-1436): every clipping plane is a vertex,
@@ -18,6 +17,11 @@
 //     bound cannot decide the sign, the FP64 kernel evaluates the exact
 //     determinant sign (the reference's PCK::det_4d decision) and the FP32
 //     kernel marks the cell for an FP64 re-clip;
+//   - the lanes test the triangles against a plane together (one or more
+//     triangles each, a ballot gives the conflict zone), find the border
+//     of the zone together, and create the new triangles together once one
+//     lane has walked the border; the planes of the next 32 list positions
+//     are computed one per lane ahead of the loop;
 //   - the security-radius test (generic_RVD.h:2278-2352) reads the cached
 //     corner radii.
 // The kernel writes the cell's combinatorics; gbv_geom.cu turns them into
@@ -31,7 +35,9 @@
 // clip is: parity flips (survivors reversed, nothing rewritten), the c-th
 // new triangle gets eff = -(max eff of the survivors) - 1 - c, and the walk
 // starts at the border edge maximising (new eff of the kept triangle, edge).
+#include <algorithm>
 #include <cfloat>
+#include <climits>
 #include <cmath>
 #include <type_traits>
 
@@ -43,7 +49,14 @@
 namespace gbv {
 
 cudaError_t last_launch_error = cudaSuccess;
-constexpr int kClipThreads = 32;
+constexpr int kClipWarps = 8;  // cells in flight per block, one per warp
+// resident blocks per SM the registers must allow: 3 (80 registers) for the
+// lean FP32 loop that runs every cell, 2 where the exact-sign fallback's
+// registers would spill
+template <typename Real, bool XF>
+constexpr int clip_min_blocks() {
+  return (std::is_same<Real, float>::value && !XF) ? 3 : 2;
+}
 
 // ---------------------------------------------------------------------
 // Small fixed-capacity bit sets
@@ -103,36 +116,121 @@ __device__ __forceinline__ Bits<NW> full_bits(int n) {
   return r;
 }
 
-// ---------------------------------------------------------------------
-// Per-thread cell storage in shared memory, [slot][thread]
-// ---------------------------------------------------------------------
-template <typename Real, int BS, int T, int P>
-struct CellSmem;
+// k-th (0-based) set bit of m; the bit must exist
+__device__ __forceinline__ int select32(uint32_t m, int k) {
+  int base = 0;
+#pragma unroll
+  for (int w = 16; w >= 1; w >>= 1) {
+    const uint32_t low = m & ((1u << w) - 1u);
+    const int c = __popc(low);
+    if (k >= c) {
+      k -= c;
+      m >>= w;
+      base += w;
+    } else {
+      m = low;
+    }
+  }
+  return base;
+}
 
-template <int BS, int T, int P>
-struct CellSmem<double, BS, T, P> {
-  double2 cxy[T][BS];     // corner x, y (reference frame and arithmetic)
-  double2 czr[T][BS];     // corner z, squared distance to the seed
-  float eps[T][BS];       // corner error bound (cramer_bound)
-  uint32_t tv[T][BS];     // planes i | j << 8 | k << 16
-  uint32_t ta[T][BS];     // triangles across the edges opposite i, j, k
-  int16_t key[T][BS];
-  uint32_t pown[P][BS];   // plane owner: seed slot or kBoxBase + face
-  uint16_t prank[P][BS];  // list position of the plane's seed
-  uint16_t pnb[P][BS];    // border scratch: kept triangle | edge << 8
-  uint8_t pnext[P][BS];   // border scratch: next border plane
+template <int NW>
+__device__ __forceinline__ int select_bit(const Bits<NW>& b, int k) {
+#pragma unroll
+  for (int i = 0; i < NW; ++i) {
+    const uint32_t lo = (uint32_t)b.w[i], hi = (uint32_t)(b.w[i] >> 32);
+    const int cl = __popc(lo), ch = __popc(hi);
+    if (k < cl) return 64 * i + select32(lo, k);
+    k -= cl;
+    if (k < ch) return 64 * i + 32 + select32(hi, k);
+    k -= ch;
+  }
+  return -1;
+}
+
+// The n lowest set bits of b.
+template <int NW>
+__device__ __forceinline__ Bits<NW> lowest_bits(const Bits<NW>& b, int n) {
+  Bits<NW> r;
+#pragma unroll
+  for (int i = 0; i < NW; ++i) {
+    const int c = __popcll(b.w[i]);
+    if (n >= c) {
+      r.w[i] = b.w[i];
+      n -= c;
+    } else if (n > 0) {
+      const uint32_t lo = (uint32_t)b.w[i];
+      const int cl = __popc(lo);
+      const int pos = n <= cl ? select32(lo, n - 1) : 32 + select32((uint32_t)(b.w[i] >> 32), n - 1 - cl);
+      r.w[i] = b.w[i] & (pos >= 63 ? ~0ull : ((2ull << pos) - 1ull));
+      n = 0;
+    } else {
+      r.w[i] = 0;
+    }
+  }
+  return r;
+}
+
+template <int NW>
+__device__ __forceinline__ void or_into(Bits<NW>& a, const Bits<NW>& b) {
+#pragma unroll
+  for (int i = 0; i < NW; ++i) a.w[i] |= b.w[i];
+}
+
+template <typename R>
+__device__ __forceinline__ R warp_max(R v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+  return v;
+}
+__device__ __forceinline__ float warp_maxf(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+  return v;
+}
+__device__ __forceinline__ double warp_maxf(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+  return v;
+}
+__device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+  return v;
+}
+
+// ---------------------------------------------------------------------
+// Cell record in shared memory, one per warp
+// ---------------------------------------------------------------------
+template <typename Real, int T, int P>
+struct CellRec;
+
+template <int T, int P>
+struct __align__(16) CellRec<double, T, P> {
+  double2 cxy[T];     // corner x, y (reference frame and arithmetic)
+  double2 czr[T];     // corner z, squared distance to the seed
+  float eps[T];       // corner error bound (cramer_bound)
+  uint32_t tv[T];     // planes i | j << 8 | k << 16
+  uint32_t ta[T];     // triangles across the edges opposite i, j, k (bytes 0-2)
+  uint32_t pown[P];   // plane owner: seed slot or kBoxBase + face
+  int16_t key[T];
+  uint16_t prank[P];  // list position of the plane's seed
+  uint16_t pnb[P];    // border scratch: kept triangle | edge << 8
+  uint8_t pnext[P];   // border scratch: next border plane
+  uint8_t order[T];   // border planes in walk order
 };
 
-template <int BS, int T, int P>
-struct CellSmem<float, BS, T, P> {
-  float4 c4[T][BS];       // corner x, y, z (frame centred on the seed), eps
-  uint32_t tv[T][BS];
-  uint32_t ta[T][BS];
-  int16_t key[T][BS];
-  float4 pl[P][BS];       // local-frame plane equations
-  uint16_t prank[P][BS];
-  uint16_t pnb[P][BS];
-  uint8_t pnext[P][BS];
+template <int T, int P>
+struct __align__(16) CellRec<float, T, P> {
+  float4 c4[T];       // corner x, y, z (frame centred on the seed), eps
+  float4 pl[P];       // local-frame plane equations
+  uint32_t tv[T];
+  uint32_t ta[T];
+  int16_t key[T];
+  uint16_t prank[P];
+  uint16_t pnb[P];
+  uint8_t pnext[P];
+  uint8_t order[T];
 };
 
 // ---------------------------------------------------------------------
@@ -197,311 +295,319 @@ __device__ __noinline__ bool exact_conflict(double4 p0, double4 p1, double4 p2, 
 // ---------------------------------------------------------------------
 // XF (FP32 only): a sign the FP32 bound cannot decide is taken exactly from
 // the FP64 planes; without it the cell is marked for a recheck (a leaner
-// loop for the first pass over every cell).
+// loop for the first pass over every cell).  The warps stride over the
+// queries; every lane holds the cell's bookkeeping (valid triangles, used
+// planes, parity, R2), so control flow stays uniform across the warp.
 template <typename Real, int T, int P, bool XF>
-__global__ void __launch_bounds__(kClipThreads) clip_kernel(ClipArgs a) {
-  constexpr int BS = kClipThreads;
+__global__ void __launch_bounds__(kClipWarps * 32, clip_min_blocks<Real, XF>()) clip_kernel(ClipArgs a) {
   constexpr int NWT = (T + 63) / 64;
+  constexpr int NS = T / 32;  // triangle slots per lane: slot t on lane t % 32
   constexpr bool kFP64 = std::is_same<Real, double>::value;
-  using Smem = CellSmem<Real, BS, T, P>;
+  using Rec = CellRec<Real, T, P>;
+  using Plane = typename std::conditional<kFP64, double4, float4>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
-  const int tid = threadIdx.x;
-  const uint32_t qi = blockIdx.x * BS + tid;
-  if (qi >= a.nq) return;
+  const unsigned FULL = 0xFFFFFFFFu;
+  const int lane = threadIdx.x & 31;
+  Rec& g = reinterpret_cast<Rec*>(smem_raw)[threadIdx.x >> 5];
   const SortedSeeds& S = a.S;
-  const uint32_t s = a.qlist ? a.qlist[qi] : qi;
-  const uint32_t row = a.qrow ? a.qrow[qi] : qi;
+  const uint32_t nwarps = gridDim.x * kClipWarps;
+  unsigned long long n_exact = 0, n_tests = 0, n_created = 0;
+  uint32_t max_jj = 0;
 
-  SeedCtx sc;
-  sc.pi = S.xd[s];
+  for (uint32_t qi = blockIdx.x * kClipWarps + (threadIdx.x >> 5); qi < a.nq; qi += nwarps) {
+    const uint32_t s = a.qlist ? a.qlist[qi] : qi;
+    const uint32_t row = a.qrow ? a.qrow[qi] : qi;
+
+    SeedCtx sc;
+    sc.pi = S.xd[s];
 #pragma unroll
-  for (int c = 0; c < 6; ++c) sc.box[c] = a.box[c];
-  if constexpr (kFP64) {
-    sc.qi = S.q[s];
-  } else {
-    sc.fh = S.xf[s];
-    sc.fl = S.xl[s];
-    sc.fw = S.wf ? S.wf[s] : make_float2(0.f, 0.f);
-  }
-  const double hi2 = __dmul_rn(sc.pi.w, sc.pi.w);
-  const float hi2f = sc.fh.w * sc.fh.w;
-
-  // Plane p's equation (FP64: recomputed from its owner, FP32: stored).
-  auto plane_of = [&](uint32_t p) {
-    if constexpr (kFP64) return plane_fp64(sm.pown[p][tid], sc.pi, sc.qi, sc.box, S);
-    else return sm.pl[p][tid];
-  };
-  // The reference's FP64 plane of plane slot p (FP32 kernel: from its list
-  // position, box faces keep their slots 0-5) and of seed slot j.
-  auto plane64_of = [&](uint32_t j) -> double4 {
-    return plane_fp64(j, sc.pi, S.q[s], sc.box, S);
-  };
-  auto plane64 = [&](uint32_t p) -> double4 {
+    for (int c = 0; c < 6; ++c) sc.box[c] = a.box[c];
     if constexpr (kFP64) {
-      return plane_fp64(sm.pown[p][tid], sc.pi, sc.qi, sc.box, S);
+      sc.qi = S.q[s];
     } else {
-      const uint16_t rk = sm.prank[p][tid];
-      const uint32_t own =
-          (rk == 0xFFFF) ? kBoxBase + p : a.nbr[(size_t)rk * a.nbr_stride + row];
-      return plane_fp64(own, sc.pi, S.q[s], sc.box, S);
+      sc.fh = S.xf[s];
+      sc.fl = S.xl[s];
+      sc.fw = S.wf ? S.wf[s] : make_float2(0.f, 0.f);
     }
-  };
-  // Creates the corner of triangle t from its planes; returns its r2.
-  auto make_corner = [&](uint32_t t, const auto& pa, const auto& pb, const auto& pc) -> Real {
-    if constexpr (kFP64) {
-      double x, y, z;
-      float e;
-      corner_fp64(pa, pb, pc, x, y, z, e);
-      const double r2 = r_sqdist(sc.pi.x, sc.pi.y, sc.pi.z, make_double3(x, y, z));
-      sm.cxy[t][tid] = make_double2(x, y);
-      sm.czr[t][tid] = make_double2(z, r2);
-      sm.eps[t][tid] = e;
-      return r2;
-    } else {
-      float x, y, z, e;
-      corner_fp32(pa, pb, pc, x, y, z, e);
-      sm.c4[t][tid] = make_float4(x, y, z, e);
-      return x * x + y * y + z * z;
-    }
-  };
+    const double hi2 = __dmul_rn(sc.pi.w, sc.pi.w);
+    const float hi2f = sc.fh.w * sc.fh.w;
+    const float pn = sc.fh.x * sc.fh.x + sc.fh.y * sc.fh.y + sc.fh.z * sc.fh.z;
 
-  // ---- init_with_box (convex_cell.cpp:175-215): 6 planes, 8 corners
-#pragma unroll
-  for (int b = 0; b < 6; ++b) {
-    sm.prank[b][tid] = 0xFFFF;
-    if constexpr (kFP64) sm.pown[b][tid] = kBoxBase + b;
-    else sm.pl[b][tid] = box_plane_fp32(b, sc);
-  }
-  {
-    // triangles and adjacency of the box corners, in the reference's order
-    const uint32_t bt[8] = {2 | 5 << 8 | 0 << 16, 5 | 3 << 8 | 0 << 16, 1 | 5 << 8 | 2 << 16,
-                            5 | 1 << 8 | 3 << 16, 4 | 2 << 8 | 0 << 16, 4 | 0 << 8 | 3 << 16,
-                            2 | 4 << 8 | 1 << 16, 4 | 3 << 8 | 1 << 16};
-    const uint32_t ba[8] = {1 | 4 << 8 | 2 << 16, 5 | 0 << 8 | 3 << 16, 0 | 6 << 8 | 3 << 16,
-                            7 | 1 << 8 | 2 << 16, 0 | 5 << 8 | 6 << 16, 1 | 7 << 8 | 4 << 16,
-                            7 | 2 << 8 | 4 << 16, 3 | 6 << 8 | 5 << 16};
-#pragma unroll
-    for (int t = 0; t < 8; ++t) {
-      sm.tv[t][tid] = bt[t];
-      sm.ta[t][tid] = ba[t];
-      sm.key[t][tid] = (int16_t)(-t);  // each pushed at the head of the list
-    }
-  }
-  Bits<NWT> valid;
-  valid.clear();
-  Real R2 = 0;
-  for (int t = 0; t < 8; ++t) {
-    valid.set(t);
-    const uint32_t v = sm.tv[t][tid];
-    const Real r2 = make_corner(t, plane_of(v & 0xFF), plane_of(v >> 8 & 0xFF),
-                                plane_of(v >> 16 & 0xFF));
-    R2 = fmax(R2, r2);
-  }
-  uint64_t pused = 0x3Full;
-  int parity = 1;
-
-  const uint32_t cnt_raw = a.nbr_cnt[row];
-  const bool dup = (cnt_raw >> 31) != 0;
-  const uint32_t copies = (cnt_raw >> 24) & 0x7Fu;
-  // a seed with higher-index copies: the reference stops growing its list
-  // at reference_list_cap, certified or not
-  const uint32_t cap = copies ? reference_list_cap(a.k0, a.n_total, copies, a.check_sr != 0)
-                              : 0xFFFFFFFFu;
-  const uint32_t cnt = dup ? 0u : min(cnt_raw & kCntMask, cap);
-  int32_t st = -1;
-  uint32_t jj = 0;
-  unsigned long long n_exact = 0;
-  uint32_t n_tests = 0, n_created = 0;  // conflict tests, corners made (the flop model)
-
-  if (dup) {
-    st = CELL_DUPLICATE;
-  } else {
-    for (; jj < cnt; ++jj) {
-      const uint32_t j = a.nbr[(size_t)jj * a.nbr_stride + row];
-      // ---- security radius (generic_RVD.h:2300-2324) and the plane
-      float4 Pf = make_float4(0.f, 0.f, 0.f, 0.f);
-      double4 Pd = make_double4(0.0, 0.0, 0.0, 0.0);
+    // Plane p's equation (FP64: recomputed from its owner, FP32: stored).
+    auto plane_of = [&](uint32_t p) {
+      if constexpr (kFP64) return plane_fp64(g.pown[p], sc.pi, sc.qi, sc.box, S);
+      else return g.pl[p];
+    };
+    // The reference's FP64 plane of plane slot p (FP32 kernel: from its
+    // list position, box faces keep their slots 0-5) and of seed slot j.
+    auto plane64_of = [&](uint32_t j) -> double4 {
+      return plane_fp64(j, sc.pi, S.q[s], sc.box, S);
+    };
+    auto plane64 = [&](uint32_t p) -> double4 {
       if constexpr (kFP64) {
-        const double4 pj = S.xd[j];
+        return plane_fp64(g.pown[p], sc.pi, sc.qi, sc.box, S);
+      } else {
+        const uint16_t rk = g.prank[p];
+        const uint32_t own =
+            (rk == 0xFFFF) ? kBoxBase + p : a.nbr[(size_t)rk * a.nbr_stride + row];
+        return plane_fp64(own, sc.pi, S.q[s], sc.box, S);
+      }
+    };
+    // Creates the corner of triangle t from its planes; returns its r2.
+    auto make_corner = [&](uint32_t t, const auto& pa, const auto& pb, const auto& pc) -> Real {
+      if constexpr (kFP64) {
+        double x, y, z;
+        float e;
+        corner_fp64(pa, pb, pc, x, y, z, e);
+        const double r2 = r_sqdist(sc.pi.x, sc.pi.y, sc.pi.z, make_double3(x, y, z));
+        g.cxy[t] = make_double2(x, y);
+        g.czr[t] = make_double2(z, r2);
+        g.eps[t] = e;
+        return r2;
+      } else {
+        float x, y, z, e;
+        corner_fp32(pa, pb, pc, x, y, z, e);
+        g.c4[t] = make_float4(x, y, z, e);
+        return x * x + y * y + z * z;
+      }
+    };
+
+    // ---- init_with_box (convex_cell.cpp:175-215): 6 planes, 8 corners,
+    // triangles and adjacency in the reference's order, each pushed at the
+    // head of the list
+    if (lane < 6) {
+      g.prank[lane] = 0xFFFF;
+      if constexpr (kFP64) g.pown[lane] = kBoxBase + lane;
+      else g.pl[lane] = box_plane_fp32(lane, sc);
+    }
+    if (lane < 8) {
+      const uint32_t bt[8] = {2 | 5 << 8 | 0 << 16, 5 | 3 << 8 | 0 << 16, 1 | 5 << 8 | 2 << 16,
+                              5 | 1 << 8 | 3 << 16, 4 | 2 << 8 | 0 << 16, 4 | 0 << 8 | 3 << 16,
+                              2 | 4 << 8 | 1 << 16, 4 | 3 << 8 | 1 << 16};
+      const uint32_t ba[8] = {1 | 4 << 8 | 2 << 16, 5 | 0 << 8 | 3 << 16, 0 | 6 << 8 | 3 << 16,
+                              7 | 1 << 8 | 2 << 16, 0 | 5 << 8 | 6 << 16, 1 | 7 << 8 | 4 << 16,
+                              7 | 2 << 8 | 4 << 16, 3 | 6 << 8 | 5 << 16};
+      g.tv[lane] = bt[lane];
+      g.ta[lane] = ba[lane];
+      g.key[lane] = (int16_t)(-lane);
+    }
+    __syncwarp();
+    Real R2 = 0;
+    if (lane < 8) {
+      const uint32_t v = g.tv[lane];
+      R2 = make_corner(lane, plane_of(v & 0xFF), plane_of(v >> 8 & 0xFF), plane_of(v >> 16 & 0xFF));
+    }
+    R2 = warp_maxf(R2);
+    Bits<NWT> valid;
+    valid.clear();
+    valid.w[0] = 0xFFull;
+    uint64_t pused = 0x3Full;
+    int parity = 1;
+
+    const uint32_t cnt_raw = a.nbr_cnt[row];
+    const bool dup = (cnt_raw >> 31) != 0;
+    const uint32_t copies = (cnt_raw >> 24) & 0x7Fu;
+    // a seed with higher-index copies: the reference stops growing its list
+    // at reference_list_cap, certified or not
+    const uint32_t cap = copies ? reference_list_cap(a.k0, a.n_total, copies, a.check_sr != 0)
+                                : 0xFFFFFFFFu;
+    const uint32_t cnt = dup ? 0u : min(cnt_raw & kCntMask, cap);
+    int32_t st = -1;
+    uint32_t jj = 0;
+
+    if (dup) {
+      st = CELL_DUPLICATE;
+    } else {
+      // the plane of list position jj0 + lane, its security-radius
+      // distance and its conflict bound terms
+      uint32_t bj = 0;
+      Plane bP{};
+      Real bd = 0, bpa = 0, bbw = 0;
+      uint32_t jj0 = 0;
+      for (; jj < cnt; ++jj) {
+        if (jj == 0 || jj - jj0 == 32) {
+          jj0 = jj;
+          const uint32_t pos = jj0 + lane;
+          if (pos < cnt) {
+            const uint32_t j = a.nbr[(size_t)pos * a.nbr_stride + row];
+            bj = j;
+            if constexpr (kFP64) {
+              const double4 pj = S.xd[j];
+              bd = a.check_sr ? dist2_exact(sc.pi, pj) : 0.0;
+              bP = make_double4(2.0 * __dsub_rn(sc.pi.x, pj.x), 2.0 * __dsub_rn(sc.pi.y, pj.y),
+                                2.0 * __dsub_rn(sc.pi.z, pj.z), __dsub_rn(sc.qi, S.q[j]));
+              bpa = (fabs(bP.x) + fabs(bP.y) + fabs(bP.z)) * 1.0001;
+              bbw = Consts<double>::kDot * fabs(bP.w) * 1.0001;
+            } else {
+              // d = p_j - p_i from the value/remainder pairs keeps FP32
+              // relative accuracy however close the two seeds are
+              const float4 jh = S.xf[j], jl = S.xl[j];
+              const float dx = (jh.x - sc.fh.x) + (jl.x - sc.fl.x);
+              const float dy = (jh.y - sc.fh.y) + (jl.y - sc.fl.y);
+              const float dz = (jh.z - sc.fh.z) + (jl.z - sc.fl.z);
+              const float dh = (jh.w - sc.fh.w) + (jl.w - sc.fl.w);
+              const float d2 = dx * dx + dy * dy + dz * dz;
+              bd = d2 + dh * dh;
+              float dw = 0.f, wj = 0.f;
+              if (S.wf) {
+                const float2 w2 = S.wf[j];
+                dw = (w2.x - sc.fw.x) + (w2.y - sc.fw.y);
+                wj = w2.x;
+              }
+              // (-2 d, |d|^2 + w_i - w_j): the bisector in the seed's frame
+              bP = make_float4(-2.f * dx, -2.f * dy, -2.f * dz, d2 - dw);
+              bpa = (fabsf(bP.x) + fabsf(bP.y) + fabsf(bP.z)) * 1.0001f;
+              // the reference's own FP64 planes carry a rounding of about
+              // 2^-52 (|w_i| + |w_j| + |p_i|^2 + |p_j|^2) in their offset
+              const float qmag = fabsf(sc.fw.x) + fabsf(wj) + 2.f * pn + 1.f;
+              bbw = (Consts<float>::kDot * fabsf(bP.w) + 3.5527137e-15f * qmag) * 1.0001f;
+            }
+          }
+        }
+        const int src = (int)(jj - jj0);
+        const uint32_t j = __shfl_sync(FULL, bj, src);
+        // ---- security radius (generic_RVD.h:2300-2324)
         if (a.check_sr) {
-          const double dij = dist2_exact(sc.pi, pj);
-          if (dij > __dmul_rn(4.1, __dadd_rn(R2, hi2))) {
+          const Real dj = __shfl_sync(FULL, bd, src);
+          bool stop;
+          if constexpr (kFP64) stop = dj > __dmul_rn(4.1, __dadd_rn(R2, hi2));
+          else stop = dj > 4.1f * (R2 + hi2f);
+          if (stop) {
             st = CELL_CERTIFIED;
             break;
           }
         }
-        Pd = make_double4(2.0 * __dsub_rn(sc.pi.x, pj.x), 2.0 * __dsub_rn(sc.pi.y, pj.y),
-                          2.0 * __dsub_rn(sc.pi.z, pj.z), __dsub_rn(sc.qi, S.q[j]));
-      } else {
-        // d = p_j - p_i from the value/remainder pairs keeps FP32 relative
-        // accuracy however close the two seeds are
-        const float4 jh = S.xf[j], jl = S.xl[j];
-        const float dx = (jh.x - sc.fh.x) + (jl.x - sc.fl.x);
-        const float dy = (jh.y - sc.fh.y) + (jl.y - sc.fl.y);
-        const float dz = (jh.z - sc.fh.z) + (jl.z - sc.fl.z);
-        const float dh = (jh.w - sc.fh.w) + (jl.w - sc.fl.w);
-        const float d2 = dx * dx + dy * dy + dz * dz;
-        if (a.check_sr && d2 + dh * dh > 4.1f * (R2 + hi2f)) {
-          st = CELL_CERTIFIED;
+        // every clip relinks the reference's valid list in reverse order
+        const int par_old = parity;
+        parity = -parity;
+        if (!valid.any()) continue;  // empty cell: nothing left to clip
+        Plane Pn;
+        Pn.x = __shfl_sync(FULL, bP.x, src);
+        Pn.y = __shfl_sync(FULL, bP.y, src);
+        Pn.z = __shfl_sync(FULL, bP.z, src);
+        Pn.w = __shfl_sync(FULL, bP.w, src);
+        const Real pa1 = __shfl_sync(FULL, bpa, src), bw = __shfl_sync(FULL, bbw, src);
+        const Real wide = a.fast_pred ? (Real)kFastPredWide : (Real)1;
+
+        // ---- conflict scan (triangle_is_in_conflict, convex_cell.cpp:870-912)
+        bool cf[NS];
+        Real kr2 = 0;
+        int kme = -0x7FFF;
+        bool uncertain = false;
+#pragma unroll
+        for (int q = 0; q < NS; ++q) {
+          const int t = lane + 32 * q;
+          cf[q] = false;
+          if (!valid.test(t)) continue;
+          Real cx, cy, cz, r2, eps;
+          if constexpr (kFP64) {
+            const double2 xy = g.cxy[t], zr = g.czr[t];
+            cx = xy.x;
+            cy = xy.y;
+            cz = zr.x;
+            r2 = zr.y;
+            eps = (double)g.eps[t];
+          } else {
+            const float4 c = g.c4[t];
+            cx = c.x;
+            cy = c.y;
+            cz = c.z;
+            eps = c.w;
+            r2 = cx * cx + cy * cy + cz * cz;
+          }
+          Real sv;
+          if constexpr (kFP64) sv = fma(Pn.z, cz, fma(Pn.y, cy, fma(Pn.x, cx, Pn.w)));
+          else sv = fmaf(Pn.z, cz, fmaf(Pn.y, cy, fmaf(Pn.x, cx, Pn.w)));
+          const Real bound = fma(pa1, eps, bw) * wide;
+          bool in_conflict;
+          if (sv < -bound) {
+            in_conflict = true;
+          } else if (sv > bound) {
+            in_conflict = false;
+          } else {
+            if constexpr (kFP64) {
+              const uint32_t v = g.tv[t];
+              in_conflict = exact_conflict(plane_of(v & 0xFF), plane_of(v >> 8 & 0xFF),
+                                           plane_of(v >> 16 & 0xFF), Pn, a.fast_pred);
+              ++n_exact;
+            } else if constexpr (XF) {
+              // FP32 cannot decide: the exact sign of the reference's FP64
+              // planes decides, as in the FP64 kernel
+              const uint32_t v = g.tv[t];
+              in_conflict = exact_conflict(plane64(v & 0xFF), plane64(v >> 8 & 0xFF),
+                                           plane64(v >> 16 & 0xFF), plane64_of(j), a.fast_pred);
+              ++n_exact;
+            } else {
+              uncertain = true;
+              in_conflict = false;
+            }
+          }
+          cf[q] = in_conflict;
+          if (!in_conflict) {
+            kr2 = fmax(kr2, r2);
+            kme = max(kme, par_old * (int)g.key[t]);
+          }
+        }
+        if (lane == 0) n_tests += (unsigned)valid.popc();
+        if (!kFP64 && !XF && __any_sync(FULL, uncertain)) {
+          st = CELL_RECHECK;
           break;
         }
-        float dw = 0.f;
-        if (S.wf) {
-          const float2 wj = S.wf[j];
-          dw = (wj.x - sc.fw.x) + (wj.y - sc.fw.y);
-        }
-        // (-2 d, |d|^2 + w_i - w_j): the bisector in the seed's frame
-        Pf = make_float4(-2.f * dx, -2.f * dy, -2.f * dz, d2 - dw);
-      }
-      // every clip relinks the reference's valid list in reverse order
-      const int par_old = parity;
-      parity = -parity;
-      if (!valid.any()) continue;  // empty cell: nothing left to clip
-      Real pa1, bw;
-      if constexpr (kFP64) {
-        pa1 = (fabs(Pd.x) + fabs(Pd.y) + fabs(Pd.z)) * 1.0001;
-        bw = Consts<double>::kDot * fabs(Pd.w) * 1.0001;
-      } else {
-        pa1 = (fabsf(Pf.x) + fabsf(Pf.y) + fabsf(Pf.z)) * 1.0001f;
-        // the reference's own FP64 planes carry a rounding of about
-        // 2^-52 (|w_i| + |w_j| + |p_i|^2 + |p_j|^2) in their offset
-        const float wj = S.wf ? S.wf[j].x : 0.f;
-        const float pn = sc.fh.x * sc.fh.x + sc.fh.y * sc.fh.y + sc.fh.z * sc.fh.z;
-        const float qmag = fabsf(sc.fw.x) + fabsf(wj) + 2.f * pn + 1.f;
-        bw = (Consts<float>::kDot * fabsf(Pf.w) + 3.5527137e-15f * qmag) * 1.0001f;
-      }
-      // ---- conflict scan (triangle_is_in_conflict, convex_cell.cpp:870-912)
-      Bits<NWT> conflict;
-      conflict.clear();
-      Real keepR2 = 0;
-      int keep_max_eff = -0x7FFF;
-      bool uncertain = false;
-      auto test = [&](int t) {
-        ++n_tests;
-        Real cx, cy, cz, r2, eps;
-        if constexpr (kFP64) {
-          const double2 xy = sm.cxy[t][tid], zr = sm.czr[t][tid];
-          cx = xy.x;
-          cy = xy.y;
-          cz = zr.x;
-          r2 = zr.y;
-          eps = (double)sm.eps[t][tid];
-        } else {
-          const float4 c = sm.c4[t][tid];
-          cx = c.x;
-          cy = c.y;
-          cz = c.z;
-          eps = c.w;
-          r2 = cx * cx + cy * cy + cz * cz;
-        }
-        Real sv;
-        if constexpr (kFP64) sv = fma(Pd.z, cz, fma(Pd.y, cy, fma(Pd.x, cx, Pd.w)));
-        else sv = fmaf(Pf.z, cz, fmaf(Pf.y, cy, fmaf(Pf.x, cx, Pf.w)));
-        const Real bound = fma(pa1, eps, bw) * (a.fast_pred ? (Real)kFastPredWide : (Real)1);
-        bool in_conflict;
-        if (sv < -bound) {
-          in_conflict = true;
-        } else if (sv > bound) {
-          in_conflict = false;
-        } else {
-          if constexpr (kFP64) {
-            const uint32_t v = sm.tv[t][tid];
-            const double4 p0 = plane_of(v & 0xFF), p1 = plane_of(v >> 8 & 0xFF),
-                          p2 = plane_of(v >> 16 & 0xFF);
-            if (a.fast_pred) {
-              in_conflict = r_det4x4(p0, p1, p2, Pd) > 0.0;
-            } else {
-              const double r0[4] = {p0.x, p0.y, p0.z, p0.w}, r1[4] = {p1.x, p1.y, p1.z, p1.w},
-                           rr2[4] = {p2.x, p2.y, p2.z, p2.w}, r3[4] = {Pd.x, Pd.y, Pd.z, Pd.w};
-              in_conflict = det4_sign_exact(r0, r1, rr2, r3) >= 0;
-            }
-            ++n_exact;
-          } else if constexpr (XF) {
-            // FP32 cannot decide: the exact sign of the reference's FP64
-            // planes decides, as in the FP64 kernel
-            const uint32_t v = sm.tv[t][tid];
-            in_conflict = exact_conflict(plane64(v & 0xFF), plane64(v >> 8 & 0xFF),
-                                         plane64(v >> 16 & 0xFF), plane64_of(j), a.fast_pred);
-            ++n_exact;
-          } else {
-            uncertain = true;
-            in_conflict = false;
-          }
-        }
-        if (in_conflict) {
-          conflict.set(t);
-        } else {
-          keepR2 = fmax(keepR2, r2);
-          keep_max_eff = max(keep_max_eff, par_old * (int)sm.key[t][tid]);
-        }
-      };
+        Bits<NWT> conflict;
+        conflict.clear();
 #pragma unroll
-      for (int wi = 0; wi < NWT; ++wi) {
-        uint64_t m = valid.w[wi];
-        while (m) {
-          // four triangles per iteration, so that their loads overlap
-          const int t0 = wi * 64 + __ffsll((long long)m) - 1;
-          m &= m - 1;
-          int t1 = -1, t2 = -1, t3 = -1;
-          if (m) { t1 = wi * 64 + __ffsll((long long)m) - 1; m &= m - 1; }
-          if (m) { t2 = wi * 64 + __ffsll((long long)m) - 1; m &= m - 1; }
-          if (m) { t3 = wi * 64 + __ffsll((long long)m) - 1; m &= m - 1; }
-          test(t0);
-          if (t1 >= 0) test(t1);
-          if (t2 >= 0) test(t2);
-          if (t3 >= 0) test(t3);
+        for (int q = 0; q < NS; ++q)
+          conflict.w[q >> 1] |= (uint64_t)__ballot_sync(FULL, cf[q]) << (32 * (q & 1));
+        if (!conflict.any()) continue;
+        if (conflict.equals(valid)) {  // the whole cell is clipped away
+          valid.clear();
+          R2 = 0;
+          continue;
         }
-      }
-      if (!kFP64 && uncertain) {
-        st = CELL_RECHECK;
-        break;
-      }
-      if (!conflict.any()) continue;
-      if (conflict.equals(valid)) {  // the whole cell is clipped away
-        valid.clear();
-        R2 = 0;
-        continue;
-      }
-      // ---- a slot for the new plane (recycle planes no triangle uses)
-      const uint64_t pmask = (P >= 64) ? ~0ull : ((1ull << P) - 1ull);
-      uint64_t freep = ~pused & pmask;
-      if (!freep) {
-        uint64_t used = 0;
-        const Bits<NWT> keep = andnot(valid, conflict);
+        const Real keepR2 = warp_maxf(kr2);
+        const int keep_max_eff = __reduce_max_sync(FULL, kme);
+        // ---- a slot for the new plane (recycle planes no triangle uses)
+        const uint64_t pmask = (P >= 64) ? ~0ull : ((1ull << P) - 1ull);
+        uint64_t freep = ~pused & pmask;
+        if (!freep) {
+          uint64_t used = 0;
 #pragma unroll
-        for (int wi = 0; wi < NWT; ++wi) {
-          uint64_t m = keep.w[wi];
-          while (m) {
-            const int t = wi * 64 + __ffsll((long long)m) - 1;
-            m &= m - 1;
-            const uint32_t v = sm.tv[t][tid];
+          for (int q = 0; q < NS; ++q) {
+            const int t = lane + 32 * q;
+            if (!valid.test(t) || cf[q]) continue;
+            const uint32_t v = g.tv[t];
             used |= (1ull << (v & 0xFF)) | (1ull << (v >> 8 & 0xFF)) | (1ull << (v >> 16 & 0xFF));
           }
+          pused = (uint64_t)__reduce_or_sync(FULL, (uint32_t)used) |
+                  ((uint64_t)__reduce_or_sync(FULL, (uint32_t)(used >> 32)) << 32);
+          freep = ~pused & pmask;
+          if (!freep) {
+            st = CELL_OVERFLOW;
+            break;
+          }
         }
-        pused = used;
-        freep = ~pused & pmask;
-        if (!freep) {
+        // list positions are stored in 16 bits (0xFFFF marks a box face):
+        // a plane further down the list sends the cell to the huge-cell
+        // kernel, which keeps them in 32 bits
+        if (jj >= 0xFFFFu) {
           st = CELL_OVERFLOW;
           break;
         }
-      }
-      const uint32_t lv = (uint32_t)(__ffsll((long long)freep) - 1);
-      pused |= 1ull << lv;
-      sm.prank[lv][tid] = (uint16_t)jj;
-      if constexpr (kFP64) sm.pown[lv][tid] = j;
-      else sm.pl[lv][tid] = Pf;
-      // ---- border of the conflict zone (triangulate_conflict_zone)
-      int nborder = 0;
-      uint32_t first_v = 0;
-      int best = -0x7FFFFFFF;
+        const uint32_t lv = (uint32_t)(__ffsll((long long)freep) - 1);
+        pused |= 1ull << lv;
+        if (lane == 0) {
+          g.prank[lv] = (uint16_t)jj;
+          if constexpr (kFP64) g.pown[lv] = j;
+          else g.pl[lv] = Pn;
+        }
+        // ---- border of the conflict zone (triangulate_conflict_zone)
+        int nb_lane = 0;
+        long long best = LLONG_MIN;
 #pragma unroll
-      for (int wi = 0; wi < NWT; ++wi) {
-        uint64_t m = conflict.w[wi];
-        while (m) {
-          const int t = wi * 64 + __ffsll((long long)m) - 1;
-          m &= m - 1;
-          const uint32_t v = sm.tv[t][tid], ad = sm.ta[t][tid];
+        for (int q = 0; q < NS; ++q) {
+          if (!cf[q]) continue;
+          const int t = lane + 32 * q;
+          const uint32_t v = g.tv[t], ad = g.ta[t];
 #pragma unroll
           for (int e = 0; e < 3; ++e) {
             const uint32_t nb = (ad >> (8 * e)) & 0xFF;
@@ -511,144 +617,158 @@ __global__ void __launch_bounds__(kClipThreads) clip_kernel(ClipArgs a) {
             // follows nb's orientation, goes from y = v[e+2] to x = v[e+1]
             const uint32_t x = (v >> (8 * ((e + 1) % 3))) & 0xFF;
             const uint32_t y = (v >> (8 * ((e + 2) % 3))) & 0xFF;
-            const uint32_t an = sm.ta[nb][tid];
+            const uint32_t an = g.ta[nb];
             const uint32_t eb =
                 ((an >> 8 & 0xFF) == (uint32_t)t) + 2 * ((an >> 16 & 0xFF) == (uint32_t)t);
-            sm.pnext[y][tid] = (uint8_t)x;
-            sm.pnb[y][tid] = (uint16_t)(nb | (eb << 8));
-            // the reference starts its walk at the border edge it meets last
-            // while scanning the relinked list (new eff = -old eff)
-            const int score = -par_old * (int)sm.key[nb][tid] * 4 + (int)eb;
-            if (score > best) {
-              best = score;
-              first_v = y;
-            }
-            ++nborder;
+            g.pnext[y] = (uint8_t)x;
+            g.pnb[y] = (uint16_t)(nb | (eb << 8));
+            // the reference starts its walk at the border edge it meets
+            // last while scanning the relinked list (new eff = -old eff);
+            // ties (none occur: keys are distinct) would go to the lowest
+            // (triangle, edge)
+            const int score = -par_old * (int)g.key[nb] * 4 + (int)eb;
+            const long long cand = ((long long)score << 24) |
+                                   ((long long)(0xFFFF - (t * 3 + e)) << 8) | (long long)y;
+            best = max(best, cand);
+            ++nb_lane;
           }
         }
-      }
-      const int nkeep = valid.popc() - conflict.popc();
-      if (nkeep + nborder > T) {
-        st = CELL_OVERFLOW;
-        break;
-      }
-      // ---- fan new triangles (lv, next, v) around the border
-      Bits<NWT> freet = andnot(full_bits<NWT>(T), andnot(valid, conflict));
-      valid = andnot(valid, conflict);
-      R2 = keepR2;
-      const int key_base = -keep_max_eff - 1;
-      uint32_t v = first_v;
-      int prev_t = -1, first_t = -1, created = 0;
-      auto Pv = plane_of(v);
-      do {
-        if (created >= nborder) break;  // not a simple cycle: reported below
-        const uint32_t x = sm.pnext[v][tid];
-        const uint32_t nbinfo = sm.pnb[v][tid];
-        const uint32_t tn = nbinfo & 0xFF, eb = nbinfo >> 8;
-        const int nt = freet.first();
-        freet.reset(nt);
-        valid.set(nt);
-        sm.tv[nt][tid] = lv | (x << 8) | (v << 16);
-        sm.ta[nt][tid] = tn | ((uint32_t)(prev_t < 0 ? 0 : prev_t) << 8);
-        sm.key[nt][tid] = (int16_t)(parity * (key_base - created));
-        {
-          uint32_t an = sm.ta[tn][tid];
-          an = (an & ~(0xFFu << (8 * eb))) | ((uint32_t)nt << (8 * eb));
-          sm.ta[tn][tid] = an;
+        const int nborder = __reduce_add_sync(FULL, nb_lane);
+        const uint32_t first_v = (uint32_t)(warp_max(best) & 0xFF);
+        const int nkeep = valid.popc() - conflict.popc();
+        if (nkeep + nborder > T) {
+          st = CELL_OVERFLOW;
+          break;
         }
-        const auto Px = plane_of(x);
-        Real r2;
-        if constexpr (kFP64) r2 = make_corner(nt, Pd, Px, Pv);
-        else r2 = make_corner(nt, Pf, Px, Pv);
-        R2 = fmax(R2, r2);
-        if (prev_t >= 0) {
-          const uint32_t ap = sm.ta[prev_t][tid];
-          sm.ta[prev_t][tid] = (ap & 0x0000FFFFu) | ((uint32_t)nt << 16);
+        const Bits<NWT> freet = andnot(full_bits<NWT>(T), andnot(valid, conflict));
+        valid = andnot(valid, conflict);
+        R2 = keepR2;
+        const int key_base = -keep_max_eff - 1;
+        if (key_base - nborder < -0x7FFF) {  // keys are stored in 16 bits
+          st = CELL_OVERFLOW;
+          break;
+        }
+        __syncwarp();
+        // ---- the border in walk order: one lane follows it
+        int ok = 1;
+        if (lane == 0) {
+          uint32_t v = first_v;
+          for (int i = 0; i < nborder; ++i) {
+            g.order[i] = (uint8_t)v;
+            v = g.pnext[v];
+            if (v == first_v && i + 1 < nborder) {  // closes early: not a simple cycle
+              ok = 0;
+              break;
+            }
+          }
+          if (v != first_v) ok = 0;
+        }
+        ok = __shfl_sync(FULL, ok, 0);
+        if (!ok) {
+          st = CELL_ERROR;
+          break;
+        }
+        __syncwarp();
+        // ---- fan new triangles (lv, next, v) around the border: the i-th
+        // takes the i-th free slot, its neighbours the slots of i - 1 and
+        // i + 1 along the border
+        Real r2n = 0;
+        for (int i = lane; i < nborder; i += 32) {
+          const uint32_t v = g.order[i];
+          const uint32_t x = g.order[i + 1 < nborder ? i + 1 : 0];
+          const uint32_t nbinfo = g.pnb[v];
+          const uint32_t tn = nbinfo & 0xFF, eb = nbinfo >> 8;
+          const int nt = select_bit(freet, i);
+          const int ntp = select_bit(freet, i > 0 ? i - 1 : nborder - 1);
+          const int ntn = select_bit(freet, i + 1 < nborder ? i + 1 : 0);
+          g.tv[nt] = lv | (x << 8) | (v << 16);
+          g.ta[nt] = tn | ((uint32_t)ntp << 8) | ((uint32_t)ntn << 16);
+          g.key[nt] = (int16_t)(parity * (key_base - i));
+          reinterpret_cast<uint8_t*>(&g.ta[tn])[eb] = (uint8_t)nt;
+          r2n = fmax(r2n, make_corner(nt, Pn, plane_of(x), plane_of(v)));
+        }
+        R2 = fmax(R2, warp_maxf(r2n));
+        or_into(valid, lowest_bits(freet, nborder));
+        if (lane == 0) n_created += (unsigned)nborder;
+        __syncwarp();
+      }
+      if (st < 0) {
+        // list exhausted without certification
+        const bool complete = ((cnt_raw & kCntMask) < a.list_k) || (a.list_k >= a.n_total - 1);
+        if (!a.check_sr) st = CELL_CERTIFIED;
+        else if (copies && cnt == cap) st = (cap == 0) ? CELL_DUPLICATE : CELL_STALLED;
+        else st = complete ? CELL_ALL_NEIGHBOURS : CELL_NEED_MORE_K;
+      }
+    }
+    max_jj = max(max_jj, jj);
+    if (lane == 0) {
+      a.status[s] = st;
+      a.nclip[s] = jj;
+    }
+    if (!(st == CELL_RECHECK || st == CELL_OVERFLOW || st == CELL_NEED_MORE_K ||
+          st == CELL_ERROR)) {
+      // ---- the combinatorics, for the geometry kernel
+      const CombBuf& cb = a.comb;
+      const size_t tb = (size_t)s * kTMax, pb = (size_t)s * kPMax;
+#pragma unroll
+      for (int q = 0; q < NS; ++q) {
+        const int t = lane + 32 * q;
+        if (!valid.test(t)) continue;
+        cb.tv[tb + t] = g.tv[t];
+        cb.ta[tb + t] = g.ta[t];
+        cb.key[tb + t] = g.key[t];
+      }
+      for (int p = lane; p < P; p += 32) {
+        if (!((pused >> p) & 1ull)) continue;
+        const uint16_t rk = g.prank[p];
+        uint32_t own;
+        if constexpr (kFP64) {
+          own = g.pown[p];
         } else {
-          first_t = nt;
+          // box faces only ever occupy their initial slots 0-5
+          own = (rk == 0xFFFF) ? kBoxBase + (uint32_t)p : a.nbr[(size_t)rk * a.nbr_stride + row];
         }
-        prev_t = nt;
-        ++created;
-        ++n_created;
-        v = x;
-        Pv = Px;
-      } while (v != first_v);
-      if (v != first_v || created != nborder) {
-        st = CELL_ERROR;
-        break;
+        cb.pown[pb + p] = own;
+        cb.prank[pb + p] = rk;
       }
-      {
-        const uint32_t ap = sm.ta[prev_t][tid];
-        sm.ta[prev_t][tid] = (ap & 0x0000FFFFu) | ((uint32_t)first_t << 16);
-        const uint32_t af = sm.ta[first_t][tid];
-        sm.ta[first_t][tid] = (af & 0xFFFF00FFu) | ((uint32_t)prev_t << 8);
+      if (lane == 0) {
+        cb.tmask[s] = make_ulonglong2(valid.w[0], NWT > 1 ? valid.w[NWT - 1] : 0ull);
+        cb.pmask[s] = pused;
+        cb.flags[s] = parity < 0 ? 1u : 0u;
       }
     }
-    if (st < 0) {
-      // list exhausted without certification
-      const bool complete = ((cnt_raw & kCntMask) < a.list_k) || (a.list_k >= a.n_total - 1);
-      if (!a.check_sr) st = CELL_CERTIFIED;
-      else if (copies && cnt == cap) st = (cap == 0) ? CELL_DUPLICATE : CELL_STALLED;
-      else st = complete ? CELL_ALL_NEIGHBOURS : CELL_NEED_MORE_K;
-    }
+    __syncwarp();  // the record is reused by the warp's next cell
   }
   if (a.counters) {
-    if (n_exact) atomicAdd(&a.counters[0], n_exact);
-    const unsigned amask = __activemask();
-    const unsigned mx = __reduce_max_sync(amask, jj);
-    const unsigned nt = __reduce_add_sync(amask, n_tests);
-    const unsigned nc = __reduce_add_sync(amask, n_created);
-    if ((unsigned)(tid & 31) == (unsigned)(__ffs(amask) - 1)) {
-      atomicMax(&a.counters[1], (unsigned long long)mx);
-      atomicAdd(&a.counters[2], (unsigned long long)nt);
-      atomicAdd(&a.counters[3], (unsigned long long)nc);
+    const unsigned long long ne = warp_sum(n_exact), nt = warp_sum(n_tests),
+                             nc = warp_sum(n_created);
+    if (lane == 0) {
+      if (ne) atomicAdd(&a.counters[0], ne);
+      atomicMax(&a.counters[1], (unsigned long long)max_jj);
+      atomicAdd(&a.counters[2], nt);
+      atomicAdd(&a.counters[3], nc);
     }
   }
-  a.status[s] = st;
-  a.nclip[s] = jj;
-  if (st == CELL_RECHECK || st == CELL_OVERFLOW || st == CELL_NEED_MORE_K || st == CELL_ERROR)
-    return;
-
-  // ---- the combinatorics, for the geometry kernel
-  const CombBuf& cb = a.comb;
-  const size_t tb = (size_t)s * kTMax, pb = (size_t)s * kPMax;
-#pragma unroll
-  for (int wi = 0; wi < NWT; ++wi) {
-    uint64_t m = valid.w[wi];
-    while (m) {
-      const int t = wi * 64 + __ffsll((long long)m) - 1;
-      m &= m - 1;
-      cb.tv[tb + t] = sm.tv[t][tid];
-      cb.ta[tb + t] = sm.ta[t][tid];
-      cb.key[tb + t] = sm.key[t][tid];
-    }
-  }
-  for (uint64_t m = pused; m; m &= m - 1) {
-    const int p = __ffsll((long long)m) - 1;
-    const uint16_t rk = sm.prank[p][tid];
-    uint32_t own;
-    if constexpr (kFP64) {
-      own = sm.pown[p][tid];
-    } else {
-      // box faces only ever occupy their initial slots 0-5
-      own = (rk == 0xFFFF) ? kBoxBase + (uint32_t)p : a.nbr[(size_t)rk * a.nbr_stride + row];
-    }
-    cb.pown[pb + p] = own;
-    cb.prank[pb + p] = rk;
-  }
-  cb.tmask[s] = make_ulonglong2(valid.w[0], NWT > 1 ? valid.w[NWT - 1] : 0ull);
-  cb.pmask[s] = pused;
-  cb.flags[s] = parity < 0 ? 1u : 0u;
 }
 
 template <typename Real, int T, int P, bool XF>
 static void launch_clip(const ClipArgs& a, cudaStream_t st) {
   if (a.nq == 0) return;
-  const size_t sh = sizeof(CellSmem<Real, kClipThreads, T, P>);
+  const size_t sh = sizeof(CellRec<Real, T, P>) * kClipWarps;
   cudaFuncSetAttribute(clip_kernel<Real, T, P, XF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)sh);
-  const unsigned nb = (a.nq + kClipThreads - 1) / kClipThreads;
-  clip_kernel<Real, T, P, XF><<<nb, kClipThreads, sh, st>>>(a); count_launch();
+  static int resident = 0;  // blocks the device holds at once
+  if (resident == 0) {
+    int per_sm = 0, dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, clip_kernel<Real, T, P, XF>,
+                                                  kClipWarps * 32, sh);
+    resident = std::max(1, per_sm) * std::max(1, sms);
+  }
+  const unsigned need = (a.nq + kClipWarps - 1) / kClipWarps;
+  const unsigned nb = std::min<unsigned>(need, (unsigned)resident);
+  clip_kernel<Real, T, P, XF><<<nb, kClipWarps * 32, sh, st>>>(a); count_launch();
   last_launch_error = cudaGetLastError();
 }
 

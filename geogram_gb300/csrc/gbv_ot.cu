@@ -10,7 +10,12 @@
 // and its Hessian is the graph Laplacian with coefficients
 // A_ij / (2 |p_i - p_j|) over the Laguerre facets.
 //
-// Reductions are deterministic: fixed partition, Neumaier compensated sums.
+// Reductions are deterministic: every block sums a fixed part of the
+// vector in a fixed order and a fixed tree, and the partial sums are added
+// in a fixed order.  FP64 instructions are the scarce resource on this part
+// (their pipe, not memory, bounds the CG kernels), so the kernels keep them
+// few: plain sums instead of compensated ones, one row per thread in the
+// product, the Jacobi preconditioner as a product by the inverse diagonal.
 #include <cfloat>
 
 #include "gbv_common.cuh"
@@ -19,29 +24,51 @@
 namespace gbv {
 
 constexpr int kOtThreads = 256;
+constexpr int kOtWarps = kOtThreads / 32;
 
-__device__ __forceinline__ void neu_add(double& s, double& c, double x) {
-  const double t = s + x;
-  if (fabs(s) >= fabs(x)) c += (s - t) + x;
-  else c += (x - t) + s;
-  s = t;
+// Sum of v over the block, in a fixed tree; the result in thread 0.
+__device__ __forceinline__ double block_sum(double v) {
+  __shared__ double ws[kOtWarps];
+  const unsigned FULL = 0xFFFFFFFFu;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
+  __syncthreads();  // ws may still be read by a previous call
+  if (lane == 0) ws[warp] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (warp == 0) {
+    t = lane < kOtWarps ? ws[lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(FULL, t, o);
+  }
+  return t;
 }
 
-// Block-level combination of per-thread (s, c) pairs into part[2*block].
-__device__ __forceinline__ void block_combine(double s, double c, double* part) {
-  __shared__ double ss[kOtThreads], sc[kOtThreads];
-  ss[threadIdx.x] = s;
-  sc[threadIdx.x] = c;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double S = 0.0, C = 0.0;
-    for (int t = 0; t < kOtThreads; ++t) {
-      neu_add(S, C, ss[t]);
-      C += sc[t];
-    }
-    part[2 * blockIdx.x] = S;
-    part[2 * blockIdx.x + 1] = C;
+// Same for max / min (results in thread 0).
+template <bool kMax>
+__device__ __forceinline__ double block_ext(double v) {
+  __shared__ double ws[kOtWarps];
+  const unsigned FULL = 0xFFFFFFFFu;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const double u = __shfl_down_sync(FULL, v, o);
+    v = kMax ? fmax(v, u) : fmin(v, u);
   }
+  __syncthreads();
+  if (lane == 0) ws[warp] = v;
+  __syncthreads();
+  double t = v;
+  if (warp == 0) {
+    t = ws[lane < kOtWarps ? lane : 0];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double u = __shfl_down_sync(FULL, t, o);
+      t = kMax ? fmax(t, u) : fmin(t, u);
+    }
+  }
+  return t;
 }
 
 // ---------------------------------------------------------------------
@@ -49,7 +76,8 @@ __device__ __forceinline__ void block_combine(double s, double c, double* part) 
 // ---------------------------------------------------------------------
 __global__ void hessian_kernel(const double* __restrict__ xyz, const uint32_t* __restrict__ rowptr,
                                const uint32_t* __restrict__ col, const double* __restrict__ area,
-                               uint32_t n, double* __restrict__ val, double* __restrict__ diag) {
+                               uint32_t n, double* __restrict__ val, double* __restrict__ diag,
+                               double* __restrict__ invd) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double xi = xyz[3 * (size_t)i], yi = xyz[3 * (size_t)i + 1], zi = xyz[3 * (size_t)i + 2];
@@ -76,6 +104,35 @@ __global__ void hessian_kernel(const double* __restrict__ xyz, const uint32_t* _
     d += c;
   }
   diag[i] = d;
+  invd[i] = d > 0.0 ? 1.0 / d : 1.0;
+}
+
+// Slice widths of the sliced-ELL copy: 32 times the longest row of each
+// slice of 32 rows (one warp per slice).
+__global__ void sell_width_kernel(const uint32_t* __restrict__ rowptr, uint32_t n, uint32_t nsl,
+                                  uint32_t* __restrict__ sl_off) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t deg = i < n ? rowptr[i + 1] - rowptr[i] : 0u;
+  const uint32_t w = __reduce_max_sync(0xFFFFFFFFu, deg);
+  if ((threadIdx.x & 31) == 0 && (i >> 5) < nsl) sl_off[i >> 5] = 32u * w;
+}
+
+// Row i of the CSR into its slice: entry k at sl_off[s] + 32 k + lane; rows
+// shorter than the slice are padded with zeros on their own column.
+__global__ void sell_pack_kernel(const uint32_t* __restrict__ rowptr,
+                                 const uint32_t* __restrict__ col, const double* __restrict__ val,
+                                 const uint32_t* __restrict__ sl_off, uint32_t n,
+                                 uint32_t* __restrict__ s_col, double* __restrict__ s_val) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t s = i >> 5, lane = i & 31;
+  const uint32_t base = sl_off[s], w = (sl_off[s + 1] - base) >> 5;
+  const uint32_t b = rowptr[i], deg = rowptr[i + 1] - b;
+  for (uint32_t k = 0; k < w; ++k) {
+    const size_t pos = (size_t)base + 32u * k + lane;
+    s_col[pos] = k < deg ? col[b + k] : i;
+    s_val[pos] = k < deg ? val[b + k] : 0.0;
+  }
 }
 
 void assemble_hessian(const double* xyz, const uint32_t* rowptr, const uint32_t* col,
@@ -83,44 +140,25 @@ void assemble_hessian(const double* xyz, const uint32_t* rowptr, const uint32_t*
   H.rowptr = rowptr;
   H.col = col;
   H.n = n;
-  hessian_kernel<<<(n + kOtThreads - 1) / kOtThreads, kOtThreads, 0, st>>>(xyz, rowptr, col, area,
-                                                                          n, H.val, H.diag); count_launch();
+  hessian_kernel<<<(n + kOtThreads - 1) / kOtThreads, kOtThreads, 0, st>>>(
+      xyz, rowptr, col, area, n, H.val, H.diag, H.invd); count_launch();
 }
 
-// ---------------------------------------------------------------------
-// y = H x, 8 lanes per row, with the partial sums of x . y
-// ---------------------------------------------------------------------
-constexpr int kRowLanes = 8;
+uint32_t sell_slices(uint32_t n) { return (n + 31) / 32; }
 
-__global__ void spmv_dot_kernel(const uint32_t* __restrict__ rowptr,
-                                const uint32_t* __restrict__ col, const double* __restrict__ val,
-                                const double* __restrict__ diag, const double* __restrict__ x,
-                                uint32_t n, double* __restrict__ y, double* __restrict__ part) {
-  const int sub = threadIdx.x & (kRowLanes - 1);
-  const unsigned FULL = 0xFFFFFFFFu;
-  double s = 0.0, cc = 0.0;
-  const uint32_t rows_per_block = kOtThreads / kRowLanes;
-  for (uint32_t base = blockIdx.x * rows_per_block; base < n; base += gridDim.x * rows_per_block) {
-    const uint32_t i = base + threadIdx.x / kRowLanes;
-    double acc = 0.0;
-    if (i < n)
-      for (uint32_t k = rowptr[i] + sub; k < rowptr[i + 1]; k += kRowLanes) acc += val[k] * x[col[k]];
-    // fixed reduction tree inside the 8-lane group
-#pragma unroll
-    for (int o = kRowLanes / 2; o > 0; o >>= 1) acc += __shfl_down_sync(FULL, acc, o, kRowLanes);
-    if (sub == 0 && i < n) {
-      const double yi = diag[i] * x[i] + acc;
-      y[i] = yi;
-      neu_add(s, cc, x[i] * yi);
-    }
-  }
-  block_combine(s, cc, part);
+void sell_widths(const Hessian& H, uint32_t* sl_off, cudaStream_t st) {
+  const uint32_t nsl = sell_slices(H.n), threads = nsl * 32u;
+  sell_width_kernel<<<(threads + kOtThreads - 1) / kOtThreads, kOtThreads, 0, st>>>(
+      H.rowptr, H.n, nsl, sl_off); count_launch();
 }
 
-void spmv_dot(const Hessian& H, const double* x, double* y, double* part, int nparts,
-              cudaStream_t st) {
-  spmv_dot_kernel<<<nparts, kOtThreads, 0, st>>>(H.rowptr, H.col, H.val, H.diag, x, H.n, y,
-                                                 part); count_launch();
+void sell_pack(Hessian& H, const uint32_t* sl_off, uint32_t* s_col, double* s_val,
+               cudaStream_t st) {
+  H.sl_off = sl_off;
+  H.s_col = s_col;
+  H.s_val = s_val;
+  sell_pack_kernel<<<(H.n + kOtThreads - 1) / kOtThreads, kOtThreads, 0, st>>>(
+      H.rowptr, H.col, H.val, sl_off, H.n, s_col, s_val); count_launch();
 }
 
 // ---------------------------------------------------------------------
@@ -128,43 +166,43 @@ void spmv_dot(const Hessian& H, const double* x, double* y, double* part, int np
 // ---------------------------------------------------------------------
 __global__ void dot_kernel(const double* __restrict__ a, const double* __restrict__ b, uint32_t n,
                            double* __restrict__ part) {
-  double s = 0.0, c = 0.0;
+  double s = 0.0;
   const uint32_t chunk = (n + gridDim.x - 1) / gridDim.x;
   const uint32_t lo = blockIdx.x * chunk, hi = min(n, lo + chunk);
-  for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x) neu_add(s, c, a[i] * b[i]);
-  block_combine(s, c, part);
+  for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x) s = fma(a[i], b[i], s);
+  s = block_sum(s);
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = s;
+    part[2 * blockIdx.x + 1] = 0.0;
+  }
 }
 
 void dot_parts(const double* a, const double* b, uint32_t n, double* part, cudaStream_t st) {
   dot_kernel<<<kOtParts, kOtThreads, 0, st>>>(a, b, n, part); count_launch();
 }
 
-// part layout: [2*kOtParts] sum of r^2 (s, c pairs), then per block
+// part layout: [2*kOtParts] sum of r^2 ((s, 0) pairs), then per block
 // max |r_i|/nu_i at [2*kOtParts + b] and min vol at [3*kOtParts + b].
 __global__ void residual_kernel(const double* __restrict__ vol, const double* __restrict__ nu,
                                 uint32_t n, double* __restrict__ r, double* __restrict__ part) {
-  __shared__ double smax[kOtThreads], smin[kOtThreads];
-  double s = 0.0, c = 0.0, mx = 0.0, mn = DBL_MAX;
+  double s = 0.0, mx = 0.0, mn = DBL_MAX;
   const uint32_t chunk = (n + gridDim.x - 1) / gridDim.x;
   const uint32_t lo = blockIdx.x * chunk, hi = min(n, lo + chunk);
   for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
     const double ri = vol[i] - nu[i];
     r[i] = ri;
-    neu_add(s, c, ri * ri);
+    s = fma(ri, ri, s);
     mx = fmax(mx, fabs(ri) / nu[i]);
     mn = fmin(mn, vol[i]);
   }
-  smax[threadIdx.x] = mx;
-  smin[threadIdx.x] = mn;
-  block_combine(s, c, part);
+  s = block_sum(s);
+  mx = block_ext<true>(mx);
+  mn = block_ext<false>(mn);
   if (threadIdx.x == 0) {
-    double M = 0.0, m = DBL_MAX;
-    for (int t = 0; t < kOtThreads; ++t) {
-      M = fmax(M, smax[t]);
-      m = fmin(m, smin[t]);
-    }
-    part[2 * kOtParts + blockIdx.x] = M;
-    part[3 * kOtParts + blockIdx.x] = m;
+    part[2 * blockIdx.x] = s;
+    part[2 * blockIdx.x + 1] = 0.0;
+    part[2 * kOtParts + blockIdx.x] = mx;
+    part[3 * kOtParts + blockIdx.x] = mn;
   }
 }
 
@@ -173,27 +211,10 @@ void residual(const double* vol, const double* nu, uint32_t n, double* r, double
   residual_kernel<<<kOtParts, kOtThreads, 0, st>>>(vol, nu, n, r, part); count_launch();
 }
 
-__global__ void cg_xr_kernel(double* __restrict__ x, double* __restrict__ r,
-                             const double* __restrict__ p, const double* __restrict__ Ap,
-                             double alpha, uint32_t n) {
+__global__ void precond_kernel(const double* __restrict__ r, const double* __restrict__ invd,
+                               double* __restrict__ z, uint32_t n) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  x[i] = fma(alpha, p[i], x[i]);
-  r[i] = fma(-alpha, Ap[i], r[i]);
-}
-
-__global__ void cg_precond_kernel(const double* __restrict__ r, const double* __restrict__ diag,
-                                  double* __restrict__ z, uint32_t n) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const double d = diag[i];
-  z[i] = d > 0.0 ? r[i] / d : r[i];
-}
-
-__global__ void cg_p_kernel(double* __restrict__ p, const double* __restrict__ z, double beta,
-                            uint32_t n) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) p[i] = fma(beta, p[i], z[i]);
+  if (i < n) z[i] = r[i] * invd[i];
 }
 
 __global__ void axpy_kernel(double* __restrict__ y, const double* __restrict__ x, double alpha,
@@ -215,15 +236,8 @@ __global__ void scale_copy_kernel(double* __restrict__ y, const double* __restri
 
 static inline unsigned nb(uint32_t n) { return (n + kOtThreads - 1) / kOtThreads; }
 
-void cg_update_xr(double* x, double* r, const double* p, const double* Ap, double alpha,
-                  uint32_t n, cudaStream_t st) {
-  cg_xr_kernel<<<nb(n), kOtThreads, 0, st>>>(x, r, p, Ap, alpha, n); count_launch();
-}
-void cg_precond(const double* r, const double* diag, double* z, uint32_t n, cudaStream_t st) {
-  cg_precond_kernel<<<nb(n), kOtThreads, 0, st>>>(r, diag, z, n); count_launch();
-}
-void cg_update_p(double* p, const double* z, double beta, uint32_t n, cudaStream_t st) {
-  cg_p_kernel<<<nb(n), kOtThreads, 0, st>>>(p, z, beta, n); count_launch();
+void cg_precond(const double* r, const double* invd, double* z, uint32_t n, cudaStream_t st) {
+  precond_kernel<<<nb(n), kOtThreads, 0, st>>>(r, invd, z, n); count_launch();
 }
 void axpy(double* y, const double* x, double alpha, uint32_t n, cudaStream_t st) {
   axpy_kernel<<<nb(n), kOtThreads, 0, st>>>(y, x, alpha, n); count_launch();
@@ -238,165 +252,136 @@ void scale_copy(double* y, const double* x, double alpha, uint32_t n, cudaStream
 // ---------------------------------------------------------------------
 // Device-resident preconditioned CG
 // ---------------------------------------------------------------------
-// (s, c) pairs added in a fixed order: a Neumaier sum of the s parts, the
-// c parts summed alongside.
-__device__ __forceinline__ void pair_add(double& s, double& c, double s2, double c2) {
-  neu_add(s, c, s2);
-  c += c2;
+// The last block of a launch to finish: every block has stored its partial
+// (thread 0, before the fence) when the ticket reaches gridDim.x - 1.  The
+// last block resets the ticket for the next launch.
+__device__ __forceinline__ bool last_block(uint32_t* ticket) {
+  __shared__ bool am_last;
+  __threadfence();
+  if (threadIdx.x == 0) am_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  __syncthreads();
+  return am_last;
 }
 
-// Fixed-order tree over the warp, then over the block's warps: the (s, c)
-// pair of the whole block in thread 0 (blockDim.x a multiple of 32, <= 1024).
-__device__ __forceinline__ void block_pair(double& s, double& c) {
-  __shared__ double ws[32], wc[32];
-  const unsigned FULL = 0xFFFFFFFFu;
+// Sum of part[stride * b + off], b < nparts, in a fixed order (thread t adds
+// parts t, t + 256, ... then the block tree); result in thread 0.  The
+// partials of the other blocks are read from L2.
+__device__ __forceinline__ double sum_parts(const double* part, int nparts, int stride, int off) {
+  double v = 0.0;
+  for (int b = threadIdx.x; b < nparts; b += blockDim.x) v += __ldcg(&part[stride * b + off]);
+  return block_sum(v);
+}
+
+// Rows of one block: a contiguous run of slices, the same in every launch.
+struct SliceRange {
+  uint32_t lo, hi;
+};
+__device__ __forceinline__ SliceRange block_slices(uint32_t n) {
+  const uint32_t nsl = (n + 31) / 32, ngrp = (nsl + kOtWarps - 1) / kOtWarps;
+  const uint32_t per = (ngrp + gridDim.x - 1) / gridDim.x;
+  const uint32_t g0 = min(ngrp, blockIdx.x * per), g1 = min(ngrp, g0 + per);
+  return {g0 * kOtWarps, min(nsl, g1 * kOtWarps)};
+}
+
+// Ap = H p on the sliced-ELL copy, one row per thread (a warp per slice);
+// the block's share of p . Ap to part[b]; the last block sets
+// alpha = rz / pAp (done if pAp <= 0).
+__global__ void __launch_bounds__(kOtThreads)
+pcg_spmv_kernel(const uint32_t* __restrict__ sl_off, const uint32_t* __restrict__ s_col,
+                const double* __restrict__ s_val, const double* __restrict__ diag,
+                const double* __restrict__ p, uint32_t n, double* __restrict__ Ap,
+                double* __restrict__ part, CgScalars* __restrict__ sc) {
+  if (sc->done) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    const double s2 = __shfl_down_sync(FULL, s, o), c2 = __shfl_down_sync(FULL, c, o);
-    if (lane < o) pair_add(s, c, s2, c2);
-  }
-  __syncthreads();  // ws/wc may still be read by a previous call
-  if (lane == 0) {
-    ws[warp] = s;
-    wc[warp] = c;
-  }
-  __syncthreads();
-  if (warp == 0) {
-    const int nw = blockDim.x >> 5;
-    s = lane < nw ? ws[lane] : 0.0;
-    c = lane < nw ? wc[lane] : 0.0;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const double s2 = __shfl_down_sync(FULL, s, o), c2 = __shfl_down_sync(FULL, c, o);
-      if (lane < o) pair_add(s, c, s2, c2);
-    }
-  }
-}
-
-// Sum of the partial pairs part[stride * b + off], b < nparts, the same in
-// every block: each lane of warp 0 adds a fixed stretch, then a fixed tree;
-// the result is broadcast through shared memory.
-__device__ __forceinline__ double sum_parts(const double* __restrict__ part, int nparts,
-                                            int stride, int off) {
-  __shared__ double res;
-  __syncthreads();  // res may still be read after a previous call
-  if (threadIdx.x < 32) {
-    const int lane = threadIdx.x;
-    const int per = (nparts + 31) / 32;
-    double s = 0.0, c = 0.0;
-    for (int b = lane * per; b < min(nparts, (lane + 1) * per); ++b)
-      pair_add(s, c, part[stride * b + off], part[stride * b + off + 1]);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const double s2 = __shfl_down_sync(0xFFFFFFFFu, s, o);
-      const double c2 = __shfl_down_sync(0xFFFFFFFFu, c, o);
-      if (lane < o) pair_add(s, c, s2, c2);
-    }
-    if (lane == 0) res = s + c;
-  }
-  __syncthreads();
-  return res;
-}
-
-// Ap = H p, partial pairs of p . Ap to part[2 b]; 8 lanes per row.
-__global__ void __launch_bounds__(kOtThreads)
-pcg_spmv_kernel(const uint32_t* __restrict__ rowptr, const uint32_t* __restrict__ col,
-                const double* __restrict__ val, const double* __restrict__ diag,
-                const double* __restrict__ x, uint32_t n, double* __restrict__ y,
-                double* __restrict__ part, const CgScalars* __restrict__ sc) {
-  if (sc->done) return;
-  const int sub = threadIdx.x & (kRowLanes - 1);
-  const unsigned FULL = 0xFFFFFFFFu;
-  double s = 0.0, cc = 0.0;
-  const uint32_t rows_per_block = kOtThreads / kRowLanes;
-  const uint32_t nblk = (n + rows_per_block - 1) / rows_per_block;
-  const uint32_t per = (nblk + gridDim.x - 1) / gridDim.x;  // contiguous row blocks
-  for (uint32_t rb = blockIdx.x * per; rb < min(nblk, (blockIdx.x + 1) * per); ++rb) {
-    const uint32_t i = rb * rows_per_block + threadIdx.x / kRowLanes;
+  const SliceRange R = block_slices(n);
+  double s = 0.0;
+  for (uint32_t sl = R.lo + warp; sl < R.hi; sl += kOtWarps) {
+    const uint32_t i = sl * 32 + lane;
+    const uint32_t base = sl_off[sl], w = (sl_off[sl + 1] - base) >> 5;
+    if (i >= n) continue;
     double acc = 0.0;
-    if (i < n)
-      for (uint32_t k = rowptr[i] + sub; k < rowptr[i + 1]; k += kRowLanes) acc += val[k] * x[col[k]];
-#pragma unroll
-    for (int o = kRowLanes / 2; o > 0; o >>= 1) acc += __shfl_down_sync(FULL, acc, o, kRowLanes);
-    if (sub == 0 && i < n) {
-      const double yi = diag[i] * x[i] + acc;
-      y[i] = yi;
-      neu_add(s, cc, x[i] * yi);
-    }
+    const uint32_t* cp = s_col + base + lane;
+    const double* vp = s_val + base + lane;
+    for (uint32_t k = 0; k < w; ++k) acc = fma(vp[32 * k], p[cp[32 * k]], acc);
+    const double pi = p[i];
+    const double yi = fma(diag[i], pi, acc);
+    Ap[i] = yi;
+    s = fma(pi, yi, s);
   }
-  block_pair(s, cc);
+  s = block_sum(s);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+  if (!last_block(&sc->ticket)) return;
+  const double pAp = sum_parts(part, gridDim.x, 1, 0);
   if (threadIdx.x == 0) {
-    part[2 * blockIdx.x] = s;
-    part[2 * blockIdx.x + 1] = cc;
+    if (pAp > 0.0) sc->alpha = sc->rz / pAp;
+    else sc->done = 1;
+    sc->ticket = 0;
   }
 }
 
-// alpha = rz / pAp; x += alpha p; r -= alpha Ap; z = r / diag; partial
-// pairs of r . r and r . z to part_b[4 b .. 4 b + 3].
+// x += alpha p; r -= alpha Ap; z = r / diag; the block's shares of r . r
+// and r . z to part[2 b], part[2 b + 1]; the last block sets beta =
+// rz' / rz, rz = rz', counts the iteration and stops at rr <= tol2 b2.
 __global__ void __launch_bounds__(kOtThreads)
-pcg_xr_kernel(const double* __restrict__ part_a, double* __restrict__ x, double* __restrict__ r,
-              const double* __restrict__ p, const double* __restrict__ Ap,
-              const double* __restrict__ diag, double* __restrict__ z, uint32_t n,
-              double* __restrict__ part_b, CgScalars* __restrict__ sc, uint32_t k) {
+pcg_xr_kernel(double* __restrict__ x, double* __restrict__ r, const double* __restrict__ p,
+              const double* __restrict__ Ap, const double* __restrict__ invd,
+              double* __restrict__ z, uint32_t n, double* __restrict__ part,
+              CgScalars* __restrict__ sc) {
   if (sc->done) return;
-  const double pAp = sum_parts(part_a, gridDim.x, 2, 0);
-  if (!(pAp > 0.0)) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) sc->done = 1;
-    return;
-  }
-  const double alpha = sc->rz[k & 1] / pAp;
-  const uint32_t chunk = (n + gridDim.x - 1) / gridDim.x;
-  const uint32_t lo = blockIdx.x * chunk, hi = min(n, lo + chunk);
-  double s1 = 0.0, c1 = 0.0, s2 = 0.0, c2 = 0.0;
+  const double alpha = sc->alpha;
+  const SliceRange R = block_slices(n);
+  const uint32_t lo = R.lo * 32, hi = min(n, R.hi * 32);
+  double rr = 0.0, rz = 0.0;
   for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
     x[i] = fma(alpha, p[i], x[i]);
     const double ri = fma(-alpha, Ap[i], r[i]);
     r[i] = ri;
-    const double d = diag[i];
-    const double zi = d > 0.0 ? ri / d : ri;
+    const double zi = ri * invd[i];
     z[i] = zi;
-    neu_add(s1, c1, ri * ri);
-    neu_add(s2, c2, ri * zi);
+    rr = fma(ri, ri, rr);
+    rz = fma(ri, zi, rz);
   }
-  block_pair(s1, c1);
-  block_pair(s2, c2);
+  rr = block_sum(rr);
+  rz = block_sum(rz);
   if (threadIdx.x == 0) {
-    part_b[4 * blockIdx.x] = s1;
-    part_b[4 * blockIdx.x + 1] = c1;
-    part_b[4 * blockIdx.x + 2] = s2;
-    part_b[4 * blockIdx.x + 3] = c2;
+    part[2 * blockIdx.x] = rr;
+    part[2 * blockIdx.x + 1] = rz;
+  }
+  if (!last_block(&sc->ticket)) return;
+  const double rr_t = sum_parts(part, gridDim.x, 2, 0);
+  const double rz_t = sum_parts(part, gridDim.x, 2, 1);
+  if (threadIdx.x == 0) {
+    sc->beta = rz_t / sc->rz;
+    sc->rz = rz_t;
+    sc->k += 1;
+    if (rr_t <= sc->tol2 * sc->b2) sc->done = 1;
+    sc->ticket = 0;
   }
 }
 
-// beta = rz' / rz; p = z + beta p; block 0 records rz', the iteration and
-// convergence.
+// p = z + beta p.
 __global__ void __launch_bounds__(kOtThreads)
-pcg_p_kernel(const double* __restrict__ part_b, double* __restrict__ p,
-             const double* __restrict__ z, uint32_t n, CgScalars* __restrict__ sc, uint32_t k) {
+pcg_p_kernel(double* __restrict__ p, const double* __restrict__ z, uint32_t n,
+             const CgScalars* __restrict__ sc) {
   if (sc->done) return;
-  const double rr = sum_parts(part_b, gridDim.x, 4, 0);
-  const double rz_new = sum_parts(part_b, gridDim.x, 4, 2);
-  const double beta = rz_new / sc->rz[k & 1];
-  const uint32_t chunk = (n + gridDim.x - 1) / gridDim.x;
-  const uint32_t lo = blockIdx.x * chunk, hi = min(n, lo + chunk);
-  for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x) p[i] = fma(beta, p[i], z[i]);
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    sc->rz[(k + 1) & 1] = rz_new;
-    sc->k = k + 1;
-    if (rr <= sc->tol2 * sc->b2) sc->done = 1;
-  }
+  const double beta = sc->beta;
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = fma(beta, p[i], z[i]);
+}
+
+uint32_t pcg_blocks(uint32_t n) {
+  const uint32_t ngrp = ((n + 31) / 32 + kOtWarps - 1) / kOtWarps;
+  return ngrp < (uint32_t)kPcgParts ? (ngrp > 0 ? ngrp : 1u) : (uint32_t)kPcgParts;
 }
 
 void pcg_iterations(const Hessian& H, double* x, double* r, double* p, double* Ap, double* z,
-                    double* part_a, double* part_b, CgScalars* sc, uint32_t k0, uint32_t count,
-                    cudaStream_t st) {
+                    double* part, CgScalars* sc, uint32_t count, cudaStream_t st) {
+  const uint32_t G = pcg_blocks(H.n);
   for (uint32_t j = 0; j < count; ++j) {
-    pcg_spmv_kernel<<<kPcgParts, kOtThreads, 0, st>>>(H.rowptr, H.col, H.val, H.diag, p, H.n,
-                                                      Ap, part_a, sc); count_launch();
-    pcg_xr_kernel<<<kPcgParts, kOtThreads, 0, st>>>(part_a, x, r, p, Ap, H.diag, z, H.n,
-                                                    part_b, sc, k0 + j); count_launch();
-    pcg_p_kernel<<<kPcgParts, kOtThreads, 0, st>>>(part_b, p, z, H.n, sc, k0 + j); count_launch();
+    pcg_spmv_kernel<<<G, kOtThreads, 0, st>>>(H.sl_off, H.s_col, H.s_val, H.diag, p, H.n, Ap,
+                                              part, sc); count_launch();
+    pcg_xr_kernel<<<G, kOtThreads, 0, st>>>(x, r, p, Ap, H.invd, z, H.n, part, sc); count_launch();
+    pcg_p_kernel<<<nb(H.n), kOtThreads, 0, st>>>(p, z, H.n, sc); count_launch();
   }
 }
 
