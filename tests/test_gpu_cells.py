@@ -191,3 +191,47 @@ def test_fast_predicates_and_walk_vs_reference(g, name, prec):
     c = g.compute_cells(ref["x"], ref["w"], precision=prec,
                         predicates="exact" if bool(ref["exact"]) else "fast")
     assert_cells_equal(c, ref)
+
+
+def _far_cutter_case():
+    """Seed 0 at (0.3, 0.3, 0.3) with 65,600 seeds packed in [0, 0.1]^3
+    behind a guard layer (363 seeds on the faces x, y, z = 0.11) and seed 1
+    at (0.9, 0.9, 0.9): seed 0's cell reaches the far corner until seed 1
+    cuts it, and seed 1 is the 65,963rd seed of its list."""
+    rng = np.random.default_rng(5)
+    g1 = np.arange(11) * 0.01 + 0.005
+    a, b = np.meshgrid(g1, g1, indexing="ij")
+    face = np.stack([np.full(a.size, 0.11), a.ravel(), b.ravel()], 1)
+    guards = np.concatenate([face, face[:, [1, 0, 2]], face[:, [1, 2, 0]]])
+    x = np.concatenate([[[0.3, 0.3, 0.3], [0.9, 0.9, 0.9]], rng.random((65600, 3)) * 0.1, guards])
+    return x
+
+
+@pytest.fixture(scope="module")
+def far_cutter(oracle_mod):
+    x = _far_cutter_case()
+    pc = oracle_mod.PreparedCells(x, None)
+    try:
+        r = pc.range(0, 2, 8, max_nbr=4096)
+    finally:
+        pc.close()
+    return x, r
+
+
+@pytest.mark.parametrize("prec", PRECISIONS)
+def test_cutting_plane_beyond_16_bit_list_positions(g, far_cutter, prec):
+    """Planes are kept with their 16-bit list position in the fixed-shape
+    clipping kernels; a cell cut by a seed further down its list goes to the
+    huge-cell kernel and must come out as the oracle's (cells 0 and 1: 364
+    and 1 facets, all 65,964 other seeds clipped)."""
+    x, r = far_cutter
+    c = g.compute_cells(x, precision=prec)
+    for k in range(2):
+        m = int(r["cnt"][k])
+        assert np.array_equal(c.neighbors[c.rowptr[k]:c.rowptr[k + 1]], r["nidx"][k * 4096:k * 4096 + m])
+        assert np.array_equal(c.facet_area[c.rowptr[k]:c.rowptr[k + 1]],
+                              r["narea"][k * 4096:k * 4096 + m])
+        assert c.volume[k] == r["vol"][k]
+        assert np.array_equal(c.mg[k], r["mg"][3 * k:3 * k + 3])
+    assert 1 in c.neighbors[c.rowptr[0]:c.rowptr[1]]
+    assert abs(c.volume.sum() - 1.0) < 1e-9
