@@ -23,7 +23,7 @@ the seeds.  --impl reference times that CPU implementation alone on the
 same workload.  `c2_lloyd10` runs the workload's ten Lloyd iterations;
 `c1` the 100k-seed Voronoi diagram in FP64 with one Lloyd step.  `ot` adds
 the optimal-transport half of the headline metric: solve time from zero
-weights and from the starts (--ot-n seeds of the clustered mixture,
+weights and from the starts (learned, multilevel, separable) (--ot-n seeds of the clustered mixture,
 1,000,000 by default); its `cpu_baseline` times the CPU restatement of the
 solver (oracle/ot.py) on --ot-cpu-n seeds of the same mixture with the GPU
 solver on the same seeds beside it.
@@ -486,17 +486,25 @@ def run_ot(n: int, ctx) -> dict:
     w3 = torch.empty(n, dtype=torch.float64, device="cuda")
     rv, tv = timed(lambda: g.ot_solve_levels_device(x, w3, ratio=8, min_level=20000, tol=1e-6,
                                                     ctx=ctx))
+
+    def separable():
+        w4 = g.ot_separable_start_device(x, ctx=ctx)
+        return g.ot_solve_device(x, w4, tol=1e-6, ctx=ctx)
+    rs, ts = timed(separable)
     plain = {k: rp[k] for k in keys}
     plain["seconds"] = tp
     learned = {k: rl[k] for k in keys}
     learned.update(seconds=tl, start_ms=rl["ms_start"], start_scale=rl["start_scale"])
     levels = {k: rv[k] for k in keys}
     levels.update(seconds=tv, levels=rv["levels"], start_scale=rv["start_scale"])
+    sep = {k: rs[k] for k in keys}
+    sep.update(seconds=ts, start_scale=rs["start_scale"])
     return {"workload": f"OT of {n} seeds, 8-component Gaussian mixture (means U[0.2,0.8]^3, "
                         "sigma 0.05, seed 0) to the uniform measure on the unit cube, "
                         "relative mass error 1e-6",
             "n": n, "plain": plain, "learned_start": learned, "speedup": tp / tl,
-            "multilevel": levels, "multilevel_speedup": tp / tv}
+            "multilevel": levels, "multilevel_speedup": tp / tv,
+            "separable_start": sep, "separable_speedup": tp / ts}
 
 
 def ot_cpu_baseline(n: int, ctx) -> dict:

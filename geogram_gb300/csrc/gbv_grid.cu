@@ -1133,6 +1133,7 @@ knn_tile_kernel(KnnArgs a, SortedSeeds S, const GridDesc* __restrict__ gdp,
   const float h2f = g.h_f * g.h_f;
   uint2* mybuf = s_buf + lane;  // entry j at mybuf[32 * j]
   uint32_t bn = 0;
+  bool searching = active;  // the lane still takes offers in this sweep
 
   // Offers the seeds of up to 32 nodes (one per lane: first slot b, count
   // n) to every query, 32 at a time.
@@ -1169,7 +1170,7 @@ knn_tile_kernel(KnnArgs a, SortedSeeds S, const GridDesc* __restrict__ gdp,
         const float dx = p.x - c.qf.x, dy = p.y - c.qf.y, dz = p.z - c.qf.z,
                     dh = p.w - c.qf.w;
         const float d32 = dx * dx + dy * dy + dz * dz + dh * dh;
-        if (active && d32 < thr) {
+        if (searching && d32 < thr) {
           mybuf[32 * bn] = make_uint2(__float_as_uint(d32), s_sl[t]);
           ++bn;
         }
@@ -1182,7 +1183,7 @@ knn_tile_kernel(KnnArgs a, SortedSeeds S, const GridDesc* __restrict__ gdp,
       }
       bn = 0;
     }
-    wthr = active ? thr : 0.f;
+    wthr = searching ? thr : 0.f;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) wthr = fmaxf(wthr, __shfl_xor_sync(FULL, wthr, o));
   };
@@ -1197,6 +1198,12 @@ knn_tile_kernel(KnnArgs a, SortedSeeds S, const GridDesc* __restrict__ gdp,
     n = S.cell_start[(code + 1u) << (3 * tsh)] - b;
   };
 
+  // A lane that finds fewer than cap seeds within its first pruning
+  // distance (a query near the domain's boundary, where the ball of the
+  // density estimate is cut) starts over with a ball of twice the radius,
+  // up to twice; the other lanes keep their heaps.
+  float t_lane = t0;
+  for (int sweep = 0; sweep < 3; ++sweep) {
   // ---- the 27 nodes around the tile
   {
     uint32_t b = 0, n = 0;
@@ -1226,6 +1233,19 @@ knn_tile_kernel(KnnArgs a, SortedSeeds S, const GridDesc* __restrict__ gdp,
       gather(b, n);
     }
   }
+    searching = active && cnt < cap && t_lane < FLT_MAX;
+    if (!__any_sync(FULL, searching)) break;
+    if (searching) {
+      t_lane = 4.f * t_lane;
+      thr = t_lane;
+      cnt = 0;
+      copies = 0;
+      dup_lower = false;
+    }
+    wthr = searching ? thr : 0.f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) wthr = fmaxf(wthr, __shfl_xor_sync(FULL, wthr, o));
+  }
   if (!active) return;
 
   // ---- per lane: heap sort, ascending FP32 distance
@@ -1238,7 +1258,7 @@ knn_tile_kernel(KnnArgs a, SortedSeeds S, const GridDesc* __restrict__ gdp,
     SL(n - 1) = sr;
     sift_down(0, n - 1);
   }
-  bool unsure = cnt < cap && t0 < FLT_MAX;  // fewer than cap within the first distance
+  bool unsure = cnt < cap && t_lane < FLT_MAX;  // fewer than cap within the last distance
   if (cnt == cap) {
     // a seed that may belong to the k nearest could have been dropped
     const float r = sqrtf(D(K - 1)) * 1.0000076f + 2.f * delta;
