@@ -51,10 +51,14 @@ FLOP_TEST, FLOP_CORNER = 7, 59
 # FP32 lanes per SM and SMs of a GB300: the CUDA-core FP32 rate is
 # 2 flop x lanes x SMs x clock (no measured FP32 figure exists for the part)
 FP32_LANES, N_SM = 128, 152
-# DRAM bytes of one launch on this workload, from ncu captures
-# (dram__bytes_read.sum + dram__bytes_write.sum); None where not captured
-CLIP_TRAFFIC_BYTES = None
-KNN_TRAFFIC_BYTES = None
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch,
+# captured with ncu on the 300k-seed diagram with weights on the same scale
+# (U[0, 2.2e-4]) and scaled by the seeds processed to this 1M-seed launch:
+# the first clipping pass moved 259.6 MB (866 B per cell), the tiled kNN
+# 82.7 MB (part of its list writes were still in L2 at the end of the
+# smaller launch, so this scaled figure is a lower bound)
+CLIP_TRAFFIC_BYTES = 259.6e6 * N_SEEDS / 300_000
+KNN_TRAFFIC_BYTES = 82.7e6 * N_SEEDS / 300_000
 W_MAX = 1e-4
 METRIC = ("Laguerre cells/s (power diagram, 1M seeds, FP32 clip + FP64 re-clip, "
           "Lloyd step from the seeded start)")
@@ -319,6 +323,34 @@ def run_ours(args) -> None:
             torch.cuda.synchronize()
             t64.append(e0.elapsed_time(e1))
         fp64_cps = N_SEEDS / (statistics.median(t64) / 1e3)
+        # ---- the FP32-geometry mode (same cells, FP32 volumes / centroids /
+        # areas) on the same seeds, and its error against the FP64 path
+        t3g = []
+        for _ in range(3):
+            flush.fill_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            g.compute_cells_device(x0, w, precision="fp32_geometry", stream=stream, ctx=ctx)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            t3g.append(e0.elapsed_time(e1))
+        cg = g.device_results(ctx)
+        vscale = np.maximum(c64["volume"], 1e-300)
+        cell_of = np.repeat(np.arange(N_SEEDS), np.diff(c64["rowptr"].astype(np.int64)))
+        geom32 = {
+            "cells_per_s": N_SEEDS / (statistics.median(t3g) / 1e3),
+            "ms": statistics.median(t3g),
+            "speedup_vs_fp64_plain": statistics.median(t64) / statistics.median(t3g),
+            "max_rel_vol_err_vs_fp64": float(np.max(np.abs(cg["volume"] - c64["volume"]) / vscale)),
+            "max_mg_err_vs_fp64_rel_to_volume": float(
+                np.max(np.abs(cg["mg"] - c64["mg"]).max(axis=1) / vscale)),
+            "max_area_err_vs_fp64_rel_to_volume_2_3": float(
+                np.max(np.abs(cg["facet_area"] - c64["facet_area"]) / vscale[cell_of] ** (2 / 3))),
+            "neighbour_lists_identical": bool(
+                np.array_equal(cg["rowptr"], c64["rowptr"]) and
+                np.array_equal(cg["neighbors"], c64["neighbors"])),
+        }
         t32 = statistics.median(r["ms_total"] for r in reports)
         rel_vol = float(np.max(np.abs(c32["volume"] - c64["volume"]) /
                                np.maximum(np.abs(c64["volume"]), 1e-300)))
@@ -368,6 +400,7 @@ def run_ours(args) -> None:
                            "speedup_of_this_mode": statistics.median(t64) / t32,
                            "max_rel_vol_err_vs_fp64": rel_vol, "max_abs_mg_err_vs_fp64": abs_mg,
                            "neighbour_lists_identical": same_nbr},
+            "fp32_geometry": geom32,
         }
         if args.extras:
             line["c2_lloyd10"] = run_lloyd10(x0, w, args.precision, stream, ctx, flush)

@@ -35,17 +35,18 @@ import numpy as np
 
 from . import _lib
 from ._lib import (CELL_ALL_NEIGHBOURS, CELL_CERTIFIED, CELL_DUPLICATE, CELL_STALLED,
-                   CERTIFY_POWER_RANGE, CERTIFY_SECURITY_RADIUS, PRECISION_FP32_RECHECK,
+                   CERTIFY_POWER_RANGE, CERTIFY_SECURITY_RADIUS, PRECISION_FP32_GEOMETRY,
+                   PRECISION_FP32_RECHECK,
                    PRECISION_FP64, CellOptions, CellReport, GbvError, OtOptions, OtReport)
 
 __all__ = [
     "Context", "NearestNeighborSearch", "Cells", "compute_cells", "lloyd_step",
     "lloyd_iterations", "compute_cells_device", "device_results", "GbvError", "CELL_CERTIFIED", "CELL_ALL_NEIGHBOURS", "CELL_DUPLICATE",
     "CELL_STALLED",
-    "PRECISION_FP64", "PRECISION_FP32_RECHECK", "cell_options", "CERTIFY_SECURITY_RADIUS",
+    "PRECISION_FP64", "PRECISION_FP32_RECHECK", "PRECISION_FP32_GEOMETRY", "cell_options", "CERTIFY_SECURITY_RADIUS",
     "CERTIFY_POWER_RANGE", "ot_options", "ot_solve", "ot_solve_device", "ot_gradient_hessian",
     "ot_solve_levels", "ot_solve_levels_device", "ot_separable_start_device", "CellMesh",
-    "cells_mesh", "restricted_cells", "periodic_cells",
+    "cells_mesh", "restricted_cells", "cvt_newton", "periodic_cells",
 ]
 
 
@@ -96,7 +97,8 @@ def default_context() -> Context:
 def _precision(precision: str | int) -> int:
     if isinstance(precision, str):
         return {"fp64": PRECISION_FP64, "fp32": PRECISION_FP32_RECHECK,
-                "fp32_recheck": PRECISION_FP32_RECHECK}[precision]
+                "fp32_recheck": PRECISION_FP32_RECHECK,
+                "fp32_geometry": PRECISION_FP32_GEOMETRY}[precision]
     return int(precision)
 
 
@@ -379,6 +381,27 @@ def restricted_cells(mesh_xyz: np.ndarray, tets: np.ndarray, xyz: np.ndarray,
     out["report"] = rep.as_dict()
     ctx.last_n, ctx.last_nnz = n, rep.nnz
     return out
+
+
+def cvt_newton(mesh_xyz: np.ndarray, tets: np.ndarray, xyz: np.ndarray, nb_iter: int, *,
+               m: int = 7, k0: int = 20, precision="fp64",
+               ctx: Context | None = None) -> tuple[np.ndarray, np.ndarray]:
+    """CentroidalVoronoiTesselation::Newton_iterations (voronoi/CVT.cpp:
+    272-307) on a tetrahedral mesh: L-BFGS with m pairs on the restricted
+    cells' CVT energy and gradient, nb_iter + 1 steps as the reference's
+    HLBFGS takes.  Returns the moved seeds and the energy at the start and
+    after each step."""
+    ctx = ctx or default_context()
+    v = np.ascontiguousarray(mesh_xyz, dtype=np.float64).reshape(-1, 3)
+    t = np.ascontiguousarray(tets, dtype=np.uint32).reshape(-1, 4)
+    x = np.array(xyz, dtype=np.float64).reshape(-1, 3)
+    o = cell_options(k0=k0, precision=precision)
+    energy = np.zeros(nb_iter + 2)
+    its = ctypes.c_uint32(0)
+    _lib.check(ctx._lib.gbv_cvt_newton(ctx.handle, _lib.ptr(v), len(v), _lib.ptr(t), len(t),
+                                       _lib.ptr(x), len(x), ctypes.byref(o), nb_iter, m,
+                                       _lib.ptr(energy), ctypes.byref(its)))
+    return x, energy[:its.value + 1]
 
 
 def _dev_arg(t, name: str, n: int | None = None, cols: int | None = None,

@@ -25,6 +25,7 @@ CELL_STALLED = 3
 
 PRECISION_FP64 = 0
 PRECISION_FP32_RECHECK = 1
+PRECISION_FP32_GEOMETRY = 2
 
 
 class GbvError(RuntimeError):
@@ -184,6 +185,9 @@ SIGNATURES = {
                                             ctypes.POINTER(CellOptions), _P, _P,
                                             ctypes.POINTER(ctypes.c_double), _P,
                                             ctypes.POINTER(CellReport)]),
+    "gbv_cvt_newton": (ctypes.c_int, [_P, _P, _U32, _P, _U32, _P, _U32,
+                                      ctypes.POINTER(CellOptions), _U32, _U32, _P,
+                                      ctypes.POINTER(ctypes.c_uint32)]),
     "gbv_cells_mesh": (ctypes.c_int, [_P, _P, _U32, ctypes.POINTER(MeshSizes), _P, _P, _P, _P,
                                       _P, _P]),
     "gbv_knn_noalloc": (ctypes.c_int, [_P, _U32, _U32, _U32, _U32, _P, _P, _P]),

@@ -29,6 +29,7 @@
 
 #include "gbv_context.cuh"
 #include "gbv_ot.cuh"
+#include "gbv_lbfgs.h"
 #include "gbv_mlp.cuh"
 #include "gbv_start.cuh"
 
@@ -486,6 +487,7 @@ struct Pipeline {
   }
 
   bool timed_first = false;  // the first clipping pass has been timed
+  bool geom32 = false;       // FP32 geometry after FP32 clipping passes
 
   // certification counters (GBV_CERT_STATS in the environment)
   unsigned long long* cert_stats = nullptr;
@@ -568,6 +570,7 @@ struct Pipeline {
     g.nq = nq;
     g.verify_sr = (f32 && check_sr) ? 1 : 0;
     g.shape = shape;
+    g.g32 = (f32 && geom32 && check_sr && !node_wmax) ? 1 : 0;
     if (node_wmax) {
       g.node_wmax = node_wmax;
       g.node_lin = node_lin;
@@ -862,8 +865,9 @@ static void cells_device(gbv_context* c, const double* d_xyz, const double* d_w,
   GBV_CUDA(cudaEventRecord(c->ev[0], st));
   build_grid(d_xyz, 3, 3, d_w, n, S.L, S, c->scr, st);
   GBV_CUDA(cudaEventRecord(c->ev[1], st));
-  Pipeline P(c, n, o.box_min, o.box_max, o.precision == GBV_PRECISION_FP32_RECHECK,
+  Pipeline P(c, n, o.box_min, o.box_max, o.precision != GBV_PRECISION_FP64,
              o.check_sr != 0, o.k0, st, o.predicates == GBV_PREDICATES_FAST);
+  P.geom32 = o.precision == GBV_PRECISION_FP32_GEOMETRY;
   uint32_t* flag_count = c->buf<uint32_t>("knn_flag_count", 1);
   uint32_t* flag_list = c->buf<uint32_t>("knn_flag_list", n);
 
@@ -1856,10 +1860,14 @@ static gbv_status guarded(F&& f) {
   }
 }
 
-static gbv_status check_opts(const gbv_cell_options* o) {
+static gbv_status check_opts(const gbv_cell_options* o, bool geometry32_ok = true) {
   if (!o) return fail(GBV_ERR_INVALID_ARGUMENT, "options is NULL");
-  if (o->precision != GBV_PRECISION_FP64 && o->precision != GBV_PRECISION_FP32_RECHECK)
+  if (o->precision != GBV_PRECISION_FP64 && o->precision != GBV_PRECISION_FP32_RECHECK &&
+      o->precision != GBV_PRECISION_FP32_GEOMETRY)
     return fail(GBV_ERR_INVALID_ARGUMENT, "unknown precision");
+  if (o->precision == GBV_PRECISION_FP32_GEOMETRY && !geometry32_ok)
+    return fail(GBV_ERR_INVALID_ARGUMENT,
+                "GBV_PRECISION_FP32_GEOMETRY is for gbv_cells_* and the Lloyd steps");
   for (int k = 0; k < 3; ++k)
     if (!(o->box_max[k] > o->box_min[k])) return fail(GBV_ERR_INVALID_ARGUMENT, "empty box");
   if (o->k0 == 0) return fail(GBV_ERR_INVALID_ARGUMENT, "k0 must be > 0");
@@ -1966,7 +1974,7 @@ gbv_status gbv_cells_compute_device(gbv_context* c, const double* d_xyz, const d
     cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
     if (opt->certification == GBV_CERTIFY_POWER_RANGE)
       laguerre_device(c, d_xyz, d_w, n, opt->box_min, opt->box_max,
-                      opt->precision == GBV_PRECISION_FP32_RECHECK, nullptr, nullptr, st, report);
+                      opt->precision != GBV_PRECISION_FP64, nullptr, nullptr, st, report);
     else
       cells_device(c, d_xyz, d_w, n, *opt, st, report);
   });
@@ -1985,7 +1993,7 @@ gbv_status gbv_cells_compute(gbv_context* c, const double* xyz, const double* w,
     if (w) GBV_CUDA(cudaMemcpyAsync(dw, w, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
     if (opt->certification == GBV_CERTIFY_POWER_RANGE)
       laguerre_device(c, dx, dw, n, opt->box_min, opt->box_max,
-                      opt->precision == GBV_PRECISION_FP32_RECHECK, nullptr, nullptr, c->stream,
+                      opt->precision != GBV_PRECISION_FP64, nullptr, nullptr, c->stream,
                       report);
     else
       cells_device(c, dx, dw, n, *opt, c->stream, report);
@@ -1998,7 +2006,7 @@ gbv_status gbv_periodic_cells(gbv_context* c, const double* xyz, const double* w
   if (!c || !xyz) return fail(GBV_ERR_INVALID_ARGUMENT, "NULL argument");
   if (n < 2) return fail(GBV_ERR_INVALID_ARGUMENT, "n must be >= 2");
   if (!(period > 0.0)) return fail(GBV_ERR_INVALID_ARGUMENT, "period must be > 0");
-  gbv_status s = check_opts(opt);
+  gbv_status s = check_opts(opt, false);
   if (s != GBV_OK) return s;
   if (opt->certification != GBV_CERTIFY_SECURITY_RADIUS || !opt->check_sr)
     return fail(GBV_ERR_INVALID_ARGUMENT, "periodic cells use the security-radius loop");
@@ -2071,6 +2079,64 @@ gbv_status gbv_periodic_fetch(gbv_context* c, double* vol, double* mg, uint32_t*
   });
 }
 
+// Restricted cells of the seeds xyz (host) on the mesh already on the device
+// (dmv, dt): per-cell m, mg, the CVT energy and its gradient; the box is
+// the bounding box of the mesh and the seeds.
+static void restricted_eval(gbv_context* c, const double* mesh_xyz, uint32_t nv, const double* dmv,
+                            const uint32_t* dt, uint32_t nt, const double* xyz, const double* w,
+                            uint32_t n, const gbv_cell_options& opt, double* m, double* mg,
+                            double* f, double* g, gbv_cell_report* report) {
+  cudaStream_t st = c->stream;
+  gbv_cell_options o = opt;
+  for (int k = 0; k < 3; ++k) {
+    o.box_min[k] = DBL_MAX;
+    o.box_max[k] = -DBL_MAX;
+  }
+  auto grow = [&](const double* p) {
+    for (int k = 0; k < 3; ++k) {
+      o.box_min[k] = std::min(o.box_min[k], p[k]);
+      o.box_max[k] = std::max(o.box_max[k], p[k]);
+    }
+  };
+  for (uint32_t v = 0; v < nv; ++v) grow(mesh_xyz + 3 * (size_t)v);
+  for (uint32_t i = 0; i < n; ++i) grow(xyz + 3 * (size_t)i);
+  for (int k = 0; k < 3; ++k)
+    if (!(o.box_max[k] > o.box_min[k])) throw StatusError{GBV_ERR_INVALID_ARGUMENT, "flat mesh"};
+  double* dx = c->buf<double>("in_xyz", 3 * (size_t)n);
+  double* dw = w ? c->buf<double>("in_w", n) : nullptr;
+  GBV_CUDA(cudaMemcpyAsync(dx, xyz, 24 * (size_t)n, cudaMemcpyHostToDevice, st));
+  if (w) GBV_CUDA(cudaMemcpyAsync(dw, w, 8 * (size_t)n, cudaMemcpyHostToDevice, st));
+  cells_device(c, dx, dw, n, o, st, report);
+  double* dm = c->buf<double>("rv_m", n);
+  double* dmg = c->buf<double>("rv_mg", 3 * (size_t)n);
+  double* dF = c->buf<double>("rv_F", n);
+  double* dg = c->buf<double>("rv_g", 3 * (size_t)n);
+  restricted_cells(c, dx, dw, n, dmv, nv, dt, nt, st, dm, dmg, dF, dg);
+  if (m) GBV_CUDA(cudaMemcpyAsync(m, dm, 8 * (size_t)n, cudaMemcpyDeviceToHost, st));
+  if (mg) GBV_CUDA(cudaMemcpyAsync(mg, dmg, 24 * (size_t)n, cudaMemcpyDeviceToHost, st));
+  if (g) GBV_CUDA(cudaMemcpyAsync(g, dg, 24 * (size_t)n, cudaMemcpyDeviceToHost, st));
+  if (f) {
+    // deterministic FP64 sum of the per-cell energies
+    double* part = c->buf<double>("rv_part", 2 * kOtParts);
+    double* ones = c->buf<double>("rv_ones", n);
+    fill_kernel<<<nblocks(n, 256), 256, 0, st>>>(ones, 1.0, n); count_launch();
+    dot_parts(dF, ones, n, part, st);
+    std::vector<double> hp(2 * kOtParts);
+    GBV_CUDA(cudaMemcpyAsync(hp.data(), part, 16 * kOtParts, cudaMemcpyDeviceToHost, st));
+    GBV_CUDA(cudaStreamSynchronize(st));
+    double S = 0.0, C = 0.0;
+    for (int b = 0; b < kOtParts; ++b) {
+      const double x = hp[2 * b], t = S + x;
+      if (std::fabs(S) >= std::fabs(x)) C += (S - t) + x;
+      else C += (x - t) + S;
+      S = t;
+      C += hp[2 * b + 1];
+    }
+    *f = S + C;
+  }
+  GBV_CUDA(cudaStreamSynchronize(st));
+}
+
 gbv_status gbv_restricted_cells(gbv_context* c, const double* mesh_xyz, uint32_t nv,
                                 const uint32_t* tets, uint32_t nt, const double* xyz,
                                 const double* w, uint32_t n, const gbv_cell_options* opt,
@@ -2078,66 +2144,66 @@ gbv_status gbv_restricted_cells(gbv_context* c, const double* mesh_xyz, uint32_t
                                 gbv_cell_report* report) {
   if (!c || !mesh_xyz || !tets || !xyz) return fail(GBV_ERR_INVALID_ARGUMENT, "NULL argument");
   if (nv == 0 || nt == 0 || n == 0) return fail(GBV_ERR_INVALID_ARGUMENT, "empty mesh or seeds");
-  gbv_status s = check_opts(opt);
+  gbv_status s = check_opts(opt, false);
   if (s != GBV_OK) return s;
   if (opt->certification != GBV_CERTIFY_SECURITY_RADIUS)
     return fail(GBV_ERR_INVALID_ARGUMENT, "restricted cells use the security-radius loop");
   return guarded([&] {
     GBV_CUDA(cudaSetDevice(c->device));
-    cudaStream_t st = c->stream;
-    // the box: bounding box of the mesh and the seeds
-    gbv_cell_options o = *opt;
-    for (int k = 0; k < 3; ++k) {
-      o.box_min[k] = DBL_MAX;
-      o.box_max[k] = -DBL_MAX;
-    }
-    auto grow = [&](const double* p) {
-      for (int k = 0; k < 3; ++k) {
-        o.box_min[k] = std::min(o.box_min[k], p[k]);
-        o.box_max[k] = std::max(o.box_max[k], p[k]);
-      }
-    };
-    for (uint32_t v = 0; v < nv; ++v) grow(mesh_xyz + 3 * (size_t)v);
-    for (uint32_t i = 0; i < n; ++i) grow(xyz + 3 * (size_t)i);
-    for (int k = 0; k < 3; ++k)
-      if (!(o.box_max[k] > o.box_min[k])) throw StatusError{GBV_ERR_INVALID_ARGUMENT, "flat mesh"};
-    double* dx = c->buf<double>("in_xyz", 3 * (size_t)n);
-    double* dw = w ? c->buf<double>("in_w", n) : nullptr;
     double* dmv = c->buf<double>("rv_mesh_xyz", 3 * (size_t)nv);
     uint32_t* dt = c->buf<uint32_t>("rv_tets_in", 4 * (size_t)nt);
-    GBV_CUDA(cudaMemcpyAsync(dx, xyz, 24 * (size_t)n, cudaMemcpyHostToDevice, st));
-    if (w) GBV_CUDA(cudaMemcpyAsync(dw, w, 8 * (size_t)n, cudaMemcpyHostToDevice, st));
-    GBV_CUDA(cudaMemcpyAsync(dmv, mesh_xyz, 24 * (size_t)nv, cudaMemcpyHostToDevice, st));
-    GBV_CUDA(cudaMemcpyAsync(dt, tets, 16 * (size_t)nt, cudaMemcpyHostToDevice, st));
-    cells_device(c, dx, dw, n, o, st, report);
-    double* dm = c->buf<double>("rv_m", n);
-    double* dmg = c->buf<double>("rv_mg", 3 * (size_t)n);
-    double* dF = c->buf<double>("rv_F", n);
-    double* dg = c->buf<double>("rv_g", 3 * (size_t)n);
-    restricted_cells(c, dx, dw, n, dmv, nv, dt, nt, st, dm, dmg, dF, dg);
-    if (m) GBV_CUDA(cudaMemcpyAsync(m, dm, 8 * (size_t)n, cudaMemcpyDeviceToHost, st));
-    if (mg) GBV_CUDA(cudaMemcpyAsync(mg, dmg, 24 * (size_t)n, cudaMemcpyDeviceToHost, st));
-    if (g) GBV_CUDA(cudaMemcpyAsync(g, dg, 24 * (size_t)n, cudaMemcpyDeviceToHost, st));
-    if (f) {
-      // deterministic FP64 sum of the per-cell energies
-      double* part = c->buf<double>("rv_part", 2 * kOtParts);
-      double* ones = c->buf<double>("rv_ones", n);
-      fill_kernel<<<nblocks(n, 256), 256, 0, st>>>(ones, 1.0, n); count_launch();
-      dot_parts(dF, ones, n, part, st);
-      std::vector<double> hp(2 * kOtParts);
-      GBV_CUDA(cudaMemcpyAsync(hp.data(), part, 16 * kOtParts, cudaMemcpyDeviceToHost, st));
-      GBV_CUDA(cudaStreamSynchronize(st));
-      double S = 0.0, C = 0.0;
-      for (int b = 0; b < kOtParts; ++b) {
-        const double x = hp[2 * b], t = S + x;
-        if (std::fabs(S) >= std::fabs(x)) C += (S - t) + x;
-        else C += (x - t) + S;
-        S = t;
-        C += hp[2 * b + 1];
-      }
-      *f = S + C;
-    }
-    GBV_CUDA(cudaStreamSynchronize(st));
+    GBV_CUDA(cudaMemcpyAsync(dmv, mesh_xyz, 24 * (size_t)nv, cudaMemcpyHostToDevice, c->stream));
+    GBV_CUDA(cudaMemcpyAsync(dt, tets, 16 * (size_t)nt, cudaMemcpyHostToDevice, c->stream));
+    restricted_eval(c, mesh_xyz, nv, dmv, dt, nt, xyz, w, n, *opt, m, mg, f, g, report);
+  });
+}
+
+gbv_status gbv_cvt_newton(gbv_context* c, const double* mesh_xyz, uint32_t nv,
+                          const uint32_t* tets, uint32_t nt, double* xyz, uint32_t n,
+                          const gbv_cell_options* opt, uint32_t nb_iter, uint32_t m,
+                          double* energy, uint32_t* iterations) {
+  if (!c || !mesh_xyz || !tets || !xyz) return fail(GBV_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (nv == 0 || nt == 0 || n == 0) return fail(GBV_ERR_INVALID_ARGUMENT, "empty mesh or seeds");
+  if (m == 0) return fail(GBV_ERR_INVALID_ARGUMENT, "m must be > 0");
+  gbv_status s = check_opts(opt, false);
+  if (s != GBV_OK) return s;
+  if (opt->certification != GBV_CERTIFY_SECURITY_RADIUS)
+    return fail(GBV_ERR_INVALID_ARGUMENT, "restricted cells use the security-radius loop");
+  return guarded([&] {
+    GBV_CUDA(cudaSetDevice(c->device));
+    double* dmv = c->buf<double>("rv_mesh_xyz", 3 * (size_t)nv);
+    uint32_t* dt = c->buf<uint32_t>("rv_tets_in", 4 * (size_t)nt);
+    GBV_CUDA(cudaMemcpyAsync(dmv, mesh_xyz, 24 * (size_t)nv, cudaMemcpyHostToDevice, c->stream));
+    GBV_CUDA(cudaMemcpyAsync(dt, tets, 16 * (size_t)nt, cudaMemcpyHostToDevice, c->stream));
+    std::vector<double> x(xyz, xyz + 3 * (size_t)n);
+    // HLBFGS stops once its iteration count exceeds max_iter
+    // (third_party/HLBFGS/HLBFGS.cpp:580), so the reference's
+    // Newton_iterations(nb_iter) takes nb_iter + 1 steps: so does this
+    LbfgsParams prm;
+    prm.m = (int)m;
+    prm.max_iter = (int)nb_iter + 1;
+    auto fg = [&](const std::vector<double>& p, std::vector<double>& g) -> double {
+      double f = 0.0;
+      restricted_eval(c, mesh_xyz, nv, dmv, dt, nt, p.data(), nullptr, n, *opt, nullptr, nullptr,
+                      &f, g.data(), nullptr);
+      return f;
+    };
+    if (energy) energy[0] = 0.0;
+    bool first = true;
+    auto newiter = [&](int it, const std::vector<double>&, double f, const std::vector<double>&) {
+      if (energy && (uint32_t)it <= nb_iter + 1) energy[it] = f;
+    };
+    const LbfgsResult r = lbfgs_minimize(
+        x, prm,
+        [&](const std::vector<double>& p, std::vector<double>& g) {
+          const double f = fg(p, g);
+          if (first && energy) energy[0] = f;
+          first = false;
+          return f;
+        },
+        newiter);
+    std::copy(x.begin(), x.end(), xyz);
+    if (iterations) *iterations = (uint32_t)r.iterations;
   });
 }
 

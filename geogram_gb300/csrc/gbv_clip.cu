@@ -491,21 +491,18 @@ __global__ void __launch_bounds__(kClipWarps * 32, clip_min_blocks<Real, XF>()) 
 
         // ---- conflict scan (triangle_is_in_conflict, convex_cell.cpp:870-912)
         bool cf[NS];
-        Real kr2 = 0;
-        int kme = -0x7FFF;
         bool uncertain = false;
 #pragma unroll
         for (int q = 0; q < NS; ++q) {
           const int t = lane + 32 * q;
           cf[q] = false;
           if (!valid.test(t)) continue;
-          Real cx, cy, cz, r2, eps;
+          Real cx, cy, cz, eps;
           if constexpr (kFP64) {
-            const double2 xy = g.cxy[t], zr = g.czr[t];
+            const double2 xy = g.cxy[t];
             cx = xy.x;
             cy = xy.y;
-            cz = zr.x;
-            r2 = zr.y;
+            cz = g.czr[t].x;
             eps = (double)g.eps[t];
           } else {
             const float4 c = g.c4[t];
@@ -513,7 +510,6 @@ __global__ void __launch_bounds__(kClipWarps * 32, clip_min_blocks<Real, XF>()) 
             cy = c.y;
             cz = c.z;
             eps = c.w;
-            r2 = cx * cx + cy * cy + cz * cz;
           }
           Real sv;
           if constexpr (kFP64) sv = fma(Pn.z, cz, fma(Pn.y, cy, fma(Pn.x, cx, Pn.w)));
@@ -543,10 +539,6 @@ __global__ void __launch_bounds__(kClipWarps * 32, clip_min_blocks<Real, XF>()) 
             }
           }
           cf[q] = in_conflict;
-          if (!in_conflict) {
-            kr2 = fmax(kr2, r2);
-            kme = max(kme, par_old * (int)g.key[t]);
-          }
         }
         if (lane == 0) n_tests += (unsigned)valid.popc();
         if (!kFP64 && !XF && __any_sync(FULL, uncertain)) {
@@ -563,6 +555,23 @@ __global__ void __launch_bounds__(kClipWarps * 32, clip_min_blocks<Real, XF>()) 
           valid.clear();
           R2 = 0;
           continue;
+        }
+        // the kept triangles: largest corner radius and list key
+        Real kr2 = 0;
+        int kme = -0x7FFF;
+#pragma unroll
+        for (int q = 0; q < NS; ++q) {
+          const int t = lane + 32 * q;
+          if (!valid.test(t) || cf[q]) continue;
+          Real r2;
+          if constexpr (kFP64) {
+            r2 = g.czr[t].y;
+          } else {
+            const float4 c = g.c4[t];
+            r2 = c.x * c.x + c.y * c.y + c.z * c.z;
+          }
+          kr2 = fmax(kr2, r2);
+          kme = max(kme, par_old * (int)g.key[t]);
         }
         const Real keepR2 = warp_maxf(kr2);
         const int keep_max_eff = __reduce_max_sync(FULL, kme);
@@ -673,14 +682,19 @@ __global__ void __launch_bounds__(kClipWarps * 32, clip_min_blocks<Real, XF>()) 
         // takes the i-th free slot, its neighbours the slots of i - 1 and
         // i + 1 along the border
         Real r2n = 0;
-        for (int i = lane; i < nborder; i += 32) {
+        for (int i0 = 0; i0 < nborder; i0 += 32) {
+          const int i = i0 + lane;
+          // slots of border positions i and, through the lanes beside it
+          // (or directly at the ends of a 32-position round), i - 1 and i + 1
+          const int nt = i < nborder ? select_bit(freet, i) : -1;
+          int ntp = __shfl_up_sync(FULL, nt, 1), ntn = __shfl_down_sync(FULL, nt, 1);
+          if (i >= nborder) continue;
+          if (lane == 0 || i == 0) ntp = select_bit(freet, i > 0 ? i - 1 : nborder - 1);
+          if (lane == 31 || i + 1 == nborder) ntn = select_bit(freet, i + 1 < nborder ? i + 1 : 0);
           const uint32_t v = g.order[i];
           const uint32_t x = g.order[i + 1 < nborder ? i + 1 : 0];
           const uint32_t nbinfo = g.pnb[v];
           const uint32_t tn = nbinfo & 0xFF, eb = nbinfo >> 8;
-          const int nt = select_bit(freet, i);
-          const int ntp = select_bit(freet, i > 0 ? i - 1 : nborder - 1);
-          const int ntn = select_bit(freet, i + 1 < nborder ? i + 1 : 0);
           g.tv[nt] = lv | (x << 8) | (v << 16);
           g.ta[nt] = tn | ((uint32_t)ntp << 8) | ((uint32_t)ntn << 16);
           g.key[nt] = (int16_t)(parity * (key_base - i));

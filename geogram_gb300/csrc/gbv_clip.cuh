@@ -72,6 +72,8 @@ struct GeomArgs {
   double box[6];
   int verify_sr;              // FP32 clipping: check its stops in FP64
   int shape;                  // ClipShape of the clipping pass
+  int g32;                    // FP32 corners, tetrahedra and facet triangles
+                              // (security-radius cells only)
   CombBuf comb;
   int32_t* status;
   const uint32_t* nclip;

@@ -17,9 +17,17 @@
 // clipped in FP32 the kernel also checks, in FP64, that the reference's
 // security-radius loop would have stopped at the same neighbour, and sends
 // the cell back to FP64 clipping otherwise.
+//
+// FP32 geometry (G32, the precision mode GBV_PRECISION_FP32_GEOMETRY): the
+// same combinatorics and fans, but corners, tetrahedra and facet triangles
+// in FP32 in the frame centred on the seed (the planes as the FP32
+// clipping kernel forms them), the terms added in FP64; the security-radius
+// stop is verified with the corners' error bounds, and a cell it cannot
+// verify goes back to the FP64 re-clip.
 #include <cfloat>
 
 #include "gbv_clip.cuh"
+#include "gbv_corner.cuh"
 #include "gbv_refgeom.cuh"
 
 namespace gbv {
@@ -248,7 +256,38 @@ __device__ __forceinline__ void certify_cell(const GeomArgs& a, const SortedSeed
   __syncwarp();
 }
 
-template <int T, int P>
+// The FP32 plane of owner `own` in the frame centred on seed s (value and
+// remainder of the coordinates, as the FP32 clipping kernel forms it).
+__device__ __forceinline__ float4 local_plane32(uint32_t own, uint32_t s, const SortedSeeds& S,
+                                                const double* box) {
+  const float4 fh = S.xf[s], fl = S.xl[s];
+  if (own >= kBoxBase) {
+    switch (own - kBoxBase) {
+      case 0: return make_float4(1.f, 0.f, 0.f, (fh.x - (float)box[0]) + fl.x);
+      case 1: return make_float4(-1.f, 0.f, 0.f, ((float)box[3] - fh.x) - fl.x);
+      case 2: return make_float4(0.f, 1.f, 0.f, (fh.y - (float)box[1]) + fl.y);
+      case 3: return make_float4(0.f, -1.f, 0.f, ((float)box[4] - fh.y) - fl.y);
+      case 4: return make_float4(0.f, 0.f, 1.f, (fh.z - (float)box[2]) + fl.z);
+      default: return make_float4(0.f, 0.f, -1.f, ((float)box[5] - fh.z) - fl.z);
+    }
+  }
+  const float4 jh = S.xf[own], jl = S.xl[own];
+  const float dx = (jh.x - fh.x) + (jl.x - fl.x);
+  const float dy = (jh.y - fh.y) + (jl.y - fl.y);
+  const float dz = (jh.z - fh.z) + (jl.z - fl.z);
+  float dw = 0.f;
+  if (S.wf) {
+    const float2 wi = S.wf[s], wj = S.wf[own];
+    dw = (wj.x - wi.x) + (wj.y - wi.y);
+  }
+  return make_float4(-2.f * dx, -2.f * dy, -2.f * dz, dx * dx + dy * dy + dz * dz - dw);
+}
+
+__device__ __forceinline__ float4 to_f4(const double4& q) {
+  return make_float4((float)q.x, (float)q.y, (float)q.z, (float)q.w);
+}
+
+template <int T, int P, bool G32>
 __global__ void __launch_bounds__(kGeomWarps * 32) geom_kernel(GeomArgs a) {
   constexpr int NH = (P + 31) / 32;  // planes (and ranks) per lane
   using Sm = GeomWarpSmem<T, P>;
@@ -292,7 +331,10 @@ __global__ void __launch_bounds__(kGeomWarps * 32) geom_kernel(GeomArgs a) {
       g.prank[p] = cb.prank[pb + p];
       const uint32_t own = cb.pown[pb + p];
       double4 Q;
-      if (own >= kBoxBase) {
+      if constexpr (G32) {
+        const float4 f = local_plane32(own, s, S, a.box);
+        Q = make_double4(f.x, f.y, f.z, f.w);
+      } else if (own >= kBoxBase) {
         switch (own - kBoxBase) {
           case 0: Q = make_double4(1.0, 0.0, 0.0, -a.box[0]); break;
           case 1: Q = make_double4(-1.0, 0.0, 0.0, a.box[3]); break;
@@ -311,16 +353,31 @@ __global__ void __launch_bounds__(kGeomWarps * 32) geom_kernel(GeomArgs a) {
   }
   __syncwarp();
   // ---- corners (compute_geometry) and v2t
-  double R2 = 0.0;
+  double R2 = 0.0, R2lo = 0.0;  // G32: bounds on the reference's R2 (R2 the upper one)
   for (int i = lane; i < ntri; i += 32) {
     const int t = g.tlist[i];
     const uint32_t v = g.tv[t];
     const int a0 = v & 0xFF, a1 = v >> 8 & 0xFF, a2 = v >> 16 & 0xFF;
-    const double3 c = r_corner(g.plane[a0], g.plane[a1], g.plane[a2]);
-    g.px[t] = c.x;
-    g.py[t] = c.y;
-    g.pz[t] = c.z;
-    R2 = fmax(R2, r_sqdist(pi.x, pi.y, pi.z, c));
+    if constexpr (G32) {
+      float x, y, z, e;
+      corner_fp32(to_f4(g.plane[a0]), to_f4(g.plane[a1]), to_f4(g.plane[a2]), x, y, z, e);
+      g.px[t] = x;
+      g.py[t] = y;
+      g.pz[t] = z;
+      // |c|^2 within 2 |c|_1 e + 3 e^2 of the exact corner's, plus its own
+      // FP32 rounding; FP64 slack for the reference's own rounding
+      const double r2 = (double)x * x + (double)y * y + (double)z * z;
+      const double m1 = fabs((double)x) + fabs((double)y) + fabs((double)z);
+      const double er = 2.0 * m1 * e + 3.0 * (double)e * e + r2 * 1e-12;
+      R2 = fmax(R2, r2 + er);
+      R2lo = fmax(R2lo, r2 - er);
+    } else {
+      const double3 c = r_corner(g.plane[a0], g.plane[a1], g.plane[a2]);
+      g.px[t] = c.x;
+      g.py[t] = c.y;
+      g.pz[t] = c.z;
+      R2 = fmax(R2, r_sqdist(pi.x, pi.y, pi.z, c));
+    }
     const int eff = parity * (int)cb.key[tb + t];
     const int packed = ((eff + 32768) << 8) | t;
     atomicMax(&g.v2t[a0], packed);
@@ -328,11 +385,14 @@ __global__ void __launch_bounds__(kGeomWarps * 32) geom_kernel(GeomArgs a) {
     atomicMax(&g.v2t[a2], packed);
   }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) R2 = fmax(R2, __shfl_xor_sync(FULL, R2, o));
+  for (int o = 16; o > 0; o >>= 1) {
+    R2 = fmax(R2, __shfl_xor_sync(FULL, R2, o));
+    if constexpr (G32) R2lo = fmax(R2lo, __shfl_xor_sync(FULL, R2lo, o));
+  }
   __syncwarp();
 
   // ---- cell-centred certification (power range query)
-  if (a.node_wmax) {
+  if (!G32 && a.node_wmax) {
     constexpr int NCL = (T + 31) / 32;
     const double wi = S.ws ? S.ws[s] : 0.0;
     float4 mine[NCL];
@@ -362,7 +422,10 @@ __global__ void __launch_bounds__(kGeomWarps * 32) geom_kernel(GeomArgs a) {
       (st == CELL_CERTIFIED || st == CELL_ALL_NEIGHBOURS || st == CELL_STALLED)) {
     const uint32_t row = a.qrow ? a.qrow[ci] : ci;
     const uint32_t jj = a.nclip[s];
+    // G32: the reference's threshold lies between these two (rounding is
+    // monotonic); the FP64 corners give it exactly
     const double thr = __dmul_rn(4.1, __dadd_rn(R2, __dmul_rn(pi.w, pi.w)));
+    const double thr_lo = G32 ? __dmul_rn(4.1, __dadd_rn(R2lo, __dmul_rn(pi.w, pi.w))) : thr;
     bool ok = true;
     if (st == CELL_CERTIFIED) {
       const uint32_t js = a.nbr[(size_t)jj * a.nbr_stride + row];
@@ -370,7 +433,7 @@ __global__ void __launch_bounds__(kGeomWarps * 32) geom_kernel(GeomArgs a) {
     }
     if (ok && jj > 0) {
       const uint32_t jl = a.nbr[(size_t)(jj - 1) * a.nbr_stride + row];
-      ok = !(dist2_exact(pi, S.xd[jl]) > thr);
+      ok = !(dist2_exact(pi, S.xd[jl]) > thr_lo);
     }
     if (!ok) {
       if (lane == 0) a.status[s] = CELL_RECHECK;
@@ -522,19 +585,44 @@ __global__ void __launch_bounds__(kGeomWarps * 32) geom_kernel(GeomArgs a) {
     const int j = k - g.vofs[r];
     const uint8_t* fan = &g.fan[g.fstart[r]];
     const double3 q1 = corner(fan[0]), q2 = corner(fan[j + 1]), q3 = corner(fan[j + 2]);
-    const double cm = r_tet_volume(po, q1, q2, q3);
-    g.tm[k] = cm;
-    // cm * (p + q + r + s) / 4.0: the division by 4 is the exact product by 0.25
-    g.tx[k] = __dmul_rn(__dmul_rn(cm, __dadd_rn(__dadd_rn(__dadd_rn(po.x, q1.x), q2.x), q3.x)), 0.25);
-    g.ty[k] = __dmul_rn(__dmul_rn(cm, __dadd_rn(__dadd_rn(__dadd_rn(po.y, q1.y), q2.y), q3.y)), 0.25);
-    g.tz[k] = __dmul_rn(__dmul_rn(cm, __dadd_rn(__dadd_rn(__dadd_rn(po.z, q1.z), q2.z), q3.z)), 0.25);
+    if constexpr (G32) {
+      const float ux = (float)q1.x - (float)po.x, uy = (float)q1.y - (float)po.y,
+                  uz = (float)q1.z - (float)po.z;
+      const float vx = (float)q2.x - (float)po.x, vy = (float)q2.y - (float)po.y,
+                  vz = (float)q2.z - (float)po.z;
+      const float wx = (float)q3.x - (float)po.x, wy = (float)q3.y - (float)po.y,
+                  wz = (float)q3.z - (float)po.z;
+      const float d = (uy * vz - uz * vy) * wx + (uz * vx - ux * vz) * wy + (ux * vy - uy * vx) * wz;
+      const float cm = fabsf(d) * (1.f / 6.f);
+      g.tm[k] = cm;
+      g.tx[k] = cm * ((float)po.x + (float)q1.x + (float)q2.x + (float)q3.x) * 0.25f;
+      g.ty[k] = cm * ((float)po.y + (float)q1.y + (float)q2.y + (float)q3.y) * 0.25f;
+      g.tz[k] = cm * ((float)po.z + (float)q1.z + (float)q2.z + (float)q3.z) * 0.25f;
+    } else {
+      const double cm = r_tet_volume(po, q1, q2, q3);
+      g.tm[k] = cm;
+      // cm * (p + q + r + s) / 4.0: the division by 4 is the exact product by 0.25
+      g.tx[k] = __dmul_rn(__dmul_rn(cm, __dadd_rn(__dadd_rn(__dadd_rn(po.x, q1.x), q2.x), q3.x)), 0.25);
+      g.ty[k] = __dmul_rn(__dmul_rn(cm, __dadd_rn(__dadd_rn(__dadd_rn(po.y, q1.y), q2.y), q3.y)), 0.25);
+      g.tz[k] = __dmul_rn(__dmul_rn(cm, __dadd_rn(__dadd_rn(__dadd_rn(po.z, q1.z), q2.z), q3.z)), 0.25);
+    }
   }
   // ---- facet-area terms: triangle j of a seed facet is (fan[0], fan[j+1], fan[j+2])
   for (int k = lane; k < narea; k += 32) {
     const int r = rank_of_term(g.aofs, k);
     const int j = k - g.aofs[r];
     const uint8_t* fan = &g.fan[g.fstart[r]];
-    g.ta[k] = r_triangle_area(corner(fan[0]), corner(fan[j + 1]), corner(fan[j + 2]));
+    if constexpr (G32) {
+      const double3 p1 = corner(fan[0]), p2 = corner(fan[j + 1]), p3 = corner(fan[j + 2]);
+      const float ux = (float)p2.x - (float)p1.x, uy = (float)p2.y - (float)p1.y,
+                  uz = (float)p2.z - (float)p1.z;
+      const float vx = (float)p3.x - (float)p1.x, vy = (float)p3.y - (float)p1.y,
+                  vz = (float)p3.z - (float)p1.z;
+      const float cx = uy * vz - uz * vy, cy = uz * vx - ux * vz, cz = ux * vy - uy * vx;
+      g.ta[k] = 0.5f * sqrtf(cx * cx + cy * cy + cz * cz);
+    } else {
+      g.ta[k] = r_triangle_area(corner(fan[0]), corner(fan[j + 1]), corner(fan[j + 2]));
+    }
   }
   __syncwarp();
   // ---- sums in the reference's order: one accumulator per lane 0-3
@@ -542,6 +630,12 @@ __global__ void __launch_bounds__(kGeomWarps * 32) geom_kernel(GeomArgs a) {
     const double* src = lane == 0 ? g.tm : (lane == 1 ? g.tx : (lane == 2 ? g.ty : g.tz));
     double acc = 0.0;
     for (int k = 0; k < nvol; ++k) acc = __dadd_rn(acc, src[k]);
+    if constexpr (G32) {
+      // back from the seed's frame: mg = mg_local + m p_i
+      const double m = __shfl_sync(0xFu, acc, 0, 4);
+      const double pc = lane == 1 ? pi.x : (lane == 2 ? pi.y : pi.z);
+      if (lane > 0) acc = fma(m, pc, acc);
+    }
     if (lane == 0) a.vol[s] = acc;
     else a.mg[(size_t)(lane - 1) * a.out_stride + s] = acc;
   }
@@ -566,19 +660,25 @@ __global__ void __launch_bounds__(kGeomWarps * 32) geom_kernel(GeomArgs a) {
   if (lane == 0) a.nf[s] = (uint32_t)nfac;
 }
 
-template <int T, int P>
+template <int T, int P, bool G32>
 static void launch_geom(const GeomArgs& a, cudaStream_t st) {
   const size_t sh = sizeof(GeomWarpSmem<T, P>) * kGeomWarps;
-  cudaFuncSetAttribute(geom_kernel<T, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh);
+  cudaFuncSetAttribute(geom_kernel<T, P, G32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)sh);
   const unsigned nb = (a.nq + kGeomWarps - 1) / kGeomWarps;
-  geom_kernel<T, P><<<nb, kGeomWarps * 32, sh, st>>>(a); count_launch();
+  geom_kernel<T, P, G32><<<nb, kGeomWarps * 32, sh, st>>>(a); count_launch();
   last_launch_error = cudaGetLastError();
 }
 
 void launch_geometry(const GeomArgs& a, cudaStream_t st) {
   if (a.nq == 0) return;
-  if (a.shape == CLIP_LARGE) launch_geom<kLargeT, kLargeP>(a, st);
-  else launch_geom<kSmallT, kSmallP>(a, st);
+  if (a.g32) {
+    if (a.shape == CLIP_LARGE) launch_geom<kLargeT, kLargeP, true>(a, st);
+    else launch_geom<kSmallT, kSmallP, true>(a, st);
+  } else {
+    if (a.shape == CLIP_LARGE) launch_geom<kLargeT, kLargeP, false>(a, st);
+    else launch_geom<kSmallT, kSmallP, false>(a, st);
+  }
 }
 
 }  // namespace gbv

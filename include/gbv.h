@@ -59,9 +59,19 @@ enum {
 
 typedef enum {
     GBV_PRECISION_FP64 = 0,          /* all clipping in FP64, exact signs   */
-    GBV_PRECISION_FP32_RECHECK = 1   /* FP32 clipping with certified signs,
+    GBV_PRECISION_FP32_RECHECK = 1,  /* FP32 clipping with certified signs,
                                         FP64 geometry, FP64 re-clip of every
-                                        cell FP32 could not certify         */
+                                        cell FP32 could not certify: results
+                                        identical to GBV_PRECISION_FP64     */
+    GBV_PRECISION_FP32_GEOMETRY = 2  /* as FP32_RECHECK (same cells, same
+                                        neighbours and facets, same status),
+                                        but volumes, centroids and facet
+                                        areas from FP32 corners in each
+                                        seed's frame, summed in FP64: within
+                                        about 1e-6 relative of FP64.  For
+                                        gbv_cells_* and Lloyd with the
+                                        security radius (power-range cells
+                                        keep FP64 geometry)                 */
 } gbv_precision;
 
 typedef struct gbv_context gbv_context;
@@ -433,6 +443,21 @@ gbv_status gbv_restricted_cells(gbv_context* ctx, const double* mesh_xyz, uint32
                                 const double* w, uint32_t n, const gbv_cell_options* opt,
                                 double* m, double* mg, double* f, double* g,
                                 gbv_cell_report* report);
+
+/* Replaces CentroidalVoronoiTesselation::Newton_iterations(nb_iter, m)
+ * (voronoi/CVT.cpp:272-307) on a tetrahedral mesh: L-BFGS keeping m pairs
+ * (the reference's HLBFGS with its default line search, epsg = epsf =
+ * epsx = 0: nb_iter iterations unless the line search fails) on the CVT
+ * energy and gradient of gbv_restricted_cells, evaluated on the GPU at
+ * every step.  HLBFGS stops once its iteration count exceeds nb_iter, so
+ * the reference takes nb_iter + 1 steps; so does this.  xyz[3 n] holds the
+ * start and receives the result; opt gives k0 and precision (security
+ * radius).  energy[nb_iter + 2] (or NULL): the energy at the start and
+ * after each step; *iterations (or NULL): the steps done. */
+gbv_status gbv_cvt_newton(gbv_context* ctx, const double* mesh_xyz, uint32_t nv,
+                          const uint32_t* tets, uint32_t nt, double* xyz, uint32_t n,
+                          const gbv_cell_options* opt, uint32_t nb_iter, uint32_t m,
+                          double* energy, uint32_t* iterations);
 
 /* ---------------------------------------------------------------- */
 /* Cell polytopes (output formats)                                   */

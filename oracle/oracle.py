@@ -86,6 +86,7 @@ def ref():
                                        ctypes.c_size_t]
         lib.ref_cells_save.restype = ctypes.c_long
         lib.ref_rvd_volume.argtypes = [P, U, P, U, P, U, P, P, P, P]
+        lib.ref_cvt_newton.argtypes = [P, U, P, U, P, U, U, U, P]
         lib.ref_set_walk.argtypes = [ctypes.c_int]
         lib.ref_periodic_cells.argtypes = [P, P, U, ctypes.c_double, P, P, P, P, P, P, U]
         lib.ref_init()
@@ -245,6 +246,22 @@ def ref_rvd_volume(mesh_xyz: np.ndarray, tets: np.ndarray, seeds: np.ndarray) ->
         raise RuntimeError("ref_rvd_volume failed")
     out["f"] = f.value
     return out
+
+
+def ref_cvt_newton(mesh_xyz: np.ndarray, tets: np.ndarray, seeds: np.ndarray, nb_iter: int,
+                   m: int = 7) -> tuple[np.ndarray, float]:
+    """The reference's CentroidalVoronoiTesselation::Newton_iterations
+    (voronoi/CVT.cpp:272-307, HLBFGS) on the volumetric tet mesh: the moved
+    seeds and the CVT energy there.  Reference build only."""
+    v = np.ascontiguousarray(mesh_xyz, dtype=np.float64).reshape(-1, 3)
+    t = np.ascontiguousarray(tets, dtype=np.uint32).reshape(-1, 4)
+    x = np.array(seeds, dtype=np.float64).reshape(-1, 3)
+    f = ctypes.c_double(0.0)
+    r = ref().ref_cvt_newton(_p(v), len(v), _p(t), len(t), _p(x), len(x), nb_iter, m,
+                             ctypes.byref(f))
+    if r != 0:
+        raise RuntimeError("ref_cvt_newton failed")
+    return x, f.value
 
 
 def ref_periodic_cells(xyz: np.ndarray, w: np.ndarray | None = None, period: float = 1.0,

@@ -38,6 +38,7 @@
 #include <geogram/points/nn_search.h>
 #include <geogram/voronoi/convex_cell.h>
 #include <geogram/voronoi/RVD.h>
+#include <geogram/voronoi/CVT.h>
 #include <geogram/delaunay/delaunay.h>
 #include <geogram/delaunay/periodic_delaunay_3d.h>
 #include <geogram/mesh/mesh.h>
@@ -369,6 +370,35 @@ int ref_rvd_volume(const double* verts, unsigned nv, const unsigned* tets, unsig
     rvd->compute_CVT_func_grad(fv, g);
     *f = fv;
     return 0;
+}
+
+/*
+ * CentroidalVoronoiTesselation::Newton_iterations(nb_iter, m) (voronoi/
+ * CVT.cpp:272-307, HLBFGS) on the volumetric tet mesh: seeds[3 n] hold the
+ * start and receive the result; *f the CVT energy at the result.
+ */
+int ref_cvt_newton(const double* verts, unsigned nv, const unsigned* tets, unsigned nt,
+                   double* seeds, unsigned n, unsigned nb_iter, unsigned m, double* f) {
+    ensure_init();
+    GEO::Process::set_max_threads(1);
+    GEO::Mesh M(3);
+    M.vertices.create_vertices(nv);
+    for (unsigned v = 0; v < nv; ++v)
+        for (unsigned c = 0; c < 3; ++c) M.vertices.point_ptr(v)[c] = verts[3 * size_t(v) + c];
+    M.cells.create_tets(nt);
+    for (unsigned t = 0; t < nt; ++t)
+        for (unsigned k = 0; k < 4; ++k) M.cells.set_vertex(t, k, tets[4 * size_t(t) + k]);
+    M.cells.connect();
+    {
+        GEO::CentroidalVoronoiTesselation cvt(&M, 3, "BDEL");
+        cvt.set_volumetric(true);
+        cvt.set_points(n, seeds);
+        cvt.Newton_iterations(nb_iter, m);
+        for (unsigned i = 0; i < n; ++i)
+            for (unsigned c = 0; c < 3; ++c) seeds[3 * size_t(i) + c] = cvt.embedding(i)[c];
+    }
+    std::vector<double> mg(3 * size_t(n)), mm(n), g(3 * size_t(n));
+    return ref_rvd_volume(verts, nv, tets, nt, seeds, n, mg.data(), mm.data(), f, g.data());
 }
 
 /*

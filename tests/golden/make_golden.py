@@ -191,6 +191,18 @@ def main(only=None):
             np.savez_compressed(os.path.join(HERE, f"rvd_{name}.npz"), mesh_xyz=v, tets=t, x=x,
                                 m=r["m"], mg=r["mg"], f=np.array(r["f"]), g=r["g"])
             print(f"rvd_{name}", len(t), "tets", len(x), "seeds, sum m", r["m"].sum())
+    if not only or "cvt" in only:
+        # the reference's CVT::Newton_iterations (HLBFGS, m = 7) on the
+        # restricted cells: after 1 and after 10 iterations
+        for name in ("cube_300", "lshape_500"):
+            v, t, x = rvd_cases()[name]
+            out = dict(mesh_xyz=v, tets=t, x=x)
+            for it in (1, 10):
+                xi, fi = oracle.ref_cvt_newton(v, t, x, it)
+                out[f"x{it}"] = xi
+                out[f"f{it}"] = np.array(fi)
+            np.savez_compressed(os.path.join(HERE, f"cvt_newton_{name}.npz"), **out)
+            print(f"cvt_newton_{name}", "f1", float(out["f1"]), "f10", float(out["f10"]))
     if only:
         return
     x = np.random.default_rng(3).random((2000, 3))

@@ -235,3 +235,31 @@ def test_cutting_plane_beyond_16_bit_list_positions(g, far_cutter, prec):
         assert np.array_equal(c.mg[k], r["mg"][3 * k:3 * k + 3])
     assert 1 in c.neighbors[c.rowptr[0]:c.rowptr[1]]
     assert abs(c.volume.sum() - 1.0) < 1e-9
+
+
+@pytest.mark.parametrize("case", ["uniform", "power", "clustered"])
+def test_fp32_geometry_mode(g, case):
+    """GBV_PRECISION_FP32_GEOMETRY: the cells of the FP64 mode (neighbours,
+    facets, status identical) with volumes, centroids and facet areas from
+    FP32 corners in each seed's frame; stated error bars: volumes and
+    centroids within 1e-5 of the cell's volume (relative), facet areas within
+    1e-5 of the cell's volume^(2/3)."""
+    rng = np.random.default_rng(31)
+    n = 100_000
+    if case == "clustered":
+        from geogram_gb300.cli import seeds
+        x = seeds(n, 8, 0.05, 3)
+    else:
+        x = rng.random((n, 3))
+    w = rng.random(n) * n ** (-2.0 / 3.0) if case == "power" else None
+    a = g.compute_cells(x, w, precision="fp64")
+    b = g.compute_cells(x, w, precision="fp32_geometry")
+    assert np.array_equal(a.status, b.status)
+    assert np.array_equal(a.rowptr, b.rowptr)
+    assert np.array_equal(a.neighbors, b.neighbors)
+    scale = np.maximum(a.volume, 1e-300)
+    assert np.max(np.abs(b.volume - a.volume) / scale) < 1e-5
+    assert np.max(np.abs(b.mg - a.mg).max(axis=1) / scale) < 1e-5
+    cell = np.repeat(np.arange(len(x)), np.diff(a.rowptr.astype(np.int64)))
+    assert np.max(np.abs(b.facet_area - a.facet_area) / scale[cell] ** (2.0 / 3.0)) < 1e-5
+    assert abs(b.volume.sum() - 1.0) < 1e-9
