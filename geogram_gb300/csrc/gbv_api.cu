@@ -487,6 +487,8 @@ struct Pipeline {
   }
 
   bool timed_first = false;  // the first clipping pass has been timed
+  unsigned int* abort_on_empty = nullptr;  // first pass stops at an empty cell
+  bool aborted = false;
   bool geom32 = false;       // FP32 geometry after FP32 clipping passes
 
   // certification counters (GBV_CERT_STATS in the environment)
@@ -553,8 +555,21 @@ struct Pipeline {
     // the first pass over every cell: its kernel time and counters alone
     const bool first = kind == 0 && !timed_first;
     if (first) GBV_CUDA(cudaEventRecord(c->ev[6], st));
+    if (abort_on_empty && kind == 0) {
+      GBV_CUDA(cudaMemsetAsync(abort_on_empty, 0, sizeof(unsigned int), st));
+      a.abort_on_empty = abort_on_empty;
+    }
     if (f32) launch_clip_fp32(a, shape, kind != 0, st);
     else launch_clip_fp64(a, shape, st);
+    if (abort_on_empty && kind == 0) {
+      unsigned int h = 0;
+      GBV_CUDA(cudaMemcpyAsync(&h, abort_on_empty, sizeof h, cudaMemcpyDeviceToHost, st));
+      GBV_CUDA(cudaStreamSynchronize(st));
+      if (h) {
+        aborted = true;
+        return;
+      }
+    }
     if (first) {
       timed_first = true;
       GBV_CUDA(cudaEventRecord(c->ev[7], st));
@@ -570,7 +585,7 @@ struct Pipeline {
     g.nq = nq;
     g.verify_sr = (f32 && check_sr) ? 1 : 0;
     g.shape = shape;
-    g.g32 = (f32 && geom32 && check_sr && !node_wmax) ? 1 : 0;
+    g.g32 = (f32 && geom32 && !node_wmax) ? 1 : 0;
     if (node_wmax) {
       g.node_wmax = node_wmax;
       g.node_lin = node_lin;
@@ -679,6 +694,7 @@ struct Pipeline {
                                         cudaMemcpyDeviceToDevice, st));
     };
     run(L, ql, qr, nq, 0);
+    if (aborted) return 0;
     uint32_t c1[4];
     classify(ql, qr, nq, c1);
     uint32_t nrc = c1[0], nov = c1[1], nmk = c1[2];
@@ -1102,8 +1118,23 @@ static bool laguerre_device(gbv_context* c, const double* d_xyz, const double* d
   if (abort_below > 0.0) {
     P.node_wmax = nullptr;
     P.size_extras(32u, cur.stride);
+    // a cell the first clipping pass empties has volume 0 < abort_below:
+    // the pass stops there, without its geometry
+    P.abort_on_empty = c->buf<unsigned int>("lag_abort", 1);
+    // this pass only decides whether to stop: FP32 geometry (volumes within
+    // about 1e-5 relative; the test below keeps a 1e-3 margin, and a cell
+    // it lets through is decided by the FP64 volumes of the full pass)
+    P.geom32 = fp32;
     if (P.process(cur, ql, nullptr, nq) != 0)
       throw StatusError{GBV_ERR_STATE, "unexpected list exhaustion in Laguerre mode"};
+    P.abort_on_empty = nullptr;
+    P.geom32 = false;
+    if (P.aborted) {
+      c->has_cells = false;
+      if (std::getenv("GBV_OT_LOG"))
+        std::fprintf(stderr, "[ot]   first clipping pass emptied a cell: stopped\n");
+      return false;
+    }
     double* part = c->buf<double>("lag_min_part", 256);
     min_partial_kernel<<<256, 256, 0, st>>>(P.vol_s, n, part); count_launch();
     double hp[256];
@@ -1111,7 +1142,7 @@ static bool laguerre_device(gbv_context* c, const double* d_xyz, const double* d
     GBV_CUDA(cudaStreamSynchronize(st));
     double mn = DBL_MAX;
     for (double v : hp) mn = std::min(mn, v);
-    if (mn < abort_below) {
+    if (mn < (fp32 ? 0.999 : 1.0) * abort_below) {
       c->has_cells = false;
       if (std::getenv("GBV_OT_LOG"))
         std::fprintf(stderr, "[ot]   first-pass min volume %.3e < %.3e: stopped\n", mn,

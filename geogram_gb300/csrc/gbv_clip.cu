@@ -315,6 +315,7 @@ __global__ void __launch_bounds__(kClipWarps * 32, clip_min_blocks<Real, XF>()) 
   uint32_t max_jj = 0;
 
   for (uint32_t qi = blockIdx.x * kClipWarps + (threadIdx.x >> 5); qi < a.nq; qi += nwarps) {
+    if (a.abort_on_empty && *(volatile unsigned int*)a.abort_on_empty) break;
     const uint32_t s = a.qlist ? a.qlist[qi] : qi;
     const uint32_t row = a.qrow ? a.qrow[qi] : qi;
 
@@ -554,6 +555,11 @@ __global__ void __launch_bounds__(kClipWarps * 32, clip_min_blocks<Real, XF>()) 
         if (conflict.equals(valid)) {  // the whole cell is clipped away
           valid.clear();
           R2 = 0;
+          if (a.abort_on_empty) {
+            if (lane == 0) atomicExch(a.abort_on_empty, 1u);
+            st = CELL_RECHECK;  // not a result: the caller stops
+            break;
+          }
           continue;
         }
         // the kept triangles: largest corner radius and list key

@@ -46,6 +46,10 @@ struct ClipArgs {
   CombBuf comb;
   unsigned long long* counters;  // [0] exact predicate calls, [1] max clips,
                                  // [2] conflict tests, [3] corners created
+  // set (nonzero) by the first cell clipped away entirely; the cells not
+  // started yet are then skipped (null: off).  An empty cell in this pass
+  // is empty for good: a caller that rejects any empty cell stops here.
+  unsigned int* abort_on_empty;
 };
 
 enum ClipShape : int { CLIP_SMALL = 0, CLIP_LARGE = 1 };

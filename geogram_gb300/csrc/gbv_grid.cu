@@ -1204,11 +1204,17 @@ knn_tile_kernel(KnnArgs a, SortedSeeds S, const GridDesc* __restrict__ gdp,
   // up to twice; the other lanes keep their heaps.
   float t_lane = t0;
   for (int sweep = 0; sweep < 3; ++sweep) {
-  // ---- the 27 nodes around the tile
+  // ---- the 27 nodes around the tile, nearest first (the node, its 6
+  // faces, 12 edges, 8 corners): the heaps fill with near seeds early, so
+  // that their bounds prune more of the farther ones
   {
     uint32_t b = 0, n = 0;
     if (lane < 27) {
-      const int x = nx + lane % 3 - 1, y = ny + (lane / 3) % 3 - 1, z = nz + lane / 9 - 1;
+      // offsets + 1 per axis, as x + 3 y + 9 z, sorted by |dx| + |dy| + |dz|
+      constexpr uint8_t kNear[27] = {13, 4, 10, 12, 14, 16, 22, 1, 3, 5, 7, 9, 11,
+                                     15, 17, 19, 21, 23, 25, 0, 2, 6, 8, 18, 20, 24, 26};
+      const int o = kNear[lane];
+      const int x = nx + o % 3 - 1, y = ny + (o / 3) % 3 - 1, z = nz + o / 9 - 1;
       if (x >= 0 && y >= 0 && z >= 0 && x < NG && y < NG && z < NG) node_range(x, y, z, b, n);
     }
     gather(b, n);

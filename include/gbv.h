@@ -67,8 +67,10 @@ typedef enum {
                                         neighbours and facets, same status),
                                         but volumes, centroids and facet
                                         areas from FP32 corners in each
-                                        seed's frame, summed in FP64: within
-                                        about 1e-6 relative of FP64.  For
+                                        seed's frame, summed in FP64: volumes
+                                        and centroids within about 1e-5 of
+                                        the cell's volume, facet areas within
+                                        1e-4 of its volume^(2/3).  For
                                         gbv_cells_* and Lloyd with the
                                         security radius (power-range cells
                                         keep FP64 geometry)                 */
