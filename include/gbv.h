@@ -69,8 +69,8 @@ typedef enum {
                                         areas from FP32 corners in each
                                         seed's frame, summed in FP64: volumes
                                         and centroids within about 1e-5 of
-                                        the cell's volume, facet areas within
-                                        1e-4 of its volume^(2/3).  For
+                                        the mean cell volume V, facet areas
+                                        within 1e-4 V^(2/3).  For
                                         gbv_cells_* and Lloyd with the
                                         security radius (power-range cells
                                         keep FP64 geometry)                 */
