@@ -1112,51 +1112,41 @@ static bool laguerre_device(gbv_context* c, const double* d_xyz, const double* d
   uint32_t* ex_s = c->buf<uint32_t>("lag_ex_s", n);
   uint32_t* ex_r = c->buf<uint32_t>("lag_ex_r", n);
   uint32_t* ex_count = c->buf<uint32_t>("lag_ex_count", 1);
-  // A call that may stop after the first pass runs that pass without the
-  // certification (its volumes bound the final ones all the same), and
-  // only certifies when it goes on.
-  if (abort_below > 0.0) {
-    P.node_wmax = nullptr;
-    P.size_extras(32u, cur.stride);
-    // a cell the first clipping pass empties has volume 0 < abort_below:
-    // the pass stops there, without its geometry
-    P.abort_on_empty = c->buf<unsigned int>("lag_abort", 1);
-    // this pass only decides whether to stop: FP32 geometry (volumes within
-    // about 1e-5 relative; the test below keeps a 1e-3 margin, and a cell
-    // it lets through is decided by the FP64 volumes of the full pass)
-    P.geom32 = fp32;
-    if (P.process(cur, ql, nullptr, nq) != 0)
-      throw StatusError{GBV_ERR_STATE, "unexpected list exhaustion in Laguerre mode"};
-    P.abort_on_empty = nullptr;
-    P.geom32 = false;
-    if (P.aborted) {
-      c->has_cells = false;
-      if (std::getenv("GBV_OT_LOG"))
-        std::fprintf(stderr, "[ot]   first clipping pass emptied a cell: stopped\n");
-      return false;
-    }
-    double* part = c->buf<double>("lag_min_part", 256);
-    min_partial_kernel<<<256, 256, 0, st>>>(P.vol_s, n, part); count_launch();
-    double hp[256];
-    GBV_CUDA(cudaMemcpyAsync(hp, part, sizeof(hp), cudaMemcpyDeviceToHost, st));
-    GBV_CUDA(cudaStreamSynchronize(st));
-    double mn = DBL_MAX;
-    for (double v : hp) mn = std::min(mn, v);
-    if (mn < (fp32 ? 0.999 : 1.0) * abort_below) {
-      c->has_cells = false;
-      if (std::getenv("GBV_OT_LOG"))
-        std::fprintf(stderr, "[ot]   first-pass min volume %.3e < %.3e: stopped\n", mn,
-                     abort_below);
-      return false;
-    }
-    P.node_wmax = wmax;
-  }
+  // A call that may stop (abort_below > 0): the first clipping pass stops
+  // at the first cell it empties, and after the first round (clipping,
+  // geometry and certification) the volumes bound the final ones from
+  // above (later rounds only add planes), so a volume below abort_below
+  // already decides.
+  if (abort_below > 0.0) P.abort_on_empty = c->buf<unsigned int>("lag_abort", 1);
   for (int round = 0;; ++round) {
     // cells far from their final shape (e.g. next to dense clusters) may
     // need hundreds of extra candidates: the room per cell doubles each round
     P.size_extras(std::min<uint32_t>(32u << std::min(round, 6), kHugeV), cur.stride);
     if (P.process(cur, ql, nullptr, nq) != 0)
       throw StatusError{GBV_ERR_STATE, "unexpected list exhaustion in Laguerre mode"};
+    if (round == 0 && abort_below > 0.0) {
+      P.abort_on_empty = nullptr;
+      if (P.aborted) {
+        c->has_cells = false;
+        if (std::getenv("GBV_OT_LOG"))
+          std::fprintf(stderr, "[ot]   first clipping pass emptied a cell: stopped\n");
+        return false;
+      }
+      double* part = c->buf<double>("lag_min_part", 256);
+      min_partial_kernel<<<256, 256, 0, st>>>(P.vol_s, n, part); count_launch();
+      double hp[256];
+      GBV_CUDA(cudaMemcpyAsync(hp, part, sizeof(hp), cudaMemcpyDeviceToHost, st));
+      GBV_CUDA(cudaStreamSynchronize(st));
+      double mn = DBL_MAX;
+      for (double v : hp) mn = std::min(mn, v);
+      if (mn < abort_below) {
+        c->has_cells = false;
+        if (std::getenv("GBV_OT_LOG"))
+          std::fprintf(stderr, "[ot]   first-round min volume %.3e < %.3e: stopped\n", mn,
+                       abort_below);
+        return false;
+      }
+    }
     if (round == 0) GBV_CUDA(cudaEventRecord(c->ev[5], st));
     GBV_CUDA(cudaMemsetAsync(ex_count, 0, 4, st));
     collect_extra_kernel<<<nblocks(nq, 256), 256, 0, st>>>(ql, nq, P.extra_cnt, P.status_s,

@@ -954,9 +954,13 @@ __device__ __forceinline__ float box_box_d2(uint32_t ix, uint32_t iy, uint32_t i
   return dx * dx + dy * dy + dz * dz;
 }
 
+// Candidates a lane buffers before emptying them into its heap (half of a
+// staged chunk: smaller buffers leave room for more warps per SM).
+constexpr uint32_t kTileBuf = 16;
+
 size_t knn_tile_smem(uint32_t k) {
   // staged seeds (float4 + slot), the lane buffers, the heaps
-  return 32 * (sizeof(float4) + sizeof(uint32_t)) + 32 * 32 * sizeof(uint2) +
+  return 32 * (sizeof(float4) + sizeof(uint32_t)) + kTileBuf * 32 * sizeof(uint2) +
          (size_t)(k + kKnnExtra) * 32 * (sizeof(float) + sizeof(uint32_t));
 }
 
@@ -1026,8 +1030,8 @@ knn_tile_kernel(KnnArgs a, SortedSeeds S, const GridDesc* __restrict__ gdp,
   const uint32_t cap = K + kKnnExtra;
   float4* s_pt = reinterpret_cast<float4*>(knn_smem);
   uint32_t* s_sl = reinterpret_cast<uint32_t*>(s_pt + 32);
-  uint2* s_buf = reinterpret_cast<uint2*>(s_sl + 32);  // [32][32] (d32 bits, slot)
-  float* hd = reinterpret_cast<float*>(s_buf + 32 * 32);
+  uint2* s_buf = reinterpret_cast<uint2*>(s_sl + 32);  // [kTileBuf][32] (d32 bits, slot)
+  float* hd = reinterpret_cast<float*>(s_buf + kTileBuf * 32);
   uint32_t* hs = reinterpret_cast<uint32_t*>(hd + (size_t)cap * 32);
   if (blockIdx.x >= *ntiles) return;
   const uint2 item = items[blockIdx.x];
@@ -1165,23 +1169,26 @@ knn_tile_kernel(KnnArgs a, SortedSeeds S, const GridDesc* __restrict__ gdp,
       }
       __syncwarp();
       const uint32_t m = min(32u, total - base);
-      for (uint32_t t = 0; t < m; ++t) {
-        const float4 p = s_pt[t];
-        const float dx = p.x - c.qf.x, dy = p.y - c.qf.y, dz = p.z - c.qf.z,
-                    dh = p.w - c.qf.w;
-        const float d32 = dx * dx + dy * dy + dz * dz + dh * dh;
-        if (searching && d32 < thr) {
-          mybuf[32 * bn] = make_uint2(__float_as_uint(d32), s_sl[t]);
-          ++bn;
+      for (uint32_t t0s = 0; t0s < m; t0s += kTileBuf) {
+        const uint32_t t1 = min(m, t0s + kTileBuf);
+        for (uint32_t t = t0s; t < t1; ++t) {
+          const float4 p = s_pt[t];
+          const float dx = p.x - c.qf.x, dy = p.y - c.qf.y, dz = p.z - c.qf.z,
+                      dh = p.w - c.qf.w;
+          const float d32 = dx * dx + dy * dy + dz * dz + dh * dh;
+          if (searching && d32 < thr) {
+            mybuf[32 * bn] = make_uint2(__float_as_uint(d32), s_sl[t]);
+            ++bn;
+          }
         }
+        // every lane empties its buffer into its heap
+        for (uint32_t j = 0; j < bn; ++j) {
+          const uint2 v = mybuf[32 * j];
+          const float d32 = __uint_as_float(v.x);
+          if (d32 < thr) offer(v.y, d32);
+        }
+        bn = 0;
       }
-      // every lane empties its buffer into its heap
-      for (uint32_t j = 0; j < bn; ++j) {
-        const uint2 v = mybuf[32 * j];
-        const float d32 = __uint_as_float(v.x);
-        if (d32 < thr) offer(v.y, d32);
-      }
-      bn = 0;
     }
     wthr = searching ? thr : 0.f;
 #pragma unroll

@@ -68,9 +68,10 @@ typedef enum {
                                         but volumes, centroids and facet
                                         areas from FP32 corners in each
                                         seed's frame, summed in FP64: volumes
-                                        and centroids within about 1e-5 of
-                                        the mean cell volume V, facet areas
-                                        within 1e-4 V^(2/3).  For
+                                        and centroids within 1e-4 s, facet
+                                        areas within 1e-3 s^(2/3), s the
+                                        larger of the cell's volume and the
+                                        mean cell volume.  For
                                         gbv_cells_* and Lloyd with the
                                         security radius (power-range cells
                                         keep FP64 geometry)                 */
