@@ -54,6 +54,7 @@ struct GeomWarpSmem {
   float4 cf[T];                          // corners (FP32) and their best power bound
   uint32_t cbest[T];                     // best seed of each corner (certification)
   uint32_t stk[96];                      // octree traversal stack
+  uint32_t owner[P];                     // seed slot of each live plane (kNone: none)
 };
 
 // Cell-centred certification.  A seed j cuts the cell only if for some
@@ -73,11 +74,12 @@ struct GeomWarpSmem {
 // corners' owners update their bounds.  best(c) starts at pi_i(c) plus an
 // FP32 margin, so a seed that may cut is never missed; a candidate that only
 // looks like a cutter within the margin is not reported.
-template <int T, int NCL>
+template <int T, int P, int NCL>
 __device__ __forceinline__ void certify_cell(const GeomArgs& a, const SortedSeeds& S,
                                              const GridDesc& gd, uint32_t s, uint32_t row,
                                              int ntri, float4 (&mine)[NCL], float4* cf,
-                                             uint32_t* cbest, uint32_t* stk, int lane) {
+                                             uint32_t* cbest, uint32_t* stk,
+                                             const uint32_t* owner, int lane) {
   const unsigned FULL = 0xFFFFFFFFu;
   const float hf = gd.h_f;
   const uint32_t ncand = a.cand_cnt[row] & kCntMask;
@@ -157,7 +159,13 @@ __device__ __forceinline__ void certify_cell(const GeomArgs& a, const SortedSeed
             cut = dx * dx + dy * dy + dz * dz - wj < c.w;
           }
           if (cut) {
-            // already in the candidate list (clipped, cutting or not)?
+            // already in the candidate list (clipped, cutting or not)?  The
+            // seeds of the cell's facets first (shared memory), which are
+            // what a corner's margin meets most; then the whole list
+            bool listed = false;
+#pragma unroll
+            for (int p = 0; p < P; ++p) listed = listed || owner[p] == j;
+            if (listed) cut = false;
             for (uint32_t k = 0; k < ncand && cut; ++k)
               if (a.nbr[(size_t)k * a.nbr_stride + row] == j) cut = false;
           }
@@ -327,9 +335,11 @@ __global__ void __launch_bounds__(kGeomWarps * 32) geom_kernel(GeomArgs a) {
   for (int p = lane; p < P; p += 32) {
     g.v2t[p] = -1;
     g.prank[p] = 0xFFFF;
+    g.owner[p] = kNone;
     if ((pm >> p) & 1ull) {
       g.prank[p] = cb.prank[pb + p];
       const uint32_t own = cb.pown[pb + p];
+      g.owner[p] = own;
       double4 Q;
       if constexpr (G32) {
         const float4 f = local_plane32(own, s, S, a.box);
@@ -411,7 +421,7 @@ __global__ void __launch_bounds__(kGeomWarps * 32) geom_kernel(GeomArgs a) {
     __syncwarp();
     const GridDesc gd = *S.gd;
     const uint32_t row = a.qrow ? a.qrow[ci] : ci;
-    certify_cell<T, NCL>(a, S, gd, s, row, ntri, mine, g.cf, g.cbest, g.stk, lane);
+    certify_cell<T, P, NCL>(a, S, gd, s, row, ntri, mine, g.cf, g.cbest, g.stk, g.owner, lane);
     __syncwarp();
   }
 
