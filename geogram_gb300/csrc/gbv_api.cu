@@ -296,6 +296,22 @@ __device__ __forceinline__ bool key_less(float ka, uint32_t oa, float kb, uint32
 
 // Cells with extra candidates from the certification: their slots, list
 // rows and counts.
+// FP32 copies of the per-node weight bounds (the certification compares in FP32).
+__global__ void node_bounds_f32_kernel(const double* __restrict__ wmax,
+                                       const double4* __restrict__ lin,
+                                       const double* __restrict__ ex, uint32_t m,
+                                       float* __restrict__ wf, float4* __restrict__ lf,
+                                       float* __restrict__ ef) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  wf[i] = (float)wmax[i];
+  if (lin) {
+    const double4 l = lin[i];
+    lf[i] = make_float4((float)l.x, (float)l.y, (float)l.z, (float)l.w);
+    ef[i] = (float)ex[i];
+  }
+}
+
 __global__ void collect_extra_kernel(const uint32_t* __restrict__ qlist, uint32_t nq,
                                      const uint32_t* __restrict__ extra_cnt,
                                      const int32_t* __restrict__ status,
@@ -494,10 +510,22 @@ struct Pipeline {
   // certification counters (GBV_CERT_STATS in the environment)
   unsigned long long* cert_stats = nullptr;
 
-  void enable_certification(const double* wmax, const double4* lin, const double* ex) {
+  const float* node_wmax_f = nullptr;
+  const float4* node_lin_f = nullptr;
+  const float* node_ex_f = nullptr;
+
+  void enable_certification(const double* wmax, const double4* lin, const double* ex,
+                            uint32_t nodes) {
     node_wmax = wmax;
     node_lin = lin;
     node_ex = ex;
+    float* wf = c->buf<float>("node_wmax_f", nodes);
+    float4* lf = lin ? c->buf<float4>("node_lin_f", nodes) : nullptr;
+    float* ef = lin ? c->buf<float>("node_ex_f", nodes) : nullptr;
+    node_bounds_f32_kernel<<<nblocks(nodes, 256), 256, 0, st>>>(wmax, lin, ex, nodes, wf, lf, ef); count_launch();
+    node_wmax_f = wf;
+    node_lin_f = lf;
+    node_ex_f = ef;
     if (std::getenv("GBV_CERT_STATS")) {
       cert_stats = c->buf<unsigned long long>("cert_stats", 5);
       GBV_CUDA(cudaMemsetAsync(cert_stats, 0, 5 * sizeof(unsigned long long), st));
@@ -590,6 +618,9 @@ struct Pipeline {
       g.node_wmax = node_wmax;
       g.node_lin = node_lin;
       g.node_ex = node_ex;
+      g.node_wmax_f = node_wmax_f;
+      g.node_lin_f = node_lin_f;
+      g.node_ex_f = node_ex_f;
       g.cand_cnt = L.cnt;
       g.extra = extra;
       g.extra_cnt = extra_cnt;
@@ -1069,7 +1100,7 @@ static bool laguerre_device(gbv_context* c, const double* d_xyz, const double* d
   GBV_CUDA(cudaEventRecord(c->ev[1], st));
   // no list cap for seeds with copies (the security-radius loop is not used)
   Pipeline P(c, n, box_min, box_max, fp32, false, n, st);
-  P.enable_certification(wmax, nlin, nex);
+  P.enable_certification(wmax, nlin, nex, node_count(S.L));
   uint32_t K;
   uint32_t* lists;
   uint32_t* cnt = c->buf<uint32_t>("lag_cnt", n);

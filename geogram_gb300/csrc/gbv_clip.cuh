@@ -96,6 +96,10 @@ struct GeomArgs {
   const double* node_wmax;
   const double4* node_lin;    // per-node linear weight bound (a, g) and its excess
   const double* node_ex;      //   (build_node_linear); may be null
+  // the same rounded to FP32 once per call (the walk compares in FP32)
+  const float* node_wmax_f;
+  const float4* node_lin_f;
+  const float* node_ex_f;
   const uint32_t* cand_cnt;   // candidate list lengths, per list row
   uint32_t* extra;
   uint32_t* extra_cnt;

@@ -84,6 +84,7 @@ __device__ __forceinline__ void certify_cell(const GeomArgs& a, const SortedSeed
   const float hf = gd.h_f;
   const uint32_t ncand = a.cand_cnt[row] & kCntMask;
   const double4 pi_d = S.xd[s];
+  const float4 pi_f = S.xf[s];
   uint32_t bj[NCL];
 #pragma unroll
   for (int q = 0; q < NCL; ++q) {
@@ -110,18 +111,18 @@ __device__ __forceinline__ void certify_cell(const GeomArgs& a, const SortedSeed
     const uint32_t en = S.cell_start[(code + 1u) << (3 * shift)];
     if (b == en) continue;
     ++n_nodes;
-    const float WB = (float)a.node_wmax[node_offset(lev) + code];
+    const float WB = a.node_wmax_f[node_offset(lev) + code];
     const float side = hf * (float)(1u << shift);
     const float bx = gd.lo_f[0] + (float)compact3(code) * side;
     const float by = gd.lo_f[1] + (float)compact3(code >> 1) * side;
     const float bz = gd.lo_f[2] + (float)compact3(code >> 2) * side;
     const float pad = 1e-6f * (1.f + fabsf(bx) + fabsf(by) + fabsf(bz)) + 1e-5f * side;
-    const bool have_lin = a.node_lin != nullptr;
-    double4 fl = make_double4(0.0, 0.0, 0.0, 0.0);
-    double fe = 0.0;
+    const bool have_lin = a.node_lin_f != nullptr;
+    float4 fl = make_float4(0.f, 0.f, 0.f, 0.f);
+    float fe = 0.f;
     if (have_lin) {
-      fl = a.node_lin[node_offset(lev) + code];
-      fe = a.node_ex[node_offset(lev) + code];
+      fl = a.node_lin_f[node_offset(lev) + code];
+      fe = a.node_ex_f[node_offset(lev) + code];
     }
     bool ok = true;
 #pragma unroll
@@ -146,13 +147,18 @@ __device__ __forceinline__ void certify_cell(const GeomArgs& a, const SortedSeed
         bool cut = false;
         float jx = 0.f, jy = 0.f, jz = 0.f, wj = 0.f;
         if (j < en && j != s) {
-          const double4 pj = S.xd[j];
+          // the seed rounded to FP32 (the FP64 copy only for a possible copy)
+          const float4 jf = S.xf[j];
+          jx = jf.x;
+          jy = jf.y;
+          jz = jf.z;
+          wj = S.wf ? S.wf[j].x : (S.ws ? (float)S.ws[j] : 0.f);
           // a copy of the seed is no neighbour (delaunay_nn.cpp:126-133)
-          const bool same = pj.x == pi_d.x && pj.y == pi_d.y && pj.z == pi_d.z;
-          jx = (float)pj.x;
-          jy = (float)pj.y;
-          jz = (float)pj.z;
-          wj = S.ws ? (float)S.ws[j] : 0.f;
+          bool same = false;
+          if (jx == pi_f.x && jy == pi_f.y && jz == pi_f.z) {
+            const double4 pj = S.xd[j];
+            same = pj.x == pi_d.x && pj.y == pi_d.y && pj.z == pi_d.z;
+          }
           for (int k = 0; k < ntri && !cut && !same; ++k) {
             const float4 c = cf[k];
             const float dx = c.x - jx, dy = c.y - jy, dz = c.z - jz;
@@ -214,7 +220,7 @@ __device__ __forceinline__ void certify_cell(const GeomArgs& a, const SortedSeed
           const float ex = fmaxf(fmaxf(qx - sx, sx - (qx + cs)), 0.f);
           const float ey = fmaxf(fmaxf(qy - sy, sy - (qy + cs)), 0.f);
           const float ez = fmaxf(fmaxf(qz - sz, sz - (qz + cs)), 0.f);
-          key = ex * ex + ey * ey + ez * ez - (float)a.node_wmax[node_offset(lev + 1) + cc];
+          key = ex * ex + ey * ey + ez * ez - a.node_wmax_f[node_offset(lev + 1) + cc];
         }
       }
       const unsigned lm = __ballot_sync(FULL, live);

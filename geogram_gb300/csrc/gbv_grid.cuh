@@ -84,9 +84,8 @@ void build_node_linear(const SortedSeeds& S, double4* lin, double* ex, double* m
 // margin that only keeps more nodes).
 __device__ __forceinline__ bool linear_bound_clears(float cx, float cy, float cz, float best,
                                                     float bx, float by, float bz, float side,
-                                                    float pad, const double4& fl, double fe) {
-  const float ga = (float)fl.x, gx = (float)fl.y, gy = (float)fl.z, gz = (float)fl.w;
-  const float ge = (float)fe;
+                                                    float pad, const float4& fl, float ge) {
+  const float ga = fl.x, gx = fl.y, gy = fl.z, gz = fl.w;
   const float px = cx + 0.5f * gx, py = cy + 0.5f * gy, pz = cz + 0.5f * gz;
   const float dx = fmaxf(fmaxf(bx - pad - px, px - (bx + side + pad)), 0.f);
   const float dy = fmaxf(fmaxf(by - pad - py, py - (by + side + pad)), 0.f);

@@ -272,10 +272,13 @@ __device__ void certify(const HugeArgs& a, HugeCell& C, uint32_t s, uint32_t row
       const float dz = fmaxf(fmaxf(bz - pad - cz, cz - (bz + side + pad)), 0.f);
       const float d2 = dx * dx + dy * dy + dz * dz;
       if (d2 >= (best + WB) + 1e-5f * (fabsf(best) + fabsf(WB) + d2) + 1e-7f) continue;
-      if (a.node_lin && linear_bound_clears(cx, cy, cz, best, bx, by, bz, side, pad,
-                                            a.node_lin[node_offset(lev) + code],
-                                            a.node_ex[node_offset(lev) + code]))
-        continue;
+      if (a.node_lin) {
+        const double4 l = a.node_lin[node_offset(lev) + code];
+        if (linear_bound_clears(cx, cy, cz, best, bx, by, bz, side, pad,
+                                make_float4((float)l.x, (float)l.y, (float)l.z, (float)l.w),
+                                (float)a.node_ex[node_offset(lev) + code]))
+          continue;
+      }
       if (en - b <= 32u || lev == gd.L) {
         C.seeds += en - b;
         for (uint32_t jn = b; jn < en; ++jn) {
