@@ -52,6 +52,9 @@ struct GeomWarpSmem {
   uint8_t order[P];                      // contributing planes in creation order
   uint8_t tlist[T];                      // used triangle slots, compacted
   float4 cf[T];                          // corners (FP32) and their best power bound
+  float4 stkl[96];                       // per stack entry, read when it is pushed: the
+  uint32_t stkb[96], stke[96];           //   node's linear weight bound, its seed range,
+  float stkw[96], stkx[96];              //   its largest weight and the bound's excess
   uint32_t cbest[T];                     // best seed of each corner (certification)
   uint32_t stk[96];                      // octree traversal stack
   uint32_t owner[P];                     // seed slot of each live plane (kNone: none)
@@ -74,12 +77,14 @@ struct GeomWarpSmem {
 // corners' owners update their bounds.  best(c) starts at pi_i(c) plus an
 // FP32 margin, so a seed that may cut is never missed; a candidate that only
 // looks like a cutter within the margin is not reported.
-template <int T, int P, int NCL>
+template <int T, int P, int NCL, typename Sm>
 __device__ __forceinline__ void certify_cell(const GeomArgs& a, const SortedSeeds& S,
                                              const GridDesc& gd, uint32_t s, uint32_t row,
-                                             int ntri, float4 (&mine)[NCL], float4* cf,
-                                             uint32_t* cbest, uint32_t* stk,
-                                             const uint32_t* owner, int lane) {
+                                             int ntri, float4 (&mine)[NCL], Sm& g, int lane) {
+  float4* cf = g.cf;
+  uint32_t* cbest = g.cbest;
+  uint32_t* stk = g.stk;
+  const uint32_t* owner = g.owner;
   const unsigned FULL = 0xFFFFFFFFu;
   const float hf = gd.h_f;
   const uint32_t ncand = a.cand_cnt[row] & kCntMask;
@@ -96,34 +101,42 @@ __device__ __forceinline__ void certify_cell(const GeomArgs& a, const SortedSeed
   }
   bool overflow = false;
   unsigned long long n_nodes = 0, n_seeds = 0;
+  const bool have_lin = a.node_lin_f != nullptr;
   int sp = 0;
-  if (lane == 0) stk[0] = 0u;
+  if (lane == 0) {
+    stk[0] = 0u;
+    g.stkb[0] = S.cell_start[0];
+    g.stke[0] = S.cell_start[1u << (3 * gd.L)];
+    g.stkw[0] = a.node_wmax_f[node_offset(0)];
+    if (have_lin) {
+      g.stkl[0] = a.node_lin_f[node_offset(0)];
+      g.stkx[0] = a.node_ex_f[node_offset(0)];
+    }
+  }
   sp = 1;
   __syncwarp();
   while (sp > 0) {
     const uint32_t e = stk[sp - 1];
+    const uint32_t b = g.stkb[sp - 1], en = g.stke[sp - 1];
+    const float WB = g.stkw[sp - 1];
+    float4 fl = make_float4(0.f, 0.f, 0.f, 0.f);
+    float fe = 0.f;
+    if (have_lin) {
+      fl = g.stkl[sp - 1];
+      fe = g.stkx[sp - 1];
+    }
     __syncwarp();
     --sp;
     const int lev = (int)(e & 15u);
     const uint32_t code = e >> 4;
     const int shift = gd.L - lev;
-    const uint32_t b = S.cell_start[code << (3 * shift)];
-    const uint32_t en = S.cell_start[(code + 1u) << (3 * shift)];
     if (b == en) continue;
     ++n_nodes;
-    const float WB = a.node_wmax_f[node_offset(lev) + code];
     const float side = hf * (float)(1u << shift);
     const float bx = gd.lo_f[0] + (float)compact3(code) * side;
     const float by = gd.lo_f[1] + (float)compact3(code >> 1) * side;
     const float bz = gd.lo_f[2] + (float)compact3(code >> 2) * side;
     const float pad = 1e-6f * (1.f + fabsf(bx) + fabsf(by) + fabsf(bz)) + 1e-5f * side;
-    const bool have_lin = a.node_lin_f != nullptr;
-    float4 fl = make_float4(0.f, 0.f, 0.f, 0.f);
-    float fe = 0.f;
-    if (have_lin) {
-      fl = a.node_lin_f[node_offset(lev) + code];
-      fe = a.node_ex_f[node_offset(lev) + code];
-    }
     bool ok = true;
 #pragma unroll
     for (int q = 0; q < NCL; ++q) {
@@ -208,10 +221,14 @@ __device__ __forceinline__ void certify_cell(const GeomArgs& a, const SortedSeed
     {
       float key = INFINITY;
       bool live = false;
+      uint32_t cb0 = 0, ce0 = 0;
+      float cw = 0.f;
       if (lane < 8) {
         const uint32_t cc = (code << 3) | (uint32_t)lane;
         const int csh = shift - 1;
-        live = S.cell_start[cc << (3 * csh)] != S.cell_start[(cc + 1u) << (3 * csh)];
+        cb0 = S.cell_start[cc << (3 * csh)];
+        ce0 = S.cell_start[(cc + 1u) << (3 * csh)];
+        live = cb0 != ce0;
         if (live) {
           const float cs = 0.5f * side;
           const float qx = bx + (float)(lane & 1) * cs, qy = by + (float)((lane >> 1) & 1) * cs,
@@ -220,7 +237,8 @@ __device__ __forceinline__ void certify_cell(const GeomArgs& a, const SortedSeed
           const float ex = fmaxf(fmaxf(qx - sx, sx - (qx + cs)), 0.f);
           const float ey = fmaxf(fmaxf(qy - sy, sy - (qy + cs)), 0.f);
           const float ez = fmaxf(fmaxf(qz - sz, sz - (qz + cs)), 0.f);
-          key = ex * ex + ey * ey + ez * ez - a.node_wmax_f[node_offset(lev + 1) + cc];
+          cw = a.node_wmax_f[node_offset(lev + 1) + cc];
+          key = ex * ex + ey * ey + ez * ez - cw;
         }
       }
       const unsigned lm = __ballot_sync(FULL, live);
@@ -231,7 +249,18 @@ __device__ __forceinline__ void certify_cell(const GeomArgs& a, const SortedSeed
         const float kk = __shfl_sync(FULL, key, k);
         if (((lm >> k) & 1u) && (kk > key || (kk == key && k < lane))) ++rank;
       }
-      if (live) stk[sp + rank] = (((code << 3) | (uint32_t)lane) << 4) | (uint32_t)(lev + 1);
+      if (live) {
+        const int at = sp + rank;
+        const uint32_t cc = (code << 3) | (uint32_t)lane;
+        stk[at] = (cc << 4) | (uint32_t)(lev + 1);
+        g.stkb[at] = cb0;
+        g.stke[at] = ce0;
+        g.stkw[at] = cw;
+        if (have_lin) {
+          g.stkl[at] = a.node_lin_f[node_offset(lev + 1) + cc];
+          g.stkx[at] = a.node_ex_f[node_offset(lev + 1) + cc];
+        }
+      }
       __syncwarp();
       sp += __popc(lm);
     }
@@ -427,7 +456,7 @@ __global__ void __launch_bounds__(kGeomWarps * 32) geom_kernel(GeomArgs a) {
     __syncwarp();
     const GridDesc gd = *S.gd;
     const uint32_t row = a.qrow ? a.qrow[ci] : ci;
-    certify_cell<T, P, NCL>(a, S, gd, s, row, ntri, mine, g.cf, g.cbest, g.stk, g.owner, lane);
+    certify_cell<T, P, NCL>(a, S, gd, s, row, ntri, mine, g, lane);
     __syncwarp();
   }
 
