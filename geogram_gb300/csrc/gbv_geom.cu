@@ -55,16 +55,17 @@ struct GeomWarpSmem {
   float4 stkl[96];                       // per stack entry, read when it is pushed: the
   uint32_t stkb[96], stke[96];           //   node's linear weight bound, its seed range,
   float stkw[96], stkx[96];              //   its largest weight and the bound's excess
+  uint32_t cbest[T];                     // best seed of each corner (certification)
   uint32_t stk[96];                      // octree traversal stack
   uint32_t owner[P];                     // seed slot of each live plane (kNone: none)
 };
 
 // Cell-centred certification.  A seed j cuts the cell only if for some
 // corner c its power pi_j(c) = |c - p_j|^2 - w_j is below the seed's own,
-// pi_i(c) = |c - p_i|^2 - w_i.  The warp looks for the seeds below pi_i(c)
-// at some corner c that are not yet in the candidate list and reports them
-// all as extra candidates (among them, for each corner, the seed of least
-// power there, whose Laguerre cell holds c: a neighbour of the final cell).
+// pi_i(c) = |c - p_i|^2 - w_i.  For every corner the warp looks for the
+// seed of least power at c among those below pi_i(c) and not yet in the
+// candidate list -- the seed whose Laguerre cell holds c, hence a neighbour
+// of the final cell -- and reports the distinct ones as extra candidates.
 // Clipping by them and certifying again ends in a few rounds; a round that
 // finds none certifies the cell.
 //
@@ -81,6 +82,7 @@ __device__ __forceinline__ void certify_cell(const GeomArgs& a, const SortedSeed
                                              const GridDesc& gd, uint32_t s, uint32_t row,
                                              int ntri, float4 (&mine)[NCL], Sm& g, int lane) {
   float4* cf = g.cf;
+  uint32_t* cbest = g.cbest;
   uint32_t* stk = g.stk;
   const uint32_t* owner = g.owner;
   const unsigned FULL = 0xFFFFFFFFu;
@@ -88,8 +90,10 @@ __device__ __forceinline__ void certify_cell(const GeomArgs& a, const SortedSeed
   const uint32_t ncand = a.cand_cnt[row] & kCntMask;
   const double4 pi_d = S.xd[s];
   const float4 pi_f = S.xf[s];
+  uint32_t bj[NCL];
 #pragma unroll
   for (int q = 0; q < NCL; ++q) {
+    bj[q] = kNone;
     if (mine[q].w > -INFINITY) {
       mine[q].w += 1e-5f * fabsf(mine[q].w) + 1e-7f;
       cf[lane + 32 * q].w = mine[q].w;
@@ -97,7 +101,6 @@ __device__ __forceinline__ void certify_cell(const GeomArgs& a, const SortedSeed
   }
   bool overflow = false;
   unsigned long long n_nodes = 0, n_seeds = 0;
-  uint32_t found = 0;  // candidates reported (written while scanning)
   const bool have_lin = a.node_lin_f != nullptr;
   int sp = 0;
   if (lane == 0) {
@@ -187,18 +190,12 @@ __device__ __forceinline__ void certify_cell(const GeomArgs& a, const SortedSeed
           }
         }
         unsigned m = __ballot_sync(FULL, cut);
-        // every seed that cuts is a candidate (each seed is scanned once):
-        // reporting them all, not only each corner's best, spares rounds
-        if (cut) {
-          const uint32_t pos = found + __popc(m & ((1u << lane) - 1u));
-          if (pos < a.max_extra) a.extra[(size_t)pos * a.nbr_stride + row] = j;
-        }
-        found += __popc(m);
         while (m) {
           const int src = __ffs(m) - 1;
           m &= m - 1;
           const float sx = __shfl_sync(FULL, jx, src), sy = __shfl_sync(FULL, jy, src),
                       sz = __shfl_sync(FULL, jz, src), sw = __shfl_sync(FULL, wj, src);
+          const uint32_t sj = __shfl_sync(FULL, j, src);
 #pragma unroll
           for (int q = 0; q < NCL; ++q) {
             if (!(mine[q].w > -INFINITY)) continue;
@@ -206,6 +203,7 @@ __device__ __forceinline__ void certify_cell(const GeomArgs& a, const SortedSeed
             const float d = dx * dx + dy * dy + dz * dz - sw;
             if (d < mine[q].w) {
               mine[q].w = d;
+              bj[q] = sj;
               cf[lane + 32 * q].w = d;
             }
           }
@@ -266,6 +264,26 @@ __device__ __forceinline__ void certify_cell(const GeomArgs& a, const SortedSeed
       __syncwarp();
       sp += __popc(lm);
     }
+  }
+  // the distinct best seeds, in corner order
+#pragma unroll
+  for (int q = 0; q < NCL; ++q)
+    if (lane + 32 * q < T) cbest[lane + 32 * q] = (lane + 32 * q < ntri) ? bj[q] : kNone;
+  __syncwarp();
+  uint32_t found = 0;
+#pragma unroll
+  for (int q = 0; q < NCL; ++q) {
+    const int i = lane + 32 * q;
+    const uint32_t v = (i < ntri) ? bj[q] : kNone;
+    bool take = v != kNone;
+    for (int k = 0; k < i && take; ++k)
+      if (cbest[k] == v) take = false;
+    const unsigned m = __ballot_sync(FULL, take);
+    if (take) {
+      const uint32_t pos = found + __popc(m & ((1u << lane) - 1u));
+      if (pos < a.max_extra) a.extra[(size_t)pos * a.nbr_stride + row] = v;
+    }
+    found += __popc(m);
   }
   if (lane == 0) {
     const bool more = overflow || found > a.max_extra;
