@@ -90,10 +90,11 @@ __device__ __forceinline__ void certify_cell(const GeomArgs& a, const SortedSeed
   const uint32_t ncand = a.cand_cnt[row] & kCntMask;
   const double4 pi_d = S.xd[s];
   const float4 pi_f = S.xf[s];
-  uint32_t bj[NCL];
+  uint32_t bj[NCL], bperm[NCL];  // best seed of each corner and its original index
 #pragma unroll
   for (int q = 0; q < NCL; ++q) {
     bj[q] = kNone;
+    bperm[q] = 0;
     if (mine[q].w > -INFINITY) {
       mine[q].w += 1e-5f * fabsf(mine[q].w) + 1e-7f;
       cf[lane + 32 * q].w = mine[q].w;
@@ -159,6 +160,7 @@ __device__ __forceinline__ void certify_cell(const GeomArgs& a, const SortedSeed
         const uint32_t j = base + lane;
         bool cut = false;
         float jx = 0.f, jy = 0.f, jz = 0.f, wj = 0.f;
+        uint32_t jperm = 0;
         if (j < en && j != s) {
           // the seed rounded to FP32 (the FP64 copy only for a possible copy)
           const float4 jf = S.xf[j];
@@ -175,7 +177,10 @@ __device__ __forceinline__ void certify_cell(const GeomArgs& a, const SortedSeed
           for (int k = 0; k < ntri && !cut && !same; ++k) {
             const float4 c = cf[k];
             const float dx = c.x - jx, dy = c.y - jy, dz = c.z - jz;
-            cut = dx * dx + dy * dy + dz * dz - wj < c.w;
+            // <=: a seed tied with a corner's current best is still
+            // considered, and the tie goes to the lower original index below,
+            // so the result does not depend on the scan order of the seeds
+            cut = dx * dx + dy * dy + dz * dz - wj <= c.w;
           }
           if (cut) {
             // already in the candidate list (clipped, cutting or not)?  The
@@ -187,6 +192,7 @@ __device__ __forceinline__ void certify_cell(const GeomArgs& a, const SortedSeed
             if (listed) cut = false;
             for (uint32_t k = 0; k < ncand && cut; ++k)
               if (a.nbr[(size_t)k * a.nbr_stride + row] == j) cut = false;
+            if (cut) jperm = S.perm[j];
           }
         }
         unsigned m = __ballot_sync(FULL, cut);
@@ -196,14 +202,16 @@ __device__ __forceinline__ void certify_cell(const GeomArgs& a, const SortedSeed
           const float sx = __shfl_sync(FULL, jx, src), sy = __shfl_sync(FULL, jy, src),
                       sz = __shfl_sync(FULL, jz, src), sw = __shfl_sync(FULL, wj, src);
           const uint32_t sj = __shfl_sync(FULL, j, src);
+          const uint32_t sperm = __shfl_sync(FULL, jperm, src);
 #pragma unroll
           for (int q = 0; q < NCL; ++q) {
             if (!(mine[q].w > -INFINITY)) continue;
             const float dx = mine[q].x - sx, dy = mine[q].y - sy, dz = mine[q].z - sz;
             const float d = dx * dx + dy * dy + dz * dz - sw;
-            if (d < mine[q].w) {
+            if (d < mine[q].w || (d == mine[q].w && bj[q] != kNone && sperm < bperm[q])) {
               mine[q].w = d;
               bj[q] = sj;
+              bperm[q] = sperm;
               cf[lane + 32 * q].w = d;
             }
           }

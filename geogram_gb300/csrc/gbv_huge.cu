@@ -288,7 +288,9 @@ __device__ void certify(const HugeArgs& a, HugeCell& C, uint32_t s, uint32_t row
           const float wj = S.ws ? (float)S.ws[jn] : 0.f;
           const float ex = cx - (float)pj.x, ey = cy - (float)pj.y, ez = cz - (float)pj.z;
           const float d = ex * ex + ey * ey + ez * ez - wj;
-          if (!(d < best)) continue;
+          // ties with the current best go to the lower original index, so
+          // that the result does not depend on the order of the slots
+          if (!(d < best || (d == best && bj != kNone && S.perm[jn] < S.perm[bj]))) continue;
           bool member = false;
           for (uint32_t k = 0; k < ncand && !member; ++k)
             member = a.nbr[(size_t)k * a.nbr_stride + row] == jn;
