@@ -121,7 +121,7 @@ def cell_options(box=((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)), k0: int = 20, check_sr:
 
 
 def ot_options(box=((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)), tol: float = 1e-6, max_newton: int = 100,
-               max_cg: int = 4000, precision: str | int = "fp32", cg_rtol: float = 1e-3,
+               max_cg: int = 4000, precision: str | int = "fp32", cg_rtol: float = 1e-4,
                step_growth: float = 4.0) -> OtOptions:
     o = OtOptions()
     _lib.load().gbv_ot_options_default(ctypes.byref(o))
@@ -493,7 +493,7 @@ def lloyd_iterations(xyz_dev, iters: int, weights_dev=None, *,
 
 def ot_solve(xyz: np.ndarray, nu: np.ndarray | None = None, w0: np.ndarray | None = None, *,
              box=((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)), tol: float = 1e-6, max_newton: int = 100,
-             max_cg: int = 4000, precision="fp32", cg_rtol: float = 1e-3,
+             max_cg: int = 4000, precision="fp32", cg_rtol: float = 1e-4,
              step_growth: float = 4.0, ctx: Context | None = None
              ) -> tuple[np.ndarray, dict]:
     """Weights of the seeds whose Laguerre cells in the box have volumes nu
@@ -512,7 +512,7 @@ def ot_solve(xyz: np.ndarray, nu: np.ndarray | None = None, w0: np.ndarray | Non
 
 def ot_solve_device(xyz_dev, w_dev, nu_dev=None, *, box=((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)),
                     tol: float = 1e-6, max_newton: int = 100, max_cg: int = 4000,
-                    precision="fp32", cg_rtol: float = 1e-3, step_growth: float = 4.0,
+                    precision="fp32", cg_rtol: float = 1e-4, step_growth: float = 4.0,
                     stream=None, ctx: Context | None = None) -> dict:
     """ot_solve on torch CUDA tensors; w_dev (float64, n) is updated in place."""
     ctx = ctx or default_context()

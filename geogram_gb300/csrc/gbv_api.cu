@@ -1594,7 +1594,7 @@ static void ot_solve(gbv_context* c, const double* xyz, const double* nu_in, uin
     Hessian H = current_hessian(c, xyz, n, st);
     // b = -(vol - nu)
     scale_copy(rr, r, -1.0, n, st);
-    cg_total += pcg(H, rr, o.cg_rtol > 0.0 ? o.cg_rtol : 1e-3);
+    cg_total += pcg(H, rr, o.cg_rtol > 0.0 ? o.cg_rtol : 1e-4);
     ms_lin += now_ms(tl);
     // damped step (Kitagawa-Merigot-Thibert): halve until every cell keeps
     // at least eps0 and the residual drops by (1 - alpha / 2); the first
@@ -2608,7 +2608,7 @@ void gbv_ot_options_default(gbv_ot_options* o) {
   o->max_newton = 100;
   o->max_cg = 4000;
   o->precision = GBV_PRECISION_FP32_RECHECK;
-  o->cg_rtol = 1e-3;
+  o->cg_rtol = 1e-4;
   o->step_growth = 4.0;
 }
 

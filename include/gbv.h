@@ -266,7 +266,9 @@ typedef struct {
     uint32_t max_cg;     /* CG iterations per Newton step (4000) */
     uint32_t precision;  /* gbv_precision of the cell computations */
     uint32_t reserved;
-    /* CG stops at ||r|| <= cg_rtol ||b|| (default and 0: 1e-3) */
+    /* CG stops at ||r|| <= cg_rtol ||b|| (default and 0: 1e-4; measured at
+       1M clustered seeds: 30 Newton steps / 17.4 s against 64 / 23.8 s at
+       1e-3, no gain below 1e-4) */
     double cg_rtol;
     /* the line search of a Newton step starts at min(1, step_growth * the
      * previous step) (default 4); 0: always at 1 */
