@@ -1151,8 +1151,10 @@ static bool laguerre_device(gbv_context* c, const double* d_xyz, const double* d
   if (abort_below > 0.0) P.abort_on_empty = c->buf<unsigned int>("lag_abort", 1);
   for (int round = 0;; ++round) {
     // cells far from their final shape (e.g. next to dense clusters) may
-    // need hundreds of extra candidates: the room per cell doubles each round
-    P.size_extras(std::min<uint32_t>(32u << std::min(round, 6), kHugeV), cur.stride);
+    // need hundreds of extra candidates, a few next to the densest clusters
+    // of 10M seeds tens of thousands: the room per cell doubles each round
+    // (to 65536)
+    P.size_extras(32u << std::min(round, 11), cur.stride);
     if (P.process(cur, ql, nullptr, nq) != 0)
       throw StatusError{GBV_ERR_STATE, "unexpected list exhaustion in Laguerre mode"};
     if (round == 0 && abort_below > 0.0) {
@@ -1190,10 +1192,10 @@ static bool laguerre_device(gbv_context* c, const double* d_xyz, const double* d
     if (std::getenv("GBV_OT_LOG"))
       std::fprintf(stderr, "[ot]   round %d: %u cells with extra candidates (room %u)\n", round, m,
                    P.max_extra);
-    if (round >= 32)
+    if (round >= 48)
       throw StatusError{GBV_ERR_NOT_CONVERGED,
                         "certification did not settle: " + std::to_string(m) +
-                            " cell(s) still found candidates after 32 rounds"};
+                            " cell(s) still found candidates after 48 rounds"};
     const std::string tag = std::to_string(round & 1);
     const uint32_t newk = cur.k + P.max_extra;
     uint32_t* q_s = c->buf<uint32_t>("lag_q" + tag, m);
