@@ -1152,9 +1152,11 @@ static bool laguerre_device(gbv_context* c, const double* d_xyz, const double* d
   for (int round = 0;; ++round) {
     // cells far from their final shape (e.g. next to dense clusters) may
     // need hundreds of extra candidates, a few next to the densest clusters
-    // of 10M seeds tens of thousands: the room per cell doubles each round
-    // (to 65536)
-    P.size_extras(32u << std::min(round, 11), cur.stride);
+    // of 10M seeds tens of thousands: the room per cell doubles each round,
+    // up to 65536 and to 2^28 entries over the round's cells (at least 2048)
+    const uint64_t room_cap = std::max<uint64_t>(kHugeV, (1ull << 28) / std::max<uint32_t>(nq, 1));
+    P.size_extras((uint32_t)std::min<uint64_t>(32ull << std::min(round, 11), room_cap),
+                  cur.stride);
     if (P.process(cur, ql, nullptr, nq) != 0)
       throw StatusError{GBV_ERR_STATE, "unexpected list exhaustion in Laguerre mode"};
     if (round == 0 && abort_below > 0.0) {

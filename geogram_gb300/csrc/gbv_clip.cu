@@ -402,6 +402,15 @@ __global__ void __launch_bounds__(kClipWarps * 32, clip_min_blocks<Real, XF>()) 
     Bits<NWT> valid;
     valid.clear();
     valid.w[0] = 0xFFull;
+    // this lane's slots (t = lane + 32 q) among the valid triangles, bit q
+    auto lane_bits = [&](const Bits<NWT>& b) {
+      uint32_t m = 0;
+#pragma unroll
+      for (int q = 0; q < NS; ++q)
+        m |= (uint32_t)((b.w[q >> 1] >> (lane + 32 * (q & 1))) & 1ull) << q;
+      return m;
+    };
+    uint32_t vm = lane_bits(valid);
     uint64_t pused = 0x3Full;
     int parity = 1;
 
@@ -424,6 +433,9 @@ __global__ void __launch_bounds__(kClipWarps * 32, clip_min_blocks<Real, XF>()) 
       uint32_t bj = 0;
       Plane bP{};
       Real bd = 0, bpa = 0, bbw = 0;
+      // the conflict bound's terms carry the fast predicates' widening
+      // (a power of two: the scaled bound rounds as the unscaled one)
+      const Real wide = a.fast_pred ? (Real)kFastPredWide : (Real)1;
       uint32_t jj0 = 0;
       for (; jj < cnt; ++jj) {
         if (jj == 0 || jj - jj0 == 32) {
@@ -437,8 +449,8 @@ __global__ void __launch_bounds__(kClipWarps * 32, clip_min_blocks<Real, XF>()) 
               bd = a.check_sr ? dist2_exact(sc.pi, pj) : 0.0;
               bP = make_double4(2.0 * __dsub_rn(sc.pi.x, pj.x), 2.0 * __dsub_rn(sc.pi.y, pj.y),
                                 2.0 * __dsub_rn(sc.pi.z, pj.z), __dsub_rn(sc.qi, S.q[j]));
-              bpa = (fabs(bP.x) + fabs(bP.y) + fabs(bP.z)) * 1.0001;
-              bbw = Consts<double>::kDot * fabs(bP.w) * 1.0001;
+              bpa = (fabs(bP.x) + fabs(bP.y) + fabs(bP.z)) * 1.0001 * wide;
+              bbw = Consts<double>::kDot * fabs(bP.w) * 1.0001 * wide;
             } else {
               // d = p_j - p_i from the value/remainder pairs keeps FP32
               // relative accuracy however close the two seeds are
@@ -457,11 +469,11 @@ __global__ void __launch_bounds__(kClipWarps * 32, clip_min_blocks<Real, XF>()) 
               }
               // (-2 d, |d|^2 + w_i - w_j): the bisector in the seed's frame
               bP = make_float4(-2.f * dx, -2.f * dy, -2.f * dz, d2 - dw);
-              bpa = (fabsf(bP.x) + fabsf(bP.y) + fabsf(bP.z)) * 1.0001f;
+              bpa = (fabsf(bP.x) + fabsf(bP.y) + fabsf(bP.z)) * 1.0001f * wide;
               // the reference's own FP64 planes carry a rounding of about
               // 2^-52 (|w_i| + |w_j| + |p_i|^2 + |p_j|^2) in their offset
               const float qmag = fabsf(sc.fw.x) + fabsf(wj) + 2.f * pn + 1.f;
-              bbw = (Consts<float>::kDot * fabsf(bP.w) + 3.5527137e-15f * qmag) * 1.0001f;
+              bbw = (Consts<float>::kDot * fabsf(bP.w) + 3.5527137e-15f * qmag) * 1.0001f * wide;
             }
           }
         }
@@ -488,7 +500,6 @@ __global__ void __launch_bounds__(kClipWarps * 32, clip_min_blocks<Real, XF>()) 
         Pn.z = __shfl_sync(FULL, bP.z, src);
         Pn.w = __shfl_sync(FULL, bP.w, src);
         const Real pa1 = __shfl_sync(FULL, bpa, src), bw = __shfl_sync(FULL, bbw, src);
-        const Real wide = a.fast_pred ? (Real)kFastPredWide : (Real)1;
 
         // ---- conflict scan (triangle_is_in_conflict, convex_cell.cpp:870-912)
         bool cf[NS];
@@ -497,7 +508,7 @@ __global__ void __launch_bounds__(kClipWarps * 32, clip_min_blocks<Real, XF>()) 
         for (int q = 0; q < NS; ++q) {
           const int t = lane + 32 * q;
           cf[q] = false;
-          if (!valid.test(t)) continue;
+          if (!((vm >> q) & 1u)) continue;
           Real cx, cy, cz, eps;
           if constexpr (kFP64) {
             const double2 xy = g.cxy[t];
@@ -515,7 +526,7 @@ __global__ void __launch_bounds__(kClipWarps * 32, clip_min_blocks<Real, XF>()) 
           Real sv;
           if constexpr (kFP64) sv = fma(Pn.z, cz, fma(Pn.y, cy, fma(Pn.x, cx, Pn.w)));
           else sv = fmaf(Pn.z, cz, fmaf(Pn.y, cy, fmaf(Pn.x, cx, Pn.w)));
-          const Real bound = fma(pa1, eps, bw) * wide;
+          const Real bound = fma(pa1, eps, bw);
           bool in_conflict;
           if (sv < -bound) {
             in_conflict = true;
@@ -554,6 +565,7 @@ __global__ void __launch_bounds__(kClipWarps * 32, clip_min_blocks<Real, XF>()) 
         if (!conflict.any()) continue;
         if (conflict.equals(valid)) {  // the whole cell is clipped away
           valid.clear();
+          vm = 0;
           R2 = 0;
           if (a.abort_on_empty) {
             if (lane == 0) atomicExch(a.abort_on_empty, 1u);
@@ -568,7 +580,7 @@ __global__ void __launch_bounds__(kClipWarps * 32, clip_min_blocks<Real, XF>()) 
 #pragma unroll
         for (int q = 0; q < NS; ++q) {
           const int t = lane + 32 * q;
-          if (!valid.test(t) || cf[q]) continue;
+          if (!((vm >> q) & 1u) || cf[q]) continue;
           Real r2;
           if constexpr (kFP64) {
             r2 = g.czr[t].y;
@@ -589,7 +601,7 @@ __global__ void __launch_bounds__(kClipWarps * 32, clip_min_blocks<Real, XF>()) 
 #pragma unroll
           for (int q = 0; q < NS; ++q) {
             const int t = lane + 32 * q;
-            if (!valid.test(t) || cf[q]) continue;
+            if (!((vm >> q) & 1u) || cf[q]) continue;
             const uint32_t v = g.tv[t];
             used |= (1ull << (v & 0xFF)) | (1ull << (v >> 8 & 0xFF)) | (1ull << (v >> 16 & 0xFF));
           }
@@ -709,6 +721,7 @@ __global__ void __launch_bounds__(kClipWarps * 32, clip_min_blocks<Real, XF>()) 
         }
         R2 = fmax(R2, warp_maxf(r2n));
         or_into(valid, lowest_bits(freet, nborder));
+        vm = lane_bits(valid);
         if (lane == 0) n_created += (unsigned)nborder;
         __syncwarp();
       }
