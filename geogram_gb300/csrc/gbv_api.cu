@@ -506,6 +506,7 @@ struct Pipeline {
   unsigned int* abort_on_empty = nullptr;  // first pass stops at an empty cell
   bool aborted = false;
   bool geom32 = false;       // FP32 geometry after FP32 clipping passes
+  bool resume = false;       // clipping continues from the stored polytopes
 
   // certification counters (GBV_CERT_STATS in the environment)
   unsigned long long* cert_stats = nullptr;
@@ -578,6 +579,7 @@ struct Pipeline {
     a.qlist = ql;
     a.qrow = qr;
     a.nq = nq;
+    a.resume = resume ? 1 : 0;
     const bool f32 = (kind == 0 && fp32) || kind == 3 || kind == 4;
     const int shape = (kind == 2 || kind == 3) ? CLIP_LARGE : CLIP_SMALL;
     // the first pass over every cell: its kernel time and counters alone
@@ -1101,6 +1103,11 @@ static bool laguerre_device(gbv_context* c, const double* d_xyz, const double* d
   // no list cap for seeds with copies (the security-radius loop is not used)
   Pipeline P(c, n, box_min, box_max, fp32, false, n, st);
   P.enable_certification(wmax, nlin, nex, node_count(S.L));
+  // a certification round extends lists at their end: its cells continue
+  // from the polytopes of the round before (GBV_CERT_RESUME=0: from the box)
+  const char* rs_env = std::getenv("GBV_CERT_RESUME");
+  P.resume = !(rs_env && rs_env[0] == '0');
+  if (P.resume) GBV_CUDA(cudaMemsetAsync(P.cbase.comb.flags, 0, sizeof(uint32_t) * n, st));
   uint32_t K;
   uint32_t* lists;
   uint32_t* cnt = c->buf<uint32_t>("lag_cnt", n);

@@ -354,6 +354,27 @@ __global__ void __launch_bounds__(kClipWarps * 32, clip_min_blocks<Real, XF>()) 
         return plane_fp64(own, sc.pi, S.q[s], sc.box, S);
       }
     };
+    // FP32 bisector of the seed and seed slot j in the seed's frame,
+    // (-2 d, |d|^2 + w_i - w_j) with d = p_j - p_i taken from the
+    // value/remainder pairs (FP32 relative accuracy however close the two
+    // seeds are); d2h = |d|^2 + (h_j - h_i)^2, wj = w_j.
+    auto seed_plane32 = [&](uint32_t j, float& d2h, float& wj) -> float4 {
+      const float4 jh = S.xf[j], jl = S.xl[j];
+      const float dx = (jh.x - sc.fh.x) + (jl.x - sc.fl.x);
+      const float dy = (jh.y - sc.fh.y) + (jl.y - sc.fl.y);
+      const float dz = (jh.z - sc.fh.z) + (jl.z - sc.fl.z);
+      const float dh = (jh.w - sc.fh.w) + (jl.w - sc.fl.w);
+      const float d2 = dx * dx + dy * dy + dz * dz;
+      d2h = d2 + dh * dh;
+      float dw = 0.f;
+      wj = 0.f;
+      if (S.wf) {
+        const float2 w2 = S.wf[j];
+        dw = (w2.x - sc.fw.x) + (w2.y - sc.fw.y);
+        wj = w2.x;
+      }
+      return make_float4(-2.f * dx, -2.f * dy, -2.f * dz, d2 - dw);
+    };
     // Creates the corner of triangle t from its planes; returns its r2.
     auto make_corner = [&](uint32_t t, const auto& pa, const auto& pb, const auto& pc) -> Real {
       if constexpr (kFP64) {
@@ -436,9 +457,65 @@ __global__ void __launch_bounds__(kClipWarps * 32, clip_min_blocks<Real, XF>()) 
       // the conflict bound's terms carry the fast predicates' widening
       // (a power of two: the scaled bound rounds as the unscaled one)
       const Real wide = a.fast_pred ? (Real)kFastPredWide : (Real)1;
-      uint32_t jj0 = 0;
+      if (a.resume) {
+        // ---- continue from the stored polytope of the list's first `done`
+        // positions (the lists only grow at their end, so clipping on from
+        // there gives the polytope a clipping from the box would give: the
+        // same planes in the same order, each conflict sign exact)
+        const CombBuf& cb = a.comb;
+        const uint32_t fl = cb.flags[s];
+        const uint32_t done = fl >> 8;
+        const ulonglong2 tm = cb.tmask[s];
+        const uint64_t pm = cb.pmask[s];
+        if ((fl & 2u) && done > 0 && done <= cnt && (NWT > 1 || tm.y == 0) &&
+            (P >= 64 || (pm >> (P & 63)) == 0)) {
+          jj = done;
+          parity = (fl & 1u) ? -1 : 1;
+          pused = pm;
+          valid.clear();
+          valid.w[0] = tm.x;
+          if (NWT > 1) valid.w[NWT - 1] = tm.y;
+          const size_t tb = (size_t)s * kTMax, pb = (size_t)s * kPMax;
+          for (int p = lane; p < P; p += 32) {
+            if (!((pm >> p) & 1ull)) continue;
+            const uint16_t rk = cb.prank[pb + p];
+            g.prank[p] = rk;
+            if constexpr (kFP64) {
+              g.pown[p] = cb.pown[pb + p];
+            } else {
+              float d2h, wj;
+              g.pl[p] = (rk == 0xFFFF) ? box_plane_fp32(p, sc)
+                                       : seed_plane32(a.nbr[(size_t)rk * a.nbr_stride + row],
+                                                      d2h, wj);
+            }
+          }
+#pragma unroll
+          for (int q = 0; q < NS; ++q) {
+            const int t = lane + 32 * q;
+            if (!valid.test(t)) continue;
+            g.tv[t] = cb.tv[tb + t];
+            g.ta[t] = cb.ta[tb + t];
+            g.key[t] = cb.key[tb + t];
+          }
+          __syncwarp();
+          Real r2 = 0;
+#pragma unroll
+          for (int q = 0; q < NS; ++q) {
+            const int t = lane + 32 * q;
+            if (!valid.test(t)) continue;
+            const uint32_t v = g.tv[t];
+            r2 = fmax(r2, make_corner(t, plane_of(v & 0xFF), plane_of(v >> 8 & 0xFF),
+                                      plane_of(v >> 16 & 0xFF)));
+          }
+          R2 = warp_maxf(r2);
+          vm = lane_bits(valid);
+          __syncwarp();
+        }
+      }
+      // the first iteration loads a batch (unsigned: jj - jj0 == 32)
+      uint32_t jj0 = jj - 32u;
       for (; jj < cnt; ++jj) {
-        if (jj == 0 || jj - jj0 == 32) {
+        if (jj - jj0 == 32) {
           jj0 = jj;
           const uint32_t pos = jj0 + lane;
           if (pos < cnt) {
@@ -452,23 +529,8 @@ __global__ void __launch_bounds__(kClipWarps * 32, clip_min_blocks<Real, XF>()) 
               bpa = (fabs(bP.x) + fabs(bP.y) + fabs(bP.z)) * 1.0001 * wide;
               bbw = Consts<double>::kDot * fabs(bP.w) * 1.0001 * wide;
             } else {
-              // d = p_j - p_i from the value/remainder pairs keeps FP32
-              // relative accuracy however close the two seeds are
-              const float4 jh = S.xf[j], jl = S.xl[j];
-              const float dx = (jh.x - sc.fh.x) + (jl.x - sc.fl.x);
-              const float dy = (jh.y - sc.fh.y) + (jl.y - sc.fl.y);
-              const float dz = (jh.z - sc.fh.z) + (jl.z - sc.fl.z);
-              const float dh = (jh.w - sc.fh.w) + (jl.w - sc.fl.w);
-              const float d2 = dx * dx + dy * dy + dz * dz;
-              bd = d2 + dh * dh;
-              float dw = 0.f, wj = 0.f;
-              if (S.wf) {
-                const float2 w2 = S.wf[j];
-                dw = (w2.x - sc.fw.x) + (w2.y - sc.fw.y);
-                wj = w2.x;
-              }
-              // (-2 d, |d|^2 + w_i - w_j): the bisector in the seed's frame
-              bP = make_float4(-2.f * dx, -2.f * dy, -2.f * dz, d2 - dw);
+              float wj;
+              bP = seed_plane32(j, bd, wj);
               bpa = (fabsf(bP.x) + fabsf(bP.y) + fabsf(bP.z)) * 1.0001f * wide;
               // the reference's own FP64 planes carry a rounding of about
               // 2^-52 (|w_i| + |w_j| + |p_i|^2 + |p_j|^2) in their offset
@@ -767,7 +829,8 @@ __global__ void __launch_bounds__(kClipWarps * 32, clip_min_blocks<Real, XF>()) 
       if (lane == 0) {
         cb.tmask[s] = make_ulonglong2(valid.w[0], NWT > 1 ? valid.w[NWT - 1] : 0ull);
         cb.pmask[s] = pused;
-        cb.flags[s] = parity < 0 ? 1u : 0u;
+        // parity, and the list positions this polytope has clipped
+        cb.flags[s] = (parity < 0 ? 1u : 0u) | (jj <= 0xFFFFFFu ? 2u | jj << 8 : 0u);
       }
     }
     __syncwarp();  // the record is reused by the warp's next cell

@@ -23,7 +23,8 @@ struct CombBuf {
   uint16_t* prank;  // [n][kPMax] position of the plane's seed in the neighbour list
   ulonglong2* tmask;  // [n] used triangle slots (bits 0-63, 64-127)
   uint64_t* pmask;    // [n] used plane slots
-  uint32_t* flags;    // [n] bit 0: parity is -1
+  uint32_t* flags;    // [n] bit 0: parity is -1; bit 1: bits 8-31 hold the
+                      // number of list positions the polytope has clipped
 };
 
 struct ClipArgs {
@@ -50,6 +51,11 @@ struct ClipArgs {
   // started yet are then skipped (null: off).  An empty cell in this pass
   // is empty for good: a caller that rejects any empty cell stops here.
   unsigned int* abort_on_empty;
+  // nonzero: a cell whose record in `comb` holds the polytope of the first
+  // d <= (its list length) positions of its list continues from there (the
+  // caller keeps the records of earlier passes over the same seeds and
+  // lists that only grew at their end, and clears the flags otherwise)
+  int resume;
 };
 
 enum ClipShape : int { CLIP_SMALL = 0, CLIP_LARGE = 1 };

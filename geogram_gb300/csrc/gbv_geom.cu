@@ -60,23 +60,48 @@ struct GeomWarpSmem {
   uint32_t owner[P];                     // seed slot of each live plane (kNone: none)
 };
 
+// Whether the bisector pj of the cell's seed and another seed may put the
+// corner of planes p0, p1, p2 in conflict: false only when the FP64 corner
+// and its error bound show the corner strictly on the kept side, the test
+// the clipping kernels apply before their exact sign (convex_cell.cpp:
+// 870-912).  Where the bound cannot decide, the answer is "may": the seed
+// is then reported, which costs at most a round.
+__device__ __forceinline__ bool corner_in_conflict(double4 p0, double4 p1, double4 p2, double4 pj) {
+  double x, y, z;
+  float e;
+  corner_fp64(p0, p1, p2, x, y, z, e);
+  const double sv = fma(pj.z, z, fma(pj.y, y, fma(pj.x, x, pj.w)));
+  const double bound = fma((fabs(pj.x) + fabs(pj.y) + fabs(pj.z)) * 1.0001, (double)e,
+                           Consts<double>::kDot * fabs(pj.w) * 1.0001);
+  return !(sv > bound);
+}
+
 // Cell-centred certification.  A seed j cuts the cell only if for some
 // corner c its power pi_j(c) = |c - p_j|^2 - w_j is below the seed's own,
 // pi_i(c) = |c - p_i|^2 - w_i.  For every corner the warp looks for the
-// seed of least power at c among those below pi_i(c) and not yet in the
-// candidate list -- the seed whose Laguerre cell holds c, hence a neighbour
-// of the final cell -- and reports the distinct ones as extra candidates.
-// Clipping by them and certifying again ends in a few rounds; a round that
-// finds none certifies the cell.
+// seed of least power at c among those that may be below pi_i(c) and are
+// not yet in the candidate list -- the seed whose Laguerre cell holds c,
+// hence a neighbour of the final cell -- and reports the distinct ones as
+// extra candidates.  Clipping by them and certifying again ends in a few
+// rounds; a round that finds none certifies the cell.
 //
 // The octree walk is a best-bound search shared by the warp: a node whose
 // seeds all have w <= W_B cannot improve corner c when dist(c, box)^2 - W_B
 // >= best(c), and is skipped when that holds for every corner (each lane
-// tests its own corners).  Leaves are scanned one seed per lane against
-// every corner; each seed that improves a corner is then broadcast and the
-// corners' owners update their bounds.  best(c) starts at pi_i(c) plus an
-// FP32 margin, so a seed that may cut is never missed; a candidate that only
-// looks like a cutter within the margin is not reported.
+// tests its own corners).  best(c) starts at pi_i(c) plus a wide FP32
+// margin.  Leaves are scanned one seed per lane against every corner, in
+// the seed's frame: with c' = c - p_i, q = p_j - p_i and dw = w_j - w_i
+// formed from FP32 value/remainder pairs, d = |c' - q|^2 - dw is pi_j(c) -
+// pi_i(c) + |c'|^2 within 1e-6 (|c'|^2 + |d| + |dw|) (coordinates,
+// squares and the subtraction each round to 2^-24 relative; |c' - q|^2 <=
+// |d| + |dw|), so the test d - 4e-6 (|d| + |dw|) <= |c'|^2 (1 + 4e-6) +
+// 1e-12 (the floor for the FP64 corner's own rounding) never drops a seed
+// that cuts.  Each seed it keeps at some corner and that is not in the list
+// yet is broadcast, and the owners of the corners where it would have the
+// least power check it there in FP64 against the corner's error bound
+// (corner_in_conflict) before keeping it: optimal transport cells lie far
+// from their seeds, so their corners' powers are large next to the gaps
+// between them, and FP32 alone would report many seeds that do not cut.
 template <int T, int P, int NCL, typename Sm>
 __device__ __forceinline__ void certify_cell(const GeomArgs& a, const SortedSeeds& S,
                                              const GridDesc& gd, uint32_t s, uint32_t row,
@@ -89,16 +114,29 @@ __device__ __forceinline__ void certify_cell(const GeomArgs& a, const SortedSeed
   const float hf = gd.h_f;
   const uint32_t ncand = a.cand_cnt[row] & kCntMask;
   const double4 pi_d = S.xd[s];
-  const float4 pi_f = S.xf[s];
+  const float4 pi_f = S.xf[s], pi_l = S.xl[s];
+  const float2 wi_f = S.wf ? S.wf[s] : make_float2(0.f, 0.f);
+  const double qi_d = S.q[s];
+  // the reference's FP64 bisector of the cell's seed and seed slot j
+  auto seed_plane64 = [&](uint32_t j) {
+    const double4 pj = S.xd[j];
+    return make_double4(2.0 * __dsub_rn(pi_d.x, pj.x), 2.0 * __dsub_rn(pi_d.y, pj.y),
+                        2.0 * __dsub_rn(pi_d.z, pj.z), __dsub_rn(qi_d, S.q[j]));
+  };
+  // the FP64 test at compacted corner k (corner_in_conflict)
+  auto cuts_corner = [&](int k, const double4& pj) {
+    const uint32_t v = g.tv[g.tlist[k]];
+    return corner_in_conflict(g.plane[v & 0xFF], g.plane[v >> 8 & 0xFF],
+                              g.plane[v >> 16 & 0xFF], pj);
+  };
   uint32_t bj[NCL], bperm[NCL];  // best seed of each corner and its original index
+  float bd[NCL];                 // its d (seed frame)
 #pragma unroll
   for (int q = 0; q < NCL; ++q) {
     bj[q] = kNone;
     bperm[q] = 0;
-    if (mine[q].w > -INFINITY) {
-      mine[q].w += 1e-5f * fabsf(mine[q].w) + 1e-7f;
-      cf[lane + 32 * q].w = mine[q].w;
-    }
+    bd[q] = INFINITY;
+    if (mine[q].w > -INFINITY) mine[q].w += 1e-5f * fabsf(mine[q].w) + 1e-7f;
   }
   bool overflow = false;
   unsigned long long n_nodes = 0, n_seeds = 0;
@@ -159,33 +197,37 @@ __device__ __forceinline__ void certify_cell(const GeomArgs& a, const SortedSeed
       for (uint32_t base = b; base < en; base += 32) {
         const uint32_t j = base + lane;
         bool cut = false;
-        float jx = 0.f, jy = 0.f, jz = 0.f, wj = 0.f;
+        float jx = 0.f, jy = 0.f, jz = 0.f, dw = 0.f, sj = 0.f;
         uint32_t jperm = 0;
         if (j < en && j != s) {
-          // the seed rounded to FP32 (the FP64 copy only for a possible copy)
-          const float4 jf = S.xf[j];
-          jx = jf.x;
-          jy = jf.y;
-          jz = jf.z;
-          wj = S.wf ? S.wf[j].x : (S.ws ? (float)S.ws[j] : 0.f);
+          // the seed in the cell seed's frame (the FP64 copy only for a
+          // possible copy)
+          const float4 jf = S.xf[j], jl = S.xl[j];
+          jx = (jf.x - pi_f.x) + (jl.x - pi_l.x);
+          jy = (jf.y - pi_f.y) + (jl.y - pi_l.y);
+          jz = (jf.z - pi_f.z) + (jl.z - pi_l.z);
+          if (S.wf) {
+            const float2 w2 = S.wf[j];
+            dw = (w2.x - wi_f.x) + (w2.y - wi_f.y);
+          }
+          // the test's slack for |dw|, with d - 4e-6 |d| folded into the
+          // corner's bound (d >= 0; a negative d passes anyway)
+          sj = 4.1e-6f * fabsf(dw);
           // a copy of the seed is no neighbour (delaunay_nn.cpp:126-133)
           bool same = false;
-          if (jx == pi_f.x && jy == pi_f.y && jz == pi_f.z) {
+          if (jf.x == pi_f.x && jf.y == pi_f.y && jf.z == pi_f.z) {
             const double4 pj = S.xd[j];
             same = pj.x == pi_d.x && pj.y == pi_d.y && pj.z == pi_d.z;
           }
           for (int k = 0; k < ntri && !cut && !same; ++k) {
             const float4 c = cf[k];
             const float dx = c.x - jx, dy = c.y - jy, dz = c.z - jz;
-            // <=: a seed tied with a corner's current best is still
-            // considered, and the tie goes to the lower original index below,
-            // so the result does not depend on the scan order of the seeds
-            cut = dx * dx + dy * dy + dz * dz - wj <= c.w;
+            cut = dx * dx + dy * dy + dz * dz - dw <= c.w + sj;
           }
           if (cut) {
             // already in the candidate list (clipped, cutting or not)?  The
             // seeds of the cell's facets first (shared memory), which are
-            // what a corner's margin meets most; then the whole list
+            // what the corners' bounds meet most; then the whole list
             bool listed = false;
 #pragma unroll
             for (int p = 0; p < P; ++p) listed = listed || owner[p] == j;
@@ -200,19 +242,42 @@ __device__ __forceinline__ void certify_cell(const GeomArgs& a, const SortedSeed
           const int src = __ffs(m) - 1;
           m &= m - 1;
           const float sx = __shfl_sync(FULL, jx, src), sy = __shfl_sync(FULL, jy, src),
-                      sz = __shfl_sync(FULL, jz, src), sw = __shfl_sync(FULL, wj, src);
-          const uint32_t sj = __shfl_sync(FULL, j, src);
+                      sz = __shfl_sync(FULL, jz, src), sw = __shfl_sync(FULL, dw, src),
+                      ss = __shfl_sync(FULL, sj, src);
+          const uint32_t sid = __shfl_sync(FULL, j, src);
           const uint32_t sperm = __shfl_sync(FULL, jperm, src);
+          // this lane's corners where the seed may cut and has the least
+          // power so far (ties to the lower original index: the result does
+          // not depend on the scan order of the seeds)
+          uint32_t need = 0;
+          float dq[NCL];
 #pragma unroll
           for (int q = 0; q < NCL; ++q) {
+            dq[q] = INFINITY;
             if (!(mine[q].w > -INFINITY)) continue;
-            const float dx = mine[q].x - sx, dy = mine[q].y - sy, dz = mine[q].z - sz;
+            const float4 c = cf[lane + 32 * q];
+            const float dx = c.x - sx, dy = c.y - sy, dz = c.z - sz;
             const float d = dx * dx + dy * dy + dz * dz - sw;
-            if (d < mine[q].w || (d == mine[q].w && bj[q] != kNone && sperm < bperm[q])) {
-              mine[q].w = d;
-              bj[q] = sj;
-              bperm[q] = sperm;
-              cf[lane + 32 * q].w = d;
+            dq[q] = d;
+            if (d <= c.w + ss &&
+                (d < bd[q] || (d == bd[q] && bj[q] != kNone && sperm < bperm[q])))
+              need |= 1u << q;
+          }
+          if (need) {
+            const double4 spl = seed_plane64(sid);
+            while (need) {  // one corner at a time: the FP64 test once in the code
+              const int qn = __ffs(need) - 1;
+              need &= need - 1;
+              if (!cuts_corner(lane + 32 * qn, spl)) continue;
+#pragma unroll
+              for (int q = 0; q < NCL; ++q) {
+                if (q != qn) continue;
+                bd[q] = dq[q];
+                bj[q] = sid;
+                bperm[q] = sperm;
+                // the walk's bound, in the global frame (w_i rounded)
+                mine[q].w = fminf(mine[q].w, dq[q] - wi_f.x);
+              }
             }
           }
         }
@@ -456,9 +521,13 @@ __global__ void __launch_bounds__(kGeomWarps * 32) geom_kernel(GeomArgs a) {
       if (i < ntri) {
         const int t = g.tlist[i];
         const double dx = g.px[t] - pi.x, dy = g.py[t] - pi.y, dz = g.pz[t] - pi.z;
-        const float rho = (float)(dx * dx + dy * dy + dz * dz - wi);
-        mine[q] = make_float4((float)g.px[t], (float)g.py[t], (float)g.pz[t], rho);
-        g.cf[i] = mine[q];
+        const double r2 = dx * dx + dy * dy + dz * dz;
+        mine[q] = make_float4((float)g.px[t], (float)g.py[t], (float)g.pz[t], (float)(r2 - wi));
+        // the corner in the seed's frame and the bound on a candidate's
+        // power there (certify_cell)
+        const float lx = (float)dx, ly = (float)dy, lz = (float)dz;
+        const float base = lx * lx + ly * ly + lz * lz;
+        g.cf[i] = make_float4(lx, ly, lz, (base * (1.f + 4e-6f) + 1e-12f) * (1.f + 5e-6f));
       }
     }
     __syncwarp();

@@ -101,6 +101,29 @@ def test_power_range_equals_security_radius_on_voronoi(g):
     assert all(p.keys() == q.keys() for p, q in zip(A, B))
 
 
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_certification_rounds_resume_bit_identical(g, prec, monkeypatch):
+    """Cells to which the range query adds candidates continue from their
+    polytope of the round before; clipping them again from the box
+    (GBV_CERT_RESUME=0) gives the same bits."""
+    rng = np.random.default_rng(12)
+    x = gaussian_mixture(20000, 8, 0.05, rng)
+    w = rng.uniform(-0.01, 0.01, len(x))
+    a = g.compute_cells(x, w, precision=prec, certification="power_range")
+    monkeypatch.setenv("GBV_CERT_RESUME", "0")
+    b = g.compute_cells(x, w, precision=prec, certification="power_range")
+    assert a.report["n_more_k"] > 1000  # rounds with many re-clipped cells
+    for f in ("volume", "mg", "rowptr", "neighbors", "facet_area", "status"):
+        assert np.array_equal(getattr(a, f), getattr(b, f)), f
+    monkeypatch.delenv("GBV_CERT_RESUME")
+    w1, rep1 = g.ot_solve(x, tol=1e-7)
+    monkeypatch.setenv("GBV_CERT_RESUME", "0")
+    w0, rep0 = g.ot_solve(x, tol=1e-7)
+    assert rep1["converged"] == 1 and rep0["converged"] == 1
+    assert np.array_equal(w1, w0)
+    assert rep1["newton_iters"] == rep0["newton_iters"]
+
+
 def test_gradient_and_hessian_vs_oracle(g, ot):
     rng = np.random.default_rng(2)
     x = gaussian_mixture(1200, 6, 0.06, rng)
