@@ -97,11 +97,12 @@ __device__ __forceinline__ bool corner_in_conflict(double4 p0, double4 p1, doubl
 // |d| + |dw|), so the test d - 4e-6 (|d| + |dw|) <= |c'|^2 (1 + 4e-6) +
 // 1e-12 (the floor for the FP64 corner's own rounding) never drops a seed
 // that cuts.  Each seed it keeps at some corner and that is not in the list
-// yet is broadcast, and the owners of the corners where it would have the
-// least power check it there in FP64 against the corner's error bound
-// (corner_in_conflict) before keeping it: optimal transport cells lie far
-// from their seeds, so their corners' powers are large next to the gaps
-// between them, and FP32 alone would report many seeds that do not cut.
+// yet is broadcast; the corners' owners count the seeds that may cut there
+// and keep the least-power one.  After the walk, a corner whose only such
+// seed does not cut in FP64 (the corner against its error bound,
+// corner_in_conflict) reports nothing: optimal transport cells lie far from
+// their seeds, so their corners' powers are large next to the gaps between
+// them, and FP32 alone would report many seeds that do not cut.
 template <int T, int P, int NCL, typename Sm>
 __device__ __forceinline__ void certify_cell(const GeomArgs& a, const SortedSeeds& S,
                                              const GridDesc& gd, uint32_t s, uint32_t row,
@@ -131,6 +132,7 @@ __device__ __forceinline__ void certify_cell(const GeomArgs& a, const SortedSeed
   };
   uint32_t bj[NCL], bperm[NCL];  // best seed of each corner and its original index
   float bd[NCL];                 // its d (seed frame)
+  uint32_t npos = 0;             // per corner (2 bits): seeds that may cut there, 0, 1, 2+
 #pragma unroll
   for (int q = 0; q < NCL; ++q) {
     bj[q] = kNone;
@@ -246,38 +248,22 @@ __device__ __forceinline__ void certify_cell(const GeomArgs& a, const SortedSeed
                       ss = __shfl_sync(FULL, sj, src);
           const uint32_t sid = __shfl_sync(FULL, j, src);
           const uint32_t sperm = __shfl_sync(FULL, jperm, src);
-          // this lane's corners where the seed may cut and has the least
-          // power so far (ties to the lower original index: the result does
-          // not depend on the scan order of the seeds)
-          uint32_t need = 0;
-          float dq[NCL];
 #pragma unroll
           for (int q = 0; q < NCL; ++q) {
-            dq[q] = INFINITY;
             if (!(mine[q].w > -INFINITY)) continue;
             const float4 c = cf[lane + 32 * q];
             const float dx = c.x - sx, dy = c.y - sy, dz = c.z - sz;
             const float d = dx * dx + dy * dy + dz * dz - sw;
-            dq[q] = d;
-            if (d <= c.w + ss &&
-                (d < bd[q] || (d == bd[q] && bj[q] != kNone && sperm < bperm[q])))
-              need |= 1u << q;
-          }
-          if (need) {
-            const double4 spl = seed_plane64(sid);
-            while (need) {  // one corner at a time: the FP64 test once in the code
-              const int qn = __ffs(need) - 1;
-              need &= need - 1;
-              if (!cuts_corner(lane + 32 * qn, spl)) continue;
-#pragma unroll
-              for (int q = 0; q < NCL; ++q) {
-                if (q != qn) continue;
-                bd[q] = dq[q];
-                bj[q] = sid;
-                bperm[q] = sperm;
-                // the walk's bound, in the global frame (w_i rounded)
-                mine[q].w = fminf(mine[q].w, dq[q] - wi_f.x);
-              }
+            if (!(d <= c.w + ss)) continue;  // cannot cut at this corner
+            if (((npos >> (2 * q)) & 3u) < 2u) npos += 1u << (2 * q);
+            // the least power so far (ties to the lower original index: the
+            // result does not depend on the scan order of the seeds)
+            if (d < bd[q] || (d == bd[q] && bj[q] != kNone && sperm < bperm[q])) {
+              bd[q] = d;
+              bj[q] = sid;
+              bperm[q] = sperm;
+              // the walk's bound, in the global frame (w_i rounded)
+              mine[q].w = fminf(mine[q].w, d - wi_f.x);
             }
           }
         }
@@ -336,6 +322,27 @@ __device__ __forceinline__ void certify_cell(const GeomArgs& a, const SortedSeed
       }
       __syncwarp();
       sp += __popc(lm);
+    }
+  }
+  // A corner whose only possible cutter does not cut in FP64 has none.
+  // (With two or more, the least-power one in FP32 is reported as it is:
+  // another may cut.)
+  {
+    uint32_t chk = 0;
+#pragma unroll
+    for (int q = 0; q < NCL; ++q)
+      if (bj[q] != kNone && ((npos >> (2 * q)) & 3u) == 1u) chk |= 1u << q;
+    while (chk) {  // one corner at a time: the FP64 test once in the code
+      const int qn = __ffs(chk) - 1;
+      chk &= chk - 1;
+      uint32_t sid = kNone;
+#pragma unroll
+      for (int q = 0; q < NCL; ++q)
+        if (q == qn) sid = bj[q];
+      if (cuts_corner(lane + 32 * qn, seed_plane64(sid))) continue;
+#pragma unroll
+      for (int q = 0; q < NCL; ++q)
+        if (q == qn) bj[q] = kNone;
     }
   }
   // the distinct best seeds, in corner order
@@ -403,7 +410,9 @@ __device__ __forceinline__ float4 to_f4(const double4& q) {
   return make_float4((float)q.x, (float)q.y, (float)q.z, (float)q.w);
 }
 
-template <int T, int P, bool G32>
+// CERT: the power-range certification (a.node_wmax set); its walk is kept
+// out of the plain kernels, whose registers it would raise.
+template <int T, int P, bool G32, bool CERT>
 __global__ void __launch_bounds__(kGeomWarps * 32) geom_kernel(GeomArgs a) {
   constexpr int NH = (P + 31) / 32;  // planes (and ranks) per lane
   using Sm = GeomWarpSmem<T, P>;
@@ -510,7 +519,7 @@ __global__ void __launch_bounds__(kGeomWarps * 32) geom_kernel(GeomArgs a) {
   __syncwarp();
 
   // ---- cell-centred certification (power range query)
-  if (!G32 && a.node_wmax) {
+  if constexpr (CERT && !G32) {
     constexpr int NCL = (T + 31) / 32;
     const double wi = S.ws ? S.ws[s] : 0.0;
     float4 mine[NCL];
@@ -782,24 +791,28 @@ __global__ void __launch_bounds__(kGeomWarps * 32) geom_kernel(GeomArgs a) {
   if (lane == 0) a.nf[s] = (uint32_t)nfac;
 }
 
-template <int T, int P, bool G32>
+template <int T, int P, bool G32, bool CERT>
 static void launch_geom(const GeomArgs& a, cudaStream_t st) {
   const size_t sh = sizeof(GeomWarpSmem<T, P>) * kGeomWarps;
-  cudaFuncSetAttribute(geom_kernel<T, P, G32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaFuncSetAttribute(geom_kernel<T, P, G32, CERT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)sh);
   const unsigned nb = (a.nq + kGeomWarps - 1) / kGeomWarps;
-  geom_kernel<T, P, G32><<<nb, kGeomWarps * 32, sh, st>>>(a); count_launch();
+  geom_kernel<T, P, G32, CERT><<<nb, kGeomWarps * 32, sh, st>>>(a); count_launch();
   last_launch_error = cudaGetLastError();
 }
 
 void launch_geometry(const GeomArgs& a, cudaStream_t st) {
   if (a.nq == 0) return;
+  const bool large = a.shape == CLIP_LARGE;
   if (a.g32) {
-    if (a.shape == CLIP_LARGE) launch_geom<kLargeT, kLargeP, true>(a, st);
-    else launch_geom<kSmallT, kSmallP, true>(a, st);
+    if (large) launch_geom<kLargeT, kLargeP, true, false>(a, st);
+    else launch_geom<kSmallT, kSmallP, true, false>(a, st);
+  } else if (a.node_wmax) {
+    if (large) launch_geom<kLargeT, kLargeP, false, true>(a, st);
+    else launch_geom<kSmallT, kSmallP, false, true>(a, st);
   } else {
-    if (a.shape == CLIP_LARGE) launch_geom<kLargeT, kLargeP, false>(a, st);
-    else launch_geom<kSmallT, kSmallP, false>(a, st);
+    if (large) launch_geom<kLargeT, kLargeP, false, false>(a, st);
+    else launch_geom<kSmallT, kSmallP, false, false>(a, st);
   }
 }
 
